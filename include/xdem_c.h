@@ -1,0 +1,371 @@
+/*
+ * xdem_c.h -- C-ABI of the GB300 DEM time step.
+ *
+ * Two surfaces:
+ *
+ *  1. Launcher surface.  The functions below carry the names, parameter order
+ *     and data layouts of the xdynamics DEM launchers declared in
+ *     include/xdynamics_parallel/xParallelDEM_decl.cuh:280-424 of the
+ *     reference, so a caller of that header can relink against
+ *     libxdem_gb300.so.  Pointers are DEVICE pointers laid out exactly as the
+ *     reference lays them out: positions double4 (x,y,z,radius), velocities
+ *     double3, Euler parameters double4 (e0..e3), pair lists
+ *     MAX_P2P_COUNT / MAX_P2PL_COUNT / MAX_P2MS_COUNT slots per particle with
+ *     double2 tangential history keyed by the partner id.  Each returns an int
+ *     status (XDEM_OK = 0) instead of void; `reduction` keeps its double
+ *     return and reports errors through xdem_last_status().
+ *
+ *  2. Scene surface (xdem_sim_*).  One handle owns the whole particle state on
+ *     the GPU and runs the step in the order of
+ *     xIntegratorVV::OneStepSimulation (source/xdynamics_simulation/
+ *     xIntegratorVV.cpp:26-63) with fused, sorted-order kernels.  The rigid
+ *     bodies of a host multibody solver exchange one 15-double pose record in
+ *     and one 6-double wrench out per body per step.
+ *
+ * Structs are byte-compatible with the reference (double3 = 3 packed doubles,
+ * 8-byte aligned; uint3 = 3 packed uints).
+ */
+#ifndef XDEM_C_H
+#define XDEM_C_H
+
+#include <stddef.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define XDEM_API __declspec(dllexport)
+#else
+#define XDEM_API __attribute__((visibility("default")))
+#endif
+
+/* Pair-list capacities per particle (decl:13-16). */
+#define MAX_P2P_COUNT 12
+#define MAX_P2PL_COUNT 3
+#define MAX_P2MS_COUNT 5
+/* Size in bytes of the 15-double rigid-body record (decl:18). */
+#define DEVICE_BODY_MEM_SIZE 120
+/* Candidate buffers of the particle-mesh search (impl:1975-1977). */
+#define XDEM_MAX_TRI_CANDIDATES 20
+
+/* Index of each entry of the 15-double body record (decl:20). */
+enum { XDEM_MM = 0, XDEM_PX, XDEM_PY, XDEM_PZ, XDEM_VX, XDEM_VY, XDEM_VZ,
+       XDEM_E0, XDEM_E1, XDEM_E2, XDEM_E3, XDEM_ED0, XDEM_ED1, XDEM_ED2, XDEM_ED3 };
+
+/* Status bits.  A launcher returns the OR of the bits its kernels raised. */
+enum {
+    XDEM_OK = 0,
+    XDEM_ERR_P2P_OVERFLOW  = 1 << 0,  /* > MAX_P2P_COUNT particle contacts   */
+    XDEM_ERR_P2PL_OVERFLOW = 1 << 1,  /* > MAX_P2PL_COUNT plane contacts     */
+    XDEM_ERR_P2MS_OVERFLOW = 1 << 2,  /* > MAX_P2MS_COUNT triangle contacts  */
+    XDEM_ERR_TRI_CANDIDATES = 1 << 3, /* > 20 face/edge/vertex candidates    */
+    XDEM_ERR_NONFINITE     = 1 << 4,  /* NaN/Inf position seen by the hash   */
+    XDEM_ERR_CUDA          = 1 << 8,  /* a CUDA runtime call failed          */
+    XDEM_ERR_ARG           = 1 << 9,  /* invalid argument (null, size, mode) */
+    XDEM_ERR_NOT_SET       = 1 << 10, /* setDEMSymbolicParameter not called  */
+    XDEM_ERR_ALLOC         = 1 << 11  /* device allocation failed            */
+};
+
+typedef struct { double x, y, z; } xdem_double3;
+typedef struct { unsigned int x, y, z; } xdem_uint3;
+
+/* decl:128-150 */
+typedef struct device_dem_parameters {
+    bool rollingCondition;
+    int contact_model;            /* 0 = DHS, 1 = Hertz-Mindlin (no slip) */
+    unsigned int np;
+    unsigned int nmp;
+    unsigned int nCluster;
+    unsigned int nClusterObject;
+    unsigned int nTsdaConnection;
+    unsigned int nTsdaConnectionList;
+    unsigned int nTsdaConnectionBodyData;
+    unsigned int nsphere;
+    unsigned int nplane;
+    unsigned int ncylinder;
+    unsigned int ncell;
+    xdem_uint3 grid_size;         /* each a power of two */
+    double dt;
+    double half2dt;               /* 0.5 dt^2 */
+    double cell_size;
+    double cohesion;
+    xdem_double3 gravity;
+    xdem_double3 world_origin;
+} device_dem_parameters;
+
+/* decl:152-159 */
+typedef struct device_triangle_info {
+    int id;
+    unsigned int tid;
+    xdem_double3 P, Q, R;
+} device_triangle_info;
+
+/* decl:161-174 */
+typedef struct device_plane_info {
+    unsigned int id;
+    double l1, l2;
+    xdem_double3 u1, u2, uw, xw, pa, pb, w2, w3, w4;
+} device_plane_info;
+
+/* decl:230-243; filled in the order of xContact.cpp:308-312 */
+typedef struct device_contact_property {
+    double Ei, Ej;
+    double pri, prj;
+    double Gi, Gj;
+    double rest;
+    double fric;
+    double s_fric;
+    double rfric;
+    double coh;
+    double sratio;
+    double amp;
+} device_contact_property;
+
+/* include/xTypes.h:263 */
+typedef struct xClusterInformation {
+    unsigned int sid, scid, count, neach;
+} xClusterInformation;
+
+/* ------------------------------------------------------------------------ */
+/* Library control                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Stream used by every launcher below (default: the legacy default stream,
+ * as the reference).  `stream` is a cudaStream_t. */
+XDEM_API int xdem_set_stream(void* stream);
+/* Status of the most recent call on this host thread. */
+XDEM_API int xdem_last_status(void);
+/* Clears and returns the accumulated device status word (overflow bits). */
+XDEM_API int xdem_take_device_status(void);
+/* Per-particle body-force partial arrays (np doubles each) written by the
+ * plane and mesh launchers, the role of xContact::deviceBodyForceX..MomentZ
+ * (source/xdynamics_object/xContact.cpp:315-345).  NULL entries make the
+ * library use its own arrays. */
+XDEM_API int xdem_set_body_force_buffers(double* fx, double* fy, double* fz,
+                                         double* mx, double* my, double* mz);
+/* Device pointers of the arrays currently used as the body-force partials. */
+XDEM_API int xdem_get_body_force_buffers(double** out6);
+/* Wrench (fx,fy,fz,mx,my,mz) on the body of the last plane/mesh launch,
+ * summed on the GPU; replaces the six `reduction` calls of
+ * xParticlePlaneContact.cpp:159-168 / xParticleMeshObjectContact.cpp:209-216.
+ * Synchronises the launcher stream. */
+XDEM_API int xdem_last_body_wrench(double out6[6]);
+/* Reference semantics switch: 1 reproduces the reference GPU sphere velocity
+ * kernel, which writes the linear velocity back unchanged (impl:208,218);
+ * 0 (default) applies the velocity-Verlet trapezoid to it as the CPU path and
+ * the cluster kernel do (xIntegratorVV.cpp:143-149, impl:279-284). */
+XDEM_API int xdem_set_velocity_compat(int reproduce_reference_gpu);
+/* Library build string. */
+XDEM_API const char* xdem_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Launcher surface (decl:280-424)                                          */
+/* ------------------------------------------------------------------------ */
+
+/* decl:280, def:16-19 */
+XDEM_API int setDEMSymbolicParameter(device_dem_parameters* h_paras);
+
+/* decl:282, def:36-49 */
+XDEM_API int vv_update_position(double* pos, double* ep, double* vel,
+                                double* ev, double* acc, double* ea,
+                                unsigned int np);
+/* decl:284, def:51-69 */
+XDEM_API int vv_update_velocity(double* vel, double* acc, double* ep,
+                                double* ev, double* ea, double* force,
+                                double* moment, double* mass, double* iner,
+                                unsigned int np);
+/* decl:287, def:71-80 */
+XDEM_API int cu_calculateHashAndIndex(unsigned int* hash, unsigned int* index,
+                                      double* pos, unsigned int sid,
+                                      unsigned int np);
+/* decl:288-290, def:82-91 */
+XDEM_API int cu_calculateHashAndIndexForPolygonSphere(
+    unsigned int* hash, unsigned int* index, unsigned int sid,
+    unsigned int nsphere, double* sphere);
+/* decl:291, def:94-124.  Stable sort of (hash,index) by hash in place, then
+ * cell start (0xffffffff when empty) / end and sorted_index. */
+XDEM_API int cu_reorderDataAndFindCellStart(unsigned int* hash,
+                                            unsigned int* index,
+                                            unsigned int* cstart,
+                                            unsigned int* cend,
+                                            unsigned int* sorted_index,
+                                            unsigned int np,
+                                            unsigned int ncell);
+/* decl:293-299, def:126-143 */
+XDEM_API int cu_calculate_p2p(double* pos, double* ep, double* vel,
+                              double* omega, double* force, double* moment,
+                              double* mass, double* tmax, double* rres,
+                              unsigned int* pair_count, unsigned int* pair_id,
+                              double* tsd, unsigned int* sorted_index,
+                              unsigned int* cstart, unsigned int* cend,
+                              device_contact_property* cp, unsigned int np);
+/* decl:301-308, def:145-184 (one plane per launch; plan->id selects the
+ * slot rule) */
+XDEM_API int cu_plane_contact_force(device_plane_info* plan, double* dbi,
+                                    device_contact_property* cp, double* pos,
+                                    double* ep, double* vel, double* omega,
+                                    double* force, double* moment,
+                                    double* mass, double* tmax, double* rres,
+                                    unsigned int* pair_count,
+                                    unsigned int* pair_id, double* tsd,
+                                    unsigned int np);
+/* decl:316-324, def:238-263 */
+XDEM_API int cu_particle_polygonObject_collision(
+    device_triangle_info* dpi, double* dbi, double* pos, double* ep,
+    double* vel, double* omega, double* force, double* moment, double* mass,
+    double* tmax, double* rres, unsigned int* pair_count,
+    unsigned int* pair_id, double* tsd, double* dsph, unsigned int* sidx,
+    unsigned int* cstart, unsigned int* cend, device_contact_property* cp,
+    unsigned int np, unsigned int ntriangle);
+/* decl:336-343, def:265-283 */
+XDEM_API int cu_decide_rolling_friction_moment(double* tmax, double* rres,
+                                               double* inertia, double* ep,
+                                               double* ev, double* moment,
+                                               unsigned int np);
+/* decl:344, def:285-317.  Sum of np doubles (device) returned to the host. */
+XDEM_API double reduction(double* in, unsigned int np);
+/* decl:345-347, def:319-331 */
+XDEM_API int cu_update_meshObjectData(double* vList, double* sph,
+                                      double* dlocal,
+                                      device_triangle_info* poly, double* dbi,
+                                      unsigned int ntriangle);
+/* decl:349-354, def:333-349 */
+XDEM_API int cu_clusters_contact(double* pos, double* cpos, double* ep,
+                                 double* vel, double* omega, double* force,
+                                 double* moment, double* mass, double* tmax,
+                                 double* rres, unsigned int* pair_count,
+                                 unsigned int* pair_id, double* tsd,
+                                 unsigned int* sorted_index,
+                                 unsigned int* cstart, unsigned int* cend,
+                                 device_contact_property* cp,
+                                 xClusterInformation* xci, unsigned int np);
+/* decl:356-362, def:351-393 */
+XDEM_API int cu_cluster_plane_contact(device_plane_info* plan, double* dbi,
+                                      device_contact_property* cp,
+                                      double* pos, double* cpos, double* ep,
+                                      double* vel, double* omega,
+                                      double* force, double* moment,
+                                      double* mass, double* tmax,
+                                      double* rres, unsigned int* pair_count,
+                                      unsigned int* pair_id, double* tsd,
+                                      xClusterInformation* xci,
+                                      unsigned int np);
+/* decl:373-381, def:422-471 */
+XDEM_API int cu_cluster_meshes_contact(
+    device_triangle_info* dpi, double* dbi, double* pos, double* cpos,
+    double* ep, double* vel, double* ev, double* force, double* moment,
+    device_contact_property* cp, double* mass, double* tmax, double* rres,
+    unsigned int* pair_count, unsigned int* pair_id, double* tsd,
+    unsigned int* sorted_index, unsigned int* cstart, unsigned int* cend,
+    xClusterInformation* xci, unsigned int np, unsigned int ntriangle);
+/* decl:383-391, def:473-493 */
+XDEM_API int cu_decide_cluster_rolling_friction_moment(
+    double* tmax, double* rres, double* inertia, double* ep, double* ev,
+    double* moment, xClusterInformation* xci, unsigned int np);
+/* decl:393-396, def:495-513 */
+XDEM_API int vv_update_cluster_position(double* pos, double* cpos, double* ep,
+                                        double* rloc, double* vel,
+                                        double* acc, double* omega,
+                                        double* alpha,
+                                        xClusterInformation* xci,
+                                        unsigned int np);
+/* decl:398-401, def:515-536 */
+XDEM_API int vv_update_cluster_velocity(double* cpos, double* ep, double* vel,
+                                        double* acc, double* omega,
+                                        double* alpha, double* force,
+                                        double* moment, double* rloc,
+                                        double* mass, double* iner,
+                                        xClusterInformation* xci,
+                                        unsigned int np);
+
+/* ------------------------------------------------------------------------ */
+/* Scene surface: handle API over the fused sorted-order step               */
+/* ------------------------------------------------------------------------ */
+
+enum { XDEM_FP64 = 0, XDEM_MIXED = 1 };
+
+typedef struct xdem_sim xdem_sim;
+
+typedef struct xdem_sim_config {
+    unsigned int np;          /* spheres (cluster members included)          */
+    unsigned int ns;          /* clusters; 0 = free spheres (ns = np)        */
+    int precision;            /* XDEM_FP64 or XDEM_MIXED                     */
+    int contact_model;        /* 0 DHS, 1 Hertz-Mindlin                      */
+    int velocity_compat;      /* see xdem_set_velocity_compat                */
+    double dt;
+    double gravity[3];
+    double world_origin[3];
+    double cell_size;
+    unsigned int grid_size[3];/* powers of two; 128^3 in the reference      */
+} xdem_sim_config;
+
+XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out);
+XDEM_API int xdem_sim_destroy(xdem_sim* sim);
+/* Host arrays, reference layout: pos[np*4], vel/acc[ns*3], ep/ev/ea[ns*4],
+ * mass[ns], inertia[ns*3].  Any pointer but pos/mass/inertia may be NULL
+ * (zero; ep defaults to (1,0,0,0)). */
+XDEM_API int xdem_sim_set_state(xdem_sim* sim, const double* pos,
+                                const double* vel, const double* acc,
+                                const double* ep, const double* ev,
+                                const double* ea, const double* mass,
+                                const double* inertia);
+/* Clusters: cpos[ns*4], xci[nco], rloc[nrloc*3] (host). */
+XDEM_API int xdem_sim_set_clusters(xdem_sim* sim, const double* cpos,
+                                   const xClusterInformation* xci,
+                                   unsigned int nco, const double* rloc,
+                                   unsigned int nrloc);
+XDEM_API int xdem_sim_set_pp_contact(xdem_sim* sim,
+                                     const device_contact_property* cp);
+/* Adds a plane; returns its body index through *body (planes and meshes
+ * share one body numbering). */
+XDEM_API int xdem_sim_add_plane(xdem_sim* sim, const device_plane_info* plane,
+                                const double body[15],
+                                const device_contact_property* cp,
+                                int* body_index);
+/* Adds a triangle mesh.  vlist_local[ntri*9] holds each triangle's P,Q,R in
+ * the body frame (as xParticleMeshObjectContact::define uploads dvList). */
+XDEM_API int xdem_sim_add_mesh(xdem_sim* sim, unsigned int ntri,
+                               const double* vlist_local,
+                               const double body[15],
+                               const device_contact_property* cp,
+                               int* body_index);
+/* Pose exchange with the host solver: new 15-double record (and, for a
+ * plane, its frame) for the next step.  plane may be NULL. */
+XDEM_API int xdem_sim_set_body(xdem_sim* sim, int body_index,
+                               const double body[15],
+                               const device_plane_info* plane);
+/* Advances nsteps steps (no host synchronisation). */
+XDEM_API int xdem_sim_step(xdem_sim* sim, unsigned int nsteps);
+/* Wrench of the last step on a body: (fx,fy,fz,mx,my,mz).  Synchronises. */
+XDEM_API int xdem_sim_body_wrench(xdem_sim* sim, int body_index,
+                                  double out6[6]);
+/* Copies the state back to host arrays (reference layout); NULL skips. */
+XDEM_API int xdem_sim_get_state(xdem_sim* sim, double* pos, double* vel,
+                                double* acc, double* ep, double* ev,
+                                double* ea, double* cpos);
+/* kind: 0 particle-particle, 1 particle-plane, 2 particle-triangle. */
+XDEM_API int xdem_sim_get_pairs(xdem_sim* sim, int kind, unsigned int* count,
+                                unsigned int* ids, double* tsd);
+XDEM_API int xdem_sim_set_pairs(xdem_sim* sim, int kind,
+                                const unsigned int* count,
+                                const unsigned int* ids, const double* tsd);
+/* Kinetic energy (translational + rotational) and stored contact count. */
+XDEM_API int xdem_sim_energy(xdem_sim* sim, double* ke, unsigned int* ncontact);
+/* Status bits accumulated since the last call. */
+XDEM_API int xdem_sim_status(xdem_sim* sim);
+/* Stream the handle's kernels run on (cudaStream_t). */
+XDEM_API int xdem_sim_set_stream(xdem_sim* sim, void* stream);
+/* Kernel timing of the last xdem_sim_step call: number of launches and the
+ * time of the particle-particle contact kernel, in milliseconds, from CUDA
+ * events recorded on the handle's stream when profiling is on. */
+XDEM_API int xdem_sim_set_profiling(xdem_sim* sim, int on);
+XDEM_API int xdem_sim_profile(xdem_sim* sim, unsigned int* launches,
+                              double* contact_ms, unsigned int* contact_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XDEM_C_H */

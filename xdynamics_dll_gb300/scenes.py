@@ -1,0 +1,330 @@
+"""Synthetic DEM scenes in the reference layout (host numpy arrays).
+
+Mass and inertia follow xParticleManager::SetMassAndInertia
+(source/xdynamics_manager/xParticleManager.cpp:1124-1140: m = rho 4/3 pi r^3,
+J = 2/5 m r^2 on each axis) and, for clusters, SetClusterMassAndInertia
+(:1058-1101).  Initial state follows xDiscreteElementMethodSimulation::
+Initialize (source/xdynamics_simulation/xDiscreteElementMethodSimulation.cpp:
+63-80): zero velocities, identity Euler parameters, acceleration (0, g_y, 0).
+All randomness is seeded.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import types as T
+
+G_Y = -9.80665
+
+
+@dataclass
+class Scene:
+    np_: int
+    ns: int
+    pos: np.ndarray            # [np*4]  x, y, z, radius
+    vel: np.ndarray            # [ns*3]
+    acc: np.ndarray            # [ns*3]
+    ep: np.ndarray             # [ns*4]
+    ev: np.ndarray             # [ns*4]
+    ea: np.ndarray             # [ns*4]
+    mass: np.ndarray           # [ns]
+    inertia: np.ndarray        # [ns*3]
+    dt: float
+    cell_size: float
+    grid: tuple = (128, 128, 128)
+    origin: tuple = (-1.0, -1.0, -1.0)
+    gravity: tuple = (0.0, G_Y, 0.0)
+    contact_model: int = 1
+    pp_cp: T.ContactProperty = None
+    planes: list = field(default_factory=list)        # PlaneInfo
+    plane_cp: list = field(default_factory=list)      # ContactProperty
+    plane_body: list = field(default_factory=list)    # 15-double records
+    meshes: list = field(default_factory=list)        # dicts: vlist_local, body, cp
+    cpos: np.ndarray = None    # clusters: [ns*4]
+    xci: np.ndarray = None     # clusters: uint32 [nco*4]
+    rloc: np.ndarray = None    # clusters: [neach*3]
+    name: str = ""
+    note: str = ""
+
+    def params(self):
+        nco = 0 if self.xci is None else self.xci.size // 4
+        return T.make_params(np_=self.np_, dt=self.dt, cell_size=self.cell_size, grid=self.grid,
+                             origin=self.origin, gravity=self.gravity,
+                             contact_model=self.contact_model,
+                             ncluster=self.ns if self.ns != self.np_ else 0, nco=nco,
+                             nplane=len(self.planes))
+
+    def copy(self):
+        import copy
+        return copy.deepcopy(self)
+
+
+def sphere_mass_inertia(r, rho):
+    m = rho * (4.0 / 3.0) * np.pi * r ** 3
+    J = (2.0 / 5.0) * m * r ** 2
+    return m, np.repeat(J, 3).reshape(-1, 3)
+
+
+def _init_state(ns, g_y=G_Y):
+    vel = np.zeros(ns * 3)
+    acc = np.zeros(ns * 3)
+    acc[1::3] = g_y
+    ep = np.zeros(ns * 4)
+    ep[0::4] = 1.0
+    return vel, acc, ep, np.zeros(ns * 4), np.zeros(ns * 4)
+
+
+def default_material(E=1e7, nu=0.3, rest=0.5, fric=0.3, rfric=0.0):
+    return T.make_contact_property(E_i=E, E_j=E, nu_i=nu, nu_j=nu, rest=rest, fric=fric, rfric=rfric)
+
+
+def open_box_planes(x0, x1, y0, y1, z0, z1, first_id=0):
+    """Floor and four walls of an open-top box with normals (u1 x u2) pointing
+    inside, as the reference's plane contact expects (plane frame of
+    xParticlePlaneContact.cpp:96-111)."""
+    P = T.plane_from_points
+    planes = [
+        P(0, (x0, y0, z0), (x0, y0, z1), (x1, y0, z0)),   # floor y = y0, normal +y
+        P(1, (x0, y0, z0), (x0, y1, z0), (x0, y0, z1)),   # wall x = x0, normal +x
+        P(2, (x1, y0, z0), (x1, y0, z1), (x1, y1, z0)),   # wall x = x1, normal -x
+        P(3, (x0, y0, z0), (x1, y0, z0), (x0, y1, z0)),   # wall z = z0, normal +z
+        P(4, (x0, y0, z1), (x0, y1, z1), (x1, y0, z1)),   # wall z = z1, normal -z
+    ]
+    for i, p in enumerate(planes):
+        p.id = first_id + i
+    return planes
+
+
+def jittered_lattice(nx, ny, nz, spacing, origin, jitter, rng):
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    # order: x fastest within a layer, then z, then y (layers stacked upward)
+    pts = np.stack([ix.transpose(1, 2, 0).ravel(), iy.transpose(1, 2, 0).ravel(),
+                    iz.transpose(1, 2, 0).ravel()], axis=1).astype(np.float64)
+    pts = np.asarray(origin, float) + pts * spacing
+    pts += rng.uniform(-jitter, jitter, size=pts.shape)
+    return pts
+
+
+def sphere_drop(n_per_layer_side=41, layers=6, r=1e-3, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3,
+                dt=1e-5, box=0.1, seed=1234, spacing_factor=2.4, wall_height=None):
+    """10,000-sphere drop of the first configuration: jittered cubic lattice
+    (spacing 2.4 r, jitter +-0.1 r), 41 x 41 per layer x 6 layers centred in a
+    0.1 x 0.1 m open box of five planes, cell size 2 r."""
+    rng = np.random.default_rng(seed)
+    sp = spacing_factor * r
+    n = n_per_layer_side
+    width = (n - 1) * sp
+    x0 = -0.5 * width
+    pts = jittered_lattice(n, layers, n, sp, (x0, 2.0 * r + 0.5 * sp, x0), 0.1 * r, rng)
+    N = pts.shape[0]
+    pos = np.zeros((N, 4))
+    pos[:, :3] = pts
+    pos[:, 3] = r
+    m, J = sphere_mass_inertia(np.full(N, r), rho)
+    vel, acc, ep, ev, ea = _init_state(N)
+    h = wall_height if wall_height is not None else max(0.05, pts[:, 1].max() + 4 * r)
+    cp = default_material(E, nu, rest, fric)
+    planes = open_box_planes(-0.5 * box, 0.5 * box, 0.0, h, -0.5 * box, 0.5 * box)
+    return Scene(np_=N, ns=N, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=m,
+                 inertia=J.ravel(), dt=dt, cell_size=2.0 * r, pp_cp=cp, planes=planes,
+                 plane_cp=[cp] * len(planes), plane_body=[T.body_record() for _ in planes],
+                 name="sphere_drop", note=f"{N} spheres r={r}")
+
+
+def pow2_at_least(n):
+    p = 1
+    while p < n:
+        p *= 2
+    return p
+
+
+def dam_break(n_target=1_000_000, r_min=1e-3, r_max=2e-3, rho=2500.0, E=1e7, nu=0.3, rest=0.3, fric=0.4,
+              dt=5e-6, seed=2024, block_x=0.2, block_z=0.4, box=(1.0, 0.4, 0.4), spacing=None,
+              grid="domain"):
+    """Polydisperse dam break of the second configuration: radii U[r_min,
+    r_max], a block at x in [0, block_x] of a box 1 m long, the gate removed
+    at t = 0 (so no gate plane is present).
+
+    The block is a jittered lattice at spacing 2 r_max + 2 jitter + margin so
+    no two spheres overlap at t = 0.  Such a lattice holds fewer spheres per
+    volume than a settled packing, so the block is as tall as n_target needs
+    (about 0.9 m for 1M spheres instead of 0.4 m) and the box walls are raised
+    to match; the box keeps its 1 x 0.4 m footprint.
+
+    grid="domain" sizes a non-wrapping power-of-two grid to the box;
+    grid="reference" keeps the reference's 128^3 wrapping grid.
+    """
+    rng = np.random.default_rng(seed)
+    jit = 0.02 * r_max
+    sp = spacing if spacing is not None else 2.0 * r_max + 2.0 * jit + 0.02 * r_max
+    nx = int(np.floor((block_x - 2 * r_max) / sp)) + 1
+    nz = int(np.floor((block_z - 2 * r_max) / sp)) + 1
+    ny = int(np.ceil(n_target / (nx * nz)))
+    pts = jittered_lattice(nx, ny, nz, sp, (r_max + jit, r_max + jit, r_max + jit), jit, rng)[:n_target]
+    N = pts.shape[0]
+    radii = rng.uniform(r_min, r_max, size=N)
+    pos = np.zeros((N, 4))
+    pos[:, :3] = pts
+    pos[:, 3] = radii
+    m, J = sphere_mass_inertia(radii, rho)
+    vel, acc, ep, ev, ea = _init_state(N)
+    height = max(box[1], pts[:, 1].max() + 2 * r_max)
+    cp = default_material(E, nu, rest, fric)
+    # floor, walls x = 0 and x = box[0], walls z = 0 and z = box[2]
+    planes = open_box_planes(0.0, box[0], 0.0, height + 0.01, 0.0, box[2])
+    cs = 2.0 * r_max
+    if grid == "domain":
+        gx = pow2_at_least(int(np.ceil((box[0] + 0.02) / cs)) + 2)
+        gy = pow2_at_least(int(np.ceil((height + 0.03) / cs)) + 2)
+        gz = pow2_at_least(int(np.ceil((box[2] + 0.02) / cs)) + 2)
+        grid_dims = (gx, gy, gz)
+        origin = (-0.01, -0.01, -0.01)
+    else:
+        grid_dims = (128, 128, 128)
+        origin = (-1.0, -1.0, -1.0)
+    return Scene(np_=N, ns=N, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=m,
+                 inertia=J.ravel(), dt=dt, cell_size=cs, grid=grid_dims, origin=origin, pp_cp=cp,
+                 planes=planes, plane_cp=[cp] * len(planes),
+                 plane_body=[T.body_record() for _ in planes], name="dam_break",
+                 note=f"{N} spheres r~U[{r_min},{r_max}] lattice {nx}x{ny}x{nz} spacing {sp:.5g} "
+                      f"block height {pts[:, 1].max():.3f} m")
+
+
+def random_packed(n, r_min, r_max, box, seed, overlap=0.05, vel_scale=0.05, omega_scale=5.0,
+                  cell_factor=2.0, grid=(128, 128, 128), origin=(-1.0, -1.0, -1.0), rho=2500.0,
+                  E=1e7, nu=0.3, rest=0.5, fric=0.3, dt=1e-5, rfric=0.0, nplanes=5):
+    """Dense random spheres with overlaps, random velocities and spins: a
+    single-step test bed where most spheres have several contacts.  The
+    lattice spacing is chosen so neighbours overlap by up to `overlap` of
+    the radius."""
+    rng = np.random.default_rng(seed)
+    sp = 2.0 * r_max * (1.0 - overlap)
+    side = int(np.ceil(n ** (1.0 / 3.0)))
+    pts = jittered_lattice(side, side, side, sp, (-0.5 * side * sp, r_max, -0.5 * side * sp),
+                           0.15 * r_max, rng)[:n]
+    radii = rng.uniform(r_min, r_max, size=n)
+    pos = np.zeros((n, 4))
+    pos[:, :3] = pts
+    pos[:, 3] = radii
+    m, J = sphere_mass_inertia(radii, rho)
+    vel = rng.normal(0, vel_scale, size=(n, 3)).ravel()
+    acc = np.zeros(n * 3)
+    acc[1::3] = G_Y
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w = rng.normal(0, omega_scale, size=(n, 3))
+    # e_dot = 1/2 G(e)^T omega with G rows of the angular-velocity map (impl:32-41)
+    e0, e1, e2, e3 = q.T
+    G = np.stack([np.stack([-e1, e0, -e3, e2], 1), np.stack([-e2, e3, e0, -e1], 1),
+                  np.stack([-e3, -e2, e1, e0], 1)], 1)  # [n,3,4]
+    ed = 0.5 * np.einsum("nij,ni->nj", G, w)
+    ea = rng.normal(0, 1.0, size=(n, 4)) * 1e-3
+    cp = default_material(E, nu, rest, fric, rfric)
+    lo = pts.min(0) - r_max
+    hi = pts.max(0) + r_max
+    # planes cut through the outer layer so boundary spheres touch them
+    planes = open_box_planes(lo[0] + 0.6 * r_max, hi[0] - 0.6 * r_max, lo[1] + 0.6 * r_max, hi[1] + 0.05,
+                             lo[2] + 0.6 * r_max, hi[2] - 0.6 * r_max)[:nplanes]
+    return Scene(np_=n, ns=n, pos=pos.ravel(), vel=vel, acc=acc, ep=q.ravel(), ev=ed.ravel(),
+                 ea=ea.ravel(), mass=m, inertia=J.ravel(), dt=dt, cell_size=cell_factor * r_max,
+                 grid=grid, origin=origin, pp_cp=cp, planes=planes, plane_cp=[cp] * len(planes),
+                 plane_body=[T.body_record() for _ in planes], name="random_packed")
+
+
+def cluster_bed(ncluster, neach=3, sub_r=2e-3, seed=7, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3,
+                dt=1e-5, spacing_factor=1.0, trough=(1.0, 0.3, 0.15), vel_scale=0.0, grid=(128, 128, 128),
+                origin=(-1.0, -1.0, -1.0), cell_size=None):
+    """Bed of rigid multi-sphere clumps (neach spheres in a row, touching,
+    seeded random orientation) on a jittered lattice in a trough of five
+    planes; cluster table, member offsets and mass/inertia as
+    xParticleManager::SetClusterMassAndInertia (xParticleManager.cpp:
+    1058-1101)."""
+    rng = np.random.default_rng(seed)
+    rloc = np.zeros((neach, 3))
+    rloc[:, 0] = (np.arange(neach) - 0.5 * (neach - 1)) * 2.0 * sub_r * 0.95
+    reach = float(np.abs(rloc[:, 0]).max()) + sub_r
+    sp = 2.0 * reach * spacing_factor + 0.1 * sub_r
+    nx = max(1, int(np.floor((trough[0] - 2 * reach) / sp)) + 1)
+    nz = max(1, int(np.floor((trough[2] - 2 * reach) / sp)) + 1)
+    ny = int(np.ceil(ncluster / (nx * nz)))
+    cent = jittered_lattice(nx, ny, nz, sp, (reach, reach, reach), 0.02 * sub_r, rng)[:ncluster]
+    ns = cent.shape[0]
+    q = rng.normal(size=(ns, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    cpos = np.zeros((ns, 4))
+    cpos[:, :3] = cent
+    cpos[:, 3] = sub_r
+    # member positions = c + A(q) rloc
+    e0, e1, e2, e3 = q.T
+    A = np.empty((ns, 3, 3))
+    A[:, 0] = np.stack([2 * (e0 * e0 + e1 * e1 - 0.5), 2 * (e1 * e2 - e0 * e3), 2 * (e1 * e3 + e0 * e2)], 1)
+    A[:, 1] = np.stack([2 * (e1 * e2 + e0 * e3), 2 * (e0 * e0 + e2 * e2 - 0.5), 2 * (e2 * e3 - e0 * e1)], 1)
+    A[:, 2] = np.stack([2 * (e1 * e3 - e0 * e2), 2 * (e2 * e3 + e0 * e1), 2 * (e0 * e0 + e3 * e3 - 0.5)], 1)
+    mem = cent[:, None, :] + np.einsum("nij,kj->nki", A, rloc)
+    N = ns * neach
+    pos = np.zeros((N, 4))
+    pos[:, :3] = mem.reshape(-1, 3)
+    pos[:, 3] = sub_r
+    m1 = rho * (4.0 / 3.0) * np.pi * sub_r ** 3
+    mass = np.full(ns, m1 * neach)
+    J3 = np.array([m1 * np.sum(rloc[:, 1] ** 2 + rloc[:, 2] ** 2), m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 2] ** 2),
+                   m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 1] ** 2)])
+    # a clump of spheres in a row has no inertia about its axis in this
+    # parallel-axis-only model; give that axis the spheres' own 2/5 m r^2
+    J3 = J3 + (2.0 / 5.0) * m1 * sub_r ** 2 * neach
+    inertia = np.tile(J3, ns)
+    vel, acc, ep, ev, ea = _init_state(ns)
+    ep = q.ravel().copy()
+    if vel_scale:
+        vel = rng.normal(0, vel_scale, size=ns * 3)
+    xci = np.array([0, 0, ns, neach], dtype=np.uint32)
+    height = max(trough[1], cent[:, 1].max() + 2 * reach)
+    cp = default_material(E, nu, rest, fric)
+    planes = open_box_planes(0.0, trough[0], 0.0, height + 0.01, 0.0, trough[2])
+    return Scene(np_=N, ns=ns, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=mass,
+                 inertia=inertia, dt=dt, cell_size=cell_size or 2.0 * sub_r, grid=grid, origin=origin,
+                 pp_cp=cp, planes=planes, plane_cp=[cp] * len(planes),
+                 plane_body=[T.body_record() for _ in planes], cpos=cpos.ravel(), xci=xci,
+                 rloc=rloc.ravel(), name="cluster_bed", note=f"{ns} clusters x {neach}")
+
+
+def uv_sphere_mesh(radius, n_lat, n_lon):
+    """Closed triangle mesh of a sphere (body frame), vertices P,Q,R per
+    triangle as the vertex list xParticleMeshObjectContact::define uploads."""
+    tris = []
+    for i in range(n_lat):
+        t0 = np.pi * i / n_lat
+        t1 = np.pi * (i + 1) / n_lat
+        for j in range(n_lon):
+            p0 = 2 * np.pi * j / n_lon
+            p1 = 2 * np.pi * (j + 1) / n_lon
+
+            def v(t, p):
+                return radius * np.array([np.sin(t) * np.cos(p), np.cos(t), np.sin(t) * np.sin(p)])
+            a, b, c, d = v(t0, p0), v(t1, p0), v(t1, p1), v(t0, p1)
+            if i > 0:
+                tris.append((a, b, d))
+            if i < n_lat - 1:
+                tris.append((b, c, d))
+    return np.array(tris, dtype=np.float64).reshape(-1, 9)
+
+
+def wheel_mesh(radius=0.15, width=0.1, n_around=100, n_width=4):
+    """Closed cylinder (wheel) mesh in its body frame, axis along z: side
+    surface plus two capped discs."""
+    tris = []
+    zs = np.linspace(-0.5 * width, 0.5 * width, n_width + 1)
+    ang = 2 * np.pi * np.arange(n_around + 1) / n_around
+    ring = np.stack([radius * np.cos(ang), radius * np.sin(ang)], 1)
+    for k in range(n_width):
+        for j in range(n_around):
+            a = (*ring[j], zs[k]); b = (*ring[j + 1], zs[k])
+            c = (*ring[j + 1], zs[k + 1]); d = (*ring[j], zs[k + 1])
+            tris.append((a, b, c))
+            tris.append((a, c, d))
+    for z, sgn in ((zs[0], -1), (zs[-1], 1)):
+        for j in range(n_around):
+            o = (0.0, 0.0, z)
+            a = (*ring[j], z); b = (*ring[j + 1], z)
+            tris.append((o, b, a) if sgn < 0 else (o, a, b))
+    return np.array(tris, dtype=np.float64).reshape(-1, 9)
