@@ -1,0 +1,353 @@
+"""Benchmark of the DEM step: particle-steps/s at 1M polydisperse spheres.
+
+Workload (the dam-break configuration): 1,000,000 spheres, radii U[1, 2] mm,
+rho 2500, E 1e7, nu 0.3, restitution 0.3, friction 0.4, Hertz-Mindlin,
+dt 5e-6 s, a block at one end of a 1 x 0.4 m box (floor + 4 walls; the gate
+plane is removed at t = 0), seeded jittered-lattice packing (synthetic data).
+
+A step is one pass of the whole DEM step over all spheres (position update,
+hash, sort, contact, velocity update).  `value` is the mixed-precision path
+(FP32 contact geometry/forces, FP64 state); the plain FP64 path is timed on
+the same scene and reported under "fp64".  Inputs stay resident in HBM; the
+state (0.5 GB) is larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs one independent replica per GPU (launched by torchrun), weak
+scaling, no collective on the data path.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-steps/s at 1M spheres, mixed vs plain FP64 on same GB300; % HBM peak"
+UNIT = "particle-steps/s"
+# Algorithmic bytes per sphere-step of the fused contact kernel: every state
+# array read once (pos 32, vel 24, acc 24, ep 32, ev 32, ea 32, mass 8,
+# inertia 24 = 208) and written once (pos 32, vel 24, acc 24, ep 32, ev 32,
+# ea 32 = 176), the next cell hash + index (8), the pair count (read + write
+# 8) and 40 bytes per stored contact (id 4 + history 16, read + write).  The
+# whole step adds the grid's 28 bytes (sort pass 16, sorted index 4, cell
+# ranges 8): 428 + 40 c.
+B_CONTACT_FIXED = 400.0
+B_STEP_FIXED = 428.0
+B_PER_CONTACT = 40.0
+
+
+def load_peaks():
+    for path in (os.path.join(ROOT, "MEASURED_PEAKS.json"),):
+        if os.path.exists(path):
+            d = json.load(open(path))
+            return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per sphere of the contact kernel from the committed ncu
+    summary (profiles/*contact*.md, line 'dram_bytes_per_sphere: X')."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None, None
+    for f in sorted(os.listdir(pdir)):
+        if "contact" in f and f.endswith(".md"):
+            for line in open(os.path.join(pdir, f)):
+                if line.strip().startswith("dram_bytes_per_sphere_mixed:"):
+                    try:
+                        return float(line.split(":")[1].split()[0]), f
+                    except ValueError:
+                        pass
+    return None, None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-i", str(self.dev), "-lms", "100"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            time.sleep(0.2)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        loaded = [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_scene(n):
+    from xdynamics_dll_gb300 import scenes
+    return scenes.dam_break(n_target=n)
+
+
+def settle(scene, steps, torch):
+    """Untimed, deterministic pre-run: the block settles under gravity behind
+    a gate plane at x = 0.2 m (the dam), then the gate is removed (t = 0 of
+    the dam break).  Returns the scene with the settled state and the pair
+    lists (tangential history) to carry over."""
+    from xdynamics_dll_gb300 import scenes, sim as S, types as T
+    sc = scene.copy()
+    p = sc.pos.reshape(-1, 4)
+    gate_x = float(p[:, 0].max() + p[:, 3].max() + 1e-4)
+    top = float(p[:, 1].max() + 0.01)
+    gate = T.plane_from_points(len(sc.planes), (gate_x, 0.0, 0.0), (gate_x, 0.0, 0.4), (gate_x, top, 0.0))
+    sc.planes = list(sc.planes) + [gate]
+    sc.plane_cp = list(sc.plane_cp) + [sc.plane_cp[0]]
+    sc.plane_body = list(sc.plane_body) + [T.body_record()]
+    sm = S.Sim(sc, precision=T.XDEM_MIXED)
+    sm.step(steps)
+    st = sm.state()
+    pairs = [sm.pairs(k) for k in range(3)]
+    sm.close()
+    out = scene.copy()
+    for k in ("pos", "vel", "acc", "ep", "ev", "ea"):
+        setattr(out, k, st[k])
+    out.pairs = pairs
+    return out
+
+
+def new_sim(scene, precision):
+    from xdynamics_dll_gb300 import sim as S
+    sm = S.Sim(scene, precision=precision)
+    for k, pr in enumerate(getattr(scene, "pairs", []) or []):
+        sm.set_pairs(k, *pr)
+    return sm
+
+
+def run_cpu_baseline(scene, budget_s=15.0, max_steps=40):
+    """The CPU oracle (plain C restatement of the reference kernels, OpenMP
+    over particles) on a bounded sample of the same workload: the full scene
+    for as many steps as fit in `budget_s` seconds after one warm-up step."""
+    import kseq
+    import pyoracle
+    o = pyoracle.Oracle()
+    be = kseq.OracleBackend(o)
+    s = kseq.state_arrays(scene)
+    kseq.sphere_step(be, scene, s, (), compat=0)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        kseq.sphere_step(be, scene, s, (), compat=0)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": scene.np_ * steps / dt, "unit": UNIT, "cores": o.threads(), "kind": "port",
+            "sample": f"{steps} steps of the full {scene.np_}-sphere scene after 1 warm-up step "
+                      f"({dt:.1f} s, oracle/xdem_oracle.c, OpenMP)"}
+
+
+def time_device(sim, torch, steps, stream):
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    sim.step(steps)
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end) / 1e3
+
+
+def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None):
+    sm = new_sim(scene, precision)
+    stream = torch.cuda.Stream(device=dev)
+    sm.L.xdem_sim_set_stream(sm.h, stream.cuda_stream)
+    sm.step(warmup)
+    torch.cuda.synchronize()
+    sm.set_profiling(True)
+    if sampler:
+        with sampler:
+            secs = time_device(sm, torch, steps, stream)
+    else:
+        secs = time_device(sm, torch, steps, stream)
+    launches, contact_ms, contact_n = sm.profile()
+    sm.set_profiling(False)
+    ke, ncontact = sm.energy()
+    st = sm.status()
+    return sm, stream, {"secs": secs, "launches": launches, "contact_ms": contact_ms / max(contact_n, 1),
+                        "contact_launches": contact_n, "ncontact": ncontact, "ke": ke, "status": st}
+
+
+def bench_e2e(sm, scene, torch, steps):
+    """Same metric through the C-ABI with host buffers: each step uploads
+    every body's 15-double pose record and plane frame from pinned host memory
+    (xParticlePlaneContact::update does two such copies per plane per step)
+    and reads back every body's 6-double wrench (the MBD exchange)."""
+    import ctypes as C
+    nb = len(sm.bodies)
+    rec = torch.zeros((nb, 15), dtype=torch.float64).pin_memory()
+    for b in range(nb):
+        rec[b] = torch.from_numpy(np.asarray(scene.plane_body[b], dtype=np.float64))
+    wr = torch.zeros((nb, 6), dtype=torch.float64).pin_memory()
+    planes = scene.planes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for b in range(nb):
+            sm.L.xdem_sim_set_body(sm.h, sm.bodies[b], C.c_void_p(rec[b].data_ptr()), C.byref(planes[b]))
+        sm.step(1)
+        for b in range(nb):
+            sm.L.xdem_sim_body_wrench(sm.h, sm.bodies[b], C.c_void_p(wr[b].data_ptr()))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    from xdynamics_dll_gb300 import types as T
+    h2d = nb * (15 * 8 + C.sizeof(T.PlaneInfo))
+    return {"value": scene.np_ * steps / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": nb * 48,
+            "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--settle", type=int, default=0,
+                    help="untimed GPU settling steps behind a gate before timing (0: time the deterministic "
+                         "initial packing, the same input the reference arm times)")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    warmup = max(3, args.warmup)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        scene = make_scene(args.n)
+        # the reference's own CPU DEM path does not work (plane detection is
+        # stubbed, every pair is applied to every particle); its GPU kernels
+        # restated in C (the oracle) run on the host cores instead
+        cb = run_cpu_baseline(scene, budget_s=min(60.0, 5.0 + 0.5 * args.steps), max_steps=max(args.steps, 1))
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"dam break, {scene.np_} polydisperse spheres r~U[1,2] mm, dt=5e-6 s",
+                       "precision": "f64", "grid": list(scene.grid)},
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from xdynamics_dll_gb300 import build, types as T
+    build.build()
+    scene = make_scene(args.n)
+    if args.settle:
+        scene = settle(scene, args.settle, torch)
+
+    # plain FP64 path, then mixed (the headline), same scene
+    sm64, _, r64 = bench_precision(scene, T.XDEM_FP64, args.steps, warmup, torch, local)
+    sm64.close()
+    sampler = ClockSampler(local)
+    smx, stream, rmx = bench_precision(scene, T.XDEM_MIXED, args.steps, warmup, torch, local, sampler)
+    clocks = sampler.summary()
+    e2e = bench_e2e(smx, scene, torch, min(args.steps, 200))
+    smx.close()
+
+    secs64, secsx = r64["secs"], rmx["secs"]
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([secs64, secsx, 1.0 / e2e["value"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs64, secsx, inv_e2e = t.tolist()
+        e2e["value"] = ws / inv_e2e
+    n = scene.np_
+    value = ws * n * args.steps / secsx
+    value64 = ws * n * args.steps / secs64
+    if rank != 0:
+        return
+
+    cbar = rmx["ncontact"] / n
+    peak, peak_kind = load_peaks()
+    b_contact = (B_CONTACT_FIXED + B_PER_CONTACT * cbar) * n
+    achieved = b_contact / (rmx["contact_ms"] * 1e-3) / 1e9
+    traffic_per_sphere, tfile = profile_traffic()
+    roof = {"bound": "hbm", "kernel": "k_fused_contact<float> (mixed)", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": traffic_per_sphere * n if traffic_per_sphere else None,
+            "algorithmic_bytes_per_launch": b_contact,
+            "contact_kernel_ms": rmx["contact_ms"], "traffic_source": tfile}
+    step_bw = (B_STEP_FIXED + B_PER_CONTACT * cbar) * n / (secsx / args.steps) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": warmup,
+        "ms_per_step": 1e3 * secsx / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 contact / f64 state (mixed)", "data": "synthetic",
+        "config": {"workload": f"dam break, {n} polydisperse spheres r~U[1,2] mm, dt=5e-6 s, 5 planes",
+                   "precision": "mixed", "grid": list(scene.grid), "cell_size": scene.cell_size,
+                   "l2": "inputs larger than L2 (about 0.5 GB of state), no flush", "replicas": ws,
+                   "parallelism": f"replicas{ws}"},
+        "fp64": {"value": value64, "ms_per_step": 1e3 * secs64 / args.steps, "contact_kernel_ms": r64["contact_ms"],
+                 "mixed_over_fp64": value / value64},
+        "contacts_per_sphere": cbar,
+        "step_hbm": {"achieved": step_bw, "peak": peak, "frac": step_bw / peak, "unit": "GB/s",
+                     "bytes_per_sphere": B_STEP_FIXED + B_PER_CONTACT * cbar},
+        "roofline": roof,
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": rmx["launches"],
+        "status": {"fp64": r64["status"], "mixed": rmx["status"]},
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = run_cpu_baseline(scene)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

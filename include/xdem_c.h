@@ -299,6 +299,9 @@ typedef struct xdem_sim_config {
     double world_origin[3];
     double cell_size;
     unsigned int grid_size[3];/* powers of two; 128^3 in the reference      */
+    int launcher_path;        /* 1: run the launcher kernels in the order of
+                                 xIntegratorVV (reference structure); 0: the
+                                 fused sorted-order step (default)           */
 } xdem_sim_config;
 
 XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out);
@@ -331,6 +334,11 @@ XDEM_API int xdem_sim_add_mesh(xdem_sim* sim, unsigned int ntri,
                                const double body[15],
                                const device_contact_property* cp,
                                int* body_index);
+/* Triangles (current pose) and bounding spheres of a mesh body, host
+ * arrays of ntri entries / ntri*4 doubles. */
+XDEM_API int xdem_sim_get_mesh(xdem_sim* sim, int body_index,
+                               device_triangle_info* tri, double* sphere,
+                               unsigned int* ntri);
 /* Pose exchange with the host solver: new 15-double record (and, for a
  * plane, its frame) for the next step.  plane may be NULL. */
 XDEM_API int xdem_sim_set_body(xdem_sim* sim, int body_index,

@@ -1,0 +1,147 @@
+// xdem_fused.h -- host interface of the fused, sorted-order DEM step.
+//
+// One step = [hash of mesh spheres] -> clear last step's cells -> radix sort
+// of (cell, id) -> reorder (cell ranges + a cell-sorted snapshot of position,
+// velocity, spin and mass) -> one contact kernel per sorted particle that
+// does particle-particle, plane and mesh contact, rolling resistance, the
+// velocity update, the next position update and the next hash -> per-body
+// wrench sums.  The contact kernel reads only the snapshot for neighbours, so
+// it updates the particle's own state in place without racing other threads.
+//
+// Position and Euler parameters are double-buffered (the step writes the next
+// positions into the other buffer); particle-particle pair lists are
+// double-buffered (old list read, new list written).  Swapping pointers after
+// each step costs nothing.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/xdem_c.h"
+
+namespace xdem {
+
+struct mat_pair;
+constexpr unsigned int kMaxFusedMeshes = 8;
+constexpr unsigned int kMaxFusedBodies = 64;
+constexpr unsigned int kBboxBlocks = 1024;
+
+struct FusedState {
+    bool mixed = false;
+    bool primed = false;       // next positions + keys hold the next step's input
+    bool have_prev = false;    // skey_prev lists the occupied cells of the last step
+    unsigned int np = 0, nentry = 0;
+    double* pos_alt = nullptr;  // [np*4] other position buffer
+    double* ep_alt = nullptr;   // [np*4] other Euler-parameter buffer
+    double* snap_pos = nullptr; // [nentry*4] x, y, z, r (sorted order)
+    double* snap_vel = nullptr; // [nentry*4] vx, vy, vz, mass
+    double* snap_om = nullptr;  // [nentry*4] wx, wy, wz, 0
+    float* snap_f = nullptr;    // [nentry*4] x-c, y-c, z-c, r (FP32 prefilter)
+    unsigned int* pp_count2 = nullptr;
+    unsigned int* pp_id2 = nullptr;
+    double* pp_tsd2 = nullptr;
+    unsigned int* skey_prev = nullptr;  // [nentry] sorted keys of the last step
+    double* d_energy = nullptr;
+    double* d_bbox = nullptr;        // [kBboxBlocks * 6] block min/max of positions
+    double frame_c[3] = {0, 0, 0};  // centre of the FP32 prefilter frame
+    double frame_far2 = 0.0;        // squared radius beyond which FP32 is not trusted
+    float frame_margin = 0.f;       // prefilter slack for FP32 rounding
+    const device_plane_info* planes = nullptr;
+    unsigned int nplane = 0;
+    const double* body = nullptr;
+    const mat_pair* mp = nullptr;
+};
+
+struct FusedArgs {
+    device_dem_parameters prm;
+    unsigned int np, nentry;
+    size_t ncell;
+    int sort_bits;
+    int vel_compat;
+    // state: pos/ep are swapped with the alternate buffers by fused_step
+    double** pos;
+    double** ep;
+    double *vel, *acc, *ev, *ea, *mass, *inertia, *tmax, *rres;
+    unsigned int *k0, *v0, *k1, *v1, *hist, *cstart, *cend, *sorted_index;
+    bool has_pp;
+    unsigned int** pp_count;
+    unsigned int** pp_id;
+    double** pp_tsd;
+    unsigned int *pl_count, *pl_id;
+    double* pl_tsd;
+    unsigned int nplane, nbody, nmesh;
+    unsigned int mesh_first[kMaxFusedMeshes], mesh_ntri[kMaxFusedMeshes];
+    int mesh_body[kMaxFusedMeshes];
+    const device_triangle_info* tri;
+    const double* tri_sphere;
+    unsigned int *ms_count, *ms_id;
+    double* ms_tsd;
+    const double* body;
+    const mat_pair* mp;
+    double *bsums, *wrench;
+    unsigned int* status;
+};
+
+int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st);
+void fused_free(FusedState& fs);
+void fused_invalidate(FusedState& fs);
+int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
+                     const mat_pair* mp);
+// Runs one step.  When e0/e1 are given they bracket the contact kernel.
+int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
+               unsigned int* nlaunch);
+// Kinetic energy (translational + rotational) and number of stored contacts.
+int fused_energy(FusedState& fs, const double* vel, const double* ep, const double* ev, const double* mass,
+                 const double* inertia, unsigned int ns, const unsigned int* c0, const unsigned int* c1,
+                 const unsigned int* c2, unsigned int np, double* ke, unsigned int* ncontact, cudaStream_t st);
+
+// Contact kernels (one translation unit per arithmetic type).
+struct ContactLaunch {
+    device_dem_parameters prm;
+    unsigned int np, nentry;
+    int vel_compat;
+    const double* snap_pos;
+    const double* snap_vel;
+    const double* snap_om;
+    const float* snap_f;
+    float margin;
+    const unsigned int* sorted_index;
+    const unsigned int* cstart;
+    const unsigned int* cend;
+    const unsigned int* skey;
+    // state (original order)
+    const double* pos_cur;  // x_{n+1} (this step's positions)
+    double* pos_next;       // x_{n+2} out
+    const double* ep_cur;
+    double* ep_next;
+    double *vel, *acc, *ev, *ea;
+    const double *mass, *inertia;
+    unsigned int *k_out, *v_out;
+    // contacts
+    bool has_pp;
+    const unsigned int* pp_count_old;
+    const unsigned int* pp_id_old;
+    const double* pp_tsd_old;
+    unsigned int* pp_count_new;
+    unsigned int* pp_id_new;
+    double* pp_tsd_new;
+    const device_plane_info* planes;
+    unsigned int nplane, nmesh;
+    unsigned int mesh_first[kMaxFusedMeshes], mesh_ntri[kMaxFusedMeshes];
+    int mesh_body[kMaxFusedMeshes];
+    unsigned int *pl_count, *pl_id;
+    double* pl_tsd;
+    const device_triangle_info* tri;
+    unsigned int *ms_count, *ms_id;
+    double* ms_tsd;
+    const double* body;
+    const mat_pair* mp;
+    double* bsums;  // [nbody][nblocks][6]
+    unsigned int nblocks;
+    unsigned int* status;
+};
+
+cudaError_t launch_fused_contact_fp64(const ContactLaunch& c, cudaStream_t st);
+cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st);
+constexpr int kFusedThreads = 128;
+
+}  // namespace xdem

@@ -1,0 +1,340 @@
+// xdem_fused_host.cu -- driver of the fused sorted-order step and its
+// small kernels (prologue, reorder + snapshot, per-body wrench sums, energy).
+// Compiled with -fmad=false like the other FP64 units: the prologue's
+// position update and hash round exactly as impl:135-147 / 290-302 do in the
+// CPU oracle.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "xdem_device.cuh"
+#include "xdem_fused.h"
+#include "xdem_kernels.h"
+
+namespace xdem {
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(T*& p, size_t n)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    return cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T));
+}
+
+// Position update of the first step (impl:135-147) into the alternate
+// buffers, and the cell hash of the new position (impl:290-302).
+__global__ void k_prologue(device_dem_parameters p, const double* pos, const double* ep, const double* vel,
+                           const double* ev, const double* acc, const double* ea, double* pos_next,
+                           double* ep_next, unsigned int* key, unsigned int* val, unsigned int n,
+                           unsigned int* status)
+{
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = p.dt, h = p.half2dt;
+    const d4 e = (ld4(ep, i) + dt * ld4(ev, i)) + h * ld4(ea, i);
+    const double l = sqrt(dot(e, e));
+    st4(ep_next, i, mk4(e.x / l, e.y / l, e.z / l, e.w / l));
+    const d3 d = dt * ld3(vel, i) + h * ld3(acc, i);
+    const d4 q = ld4(pos, i);
+    const d3 x = mk3(q.x + d.x, q.y + d.y, q.z + d.z);
+    st4(pos_next, i, mk4(x.x, x.y, x.z, q.w));
+    if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(status, (unsigned int)XDEM_ERR_NONFINITE);
+    const int3v g = grid_pos(p, x);
+    key[i] = grid_hash(p, g.x, g.y, g.z);
+    val[i] = i;
+}
+
+// Bounding box of the positions: block min/max into out[block*6].
+__global__ void k_bbox(const double* pos, unsigned int n, double* out)
+{
+    __shared__ double sm[6][32];
+    double v[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const d3 q = ld4xyz(pos, i);
+        if (!(isfinite(q.x) && isfinite(q.y) && isfinite(q.z))) continue;
+        v[0] = fmin(v[0], q.x); v[1] = fmin(v[1], q.y); v[2] = fmin(v[2], q.z);
+        v[3] = fmax(v[3], q.x); v[4] = fmax(v[4], q.y); v[5] = fmax(v[5], q.z);
+    }
+    for (int c = 0; c < 6; ++c)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w = __shfl_down_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? fmin(v[c], w) : fmax(v[c], w);
+        }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int c = 0; c < 6; ++c) sm[c][warp] = v[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            for (int c = 0; c < 6; ++c) v[c] = c < 3 ? fmin(v[c], sm[c][w]) : fmax(v[c], sm[c][w]);
+        for (int c = 0; c < 6; ++c) out[blockIdx.x * 6 + c] = v[c];
+    }
+}
+
+// Cell ranges of the sorted keys (impl:317-360) and the sorted snapshot the
+// contact kernel reads its neighbours from.
+__global__ void k_reorder(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
+                          unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index, unsigned int* skey,
+                          const double* pos, const double* ep, const double* vel, const double* ev,
+                          const double* mass, double* snap_pos, double* snap_vel, double* snap_om, float* snap_f,
+                          double cx, double cy, double cz, double far2)
+{
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const unsigned int k = sk[s];
+    const unsigned int prev = s ? sk[s - 1] : 0u;
+    if (s == 0 || k != prev) {
+        cstart[k] = s;
+        if (s > 0) cend[prev] = s;
+    }
+    if (s == n - 1) cend[k] = s + 1;
+    const unsigned int oid = sv[s];
+    sorted_index[s] = oid;
+    skey[s] = k;
+    float4 f = make_float4(0.f, 0.f, 0.f, -1.f);
+    if (oid < np) {
+        const d4 x = ld4(pos, oid);
+        const d3 v = ld3(vel, oid);
+        const d3 w = ang_vel(ld4(ep, oid), ld4(ev, oid));
+        st4(snap_pos, s, x);
+        st4(snap_vel, s, mk4(v.x, v.y, v.z, mass[oid]));
+        st4(snap_om, s, mk4(w.x, w.y, w.z, 0.0));
+        const double dx = x.x - cx, dy = x.y - cy, dz = x.z - cz;
+        if (dx * dx + dy * dy + dz * dz < far2)
+            f = make_float4((float)dx, (float)dy, (float)dz, (float)x.w);
+    }
+    reinterpret_cast<float4*>(snap_f)[s] = f;
+}
+
+__global__ void k_body_sums(const double* bsums, unsigned int nblocks, unsigned int nbody, double* wrench)
+{
+    // one warp per (body, component)
+    const unsigned int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const unsigned int lane = threadIdx.x & 31;
+    if (w >= nbody * 6) return;
+    const unsigned int b = w / 6, c = w % 6;
+    double s = 0.0;
+    for (unsigned int i = lane; i < nblocks; i += 32) s += bsums[((size_t)b * nblocks + i) * 6 + c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) wrench[b * 6 + c] = s;
+}
+
+__global__ void k_energy(const double* vel, const double* ep, const double* ev, const double* mass,
+                         const double* inertia, unsigned int ns, const unsigned int* c0, const unsigned int* c1,
+                         const unsigned int* c2, unsigned int np, double* out_ke, unsigned int* out_c)
+{
+    double ke = 0.0;
+    unsigned int cnt = 0;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        const d3 v = ld3(vel, i);
+        const d4 e = ld4(ep, i), d = ld4(ev, i);
+        // body-frame angular velocity 2 L(e) e_dot (L rows of impl:77-79)
+        const double w0 = 2.0 * (-e.y * d.x + e.x * d.y + e.w * d.z - e.z * d.w);
+        const double w1 = 2.0 * (-e.z * d.x - e.w * d.y + e.x * d.z + e.y * d.w);
+        const double w2 = 2.0 * (-e.w * d.x + e.z * d.y - e.y * d.z + e.x * d.w);
+        const d3 J = ld3(inertia, i);
+        ke += 0.5 * mass[i] * dot(v, v) + 0.5 * (J.x * w0 * w0 + J.y * w1 * w1 + J.z * w2 * w2);
+    }
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+        cnt += c0[i] + c1[i] + c2[i];
+    for (int o = 16; o > 0; o >>= 1) {
+        ke += __shfl_down_sync(0xffffffffu, ke, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out_ke, ke);
+        atomicAdd(out_c, cnt);
+    }
+}
+
+}  // namespace
+
+int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st)
+{
+    fs.mixed = mixed;
+    fs.np = np;
+    fs.nentry = nentry;
+    cudaError_t e = dalloc(fs.pos_alt, (size_t)np * 4);
+    if (e == cudaSuccess) e = dalloc(fs.ep_alt, (size_t)np * 4);
+    if (e == cudaSuccess) e = dalloc(fs.snap_pos, (size_t)nentry * 4);
+    if (e == cudaSuccess) e = dalloc(fs.snap_vel, (size_t)nentry * 4);
+    if (e == cudaSuccess) e = dalloc(fs.snap_om, (size_t)nentry * 4);
+    if (e == cudaSuccess) e = dalloc(fs.snap_f, (size_t)nentry * 4);
+    if (e == cudaSuccess) e = dalloc(fs.pp_count2, np);
+    if (e == cudaSuccess) e = dalloc(fs.pp_id2, (size_t)np * MAX_P2P_COUNT);
+    if (e == cudaSuccess) e = dalloc(fs.pp_tsd2, (size_t)np * MAX_P2P_COUNT * 2);
+    if (e == cudaSuccess) e = dalloc(fs.skey_prev, nentry);
+    if (e == cudaSuccess) e = dalloc(fs.d_energy, 2);
+    if (e == cudaSuccess) e = dalloc(fs.d_bbox, (size_t)kBboxBlocks * 6);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fs.pp_count2, 0, np * sizeof(unsigned int), st);
+    fs.primed = false;
+    fs.have_prev = false;
+    return e == cudaSuccess ? XDEM_OK : XDEM_ERR_ALLOC;
+}
+
+void fused_free(FusedState& fs)
+{
+    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.pp_count2,
+                  fs.pp_id2, fs.pp_tsd2, fs.skey_prev, fs.d_energy, fs.d_bbox};
+    for (void* q : ps)
+        if (q) cudaFree(q);
+    fs = FusedState{};
+}
+
+void fused_invalidate(FusedState& fs) { fs.primed = false; }
+
+int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
+                     const mat_pair* mp)
+{
+    fs.planes = planes;
+    fs.nplane = nplane;
+    fs.body = body;
+    fs.mp = mp;
+    return XDEM_OK;
+}
+
+int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, unsigned int* nlaunch)
+{
+    cudaError_t e = cudaSuccess;
+    unsigned int nl = 0;
+    auto ok = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+        nl++;
+    };
+    const unsigned int np = a.np, n = a.nentry;
+    if (!fs.primed) {
+        // empty cell table, first position update + hash, and the frame of
+        // the FP32 prefilter (centre and radius of the particle cloud)
+        ok(launch_fill_u32(a.cstart, 0xffffffffu, a.ncell, st));
+        ok(cudaMemsetAsync(a.cend, 0, a.ncell * sizeof(unsigned int), st));
+        fs.have_prev = false;
+        k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, fs.pos_alt,
+                                                        fs.ep_alt, a.k0, a.v0, np, a.status);
+        ok(cudaGetLastError());
+        const unsigned int nbb = std::min(kBboxBlocks, std::max(1u, blocks_for(np, 256)));
+        k_bbox<<<nbb, 256, 0, st>>>(*a.pos, np, fs.d_bbox);
+        ok(cudaGetLastError());
+        std::vector<double> bb((size_t)nbb * 6);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(bb.data(), fs.d_bbox, bb.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return XDEM_ERR_CUDA;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (unsigned int b = 0; b < nbb; ++b)
+            for (int c = 0; c < 3; ++c) {
+                lo[c] = std::min(lo[c], bb[b * 6 + c]);
+                hi[c] = std::max(hi[c], bb[b * 6 + 3 + c]);
+            }
+        double r2 = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            if (!(hi[c] >= lo[c])) { lo[c] = 0.0; hi[c] = 0.0; }
+            fs.frame_c[c] = 0.5 * (lo[c] + hi[c]);
+            r2 += 0.25 * (hi[c] - lo[c]) * (hi[c] - lo[c]);
+        }
+        // particles may drift: the float frame covers the cloud plus 1 m
+        const double R = std::sqrt(r2) + 1.0;
+        fs.frame_far2 = R * R;
+        // float rounding of two coordinates of size <= R, their difference
+        // and the sum of squares; 4x slack
+        fs.frame_margin = (float)(16.0 * R * std::ldexp(1.0, -24) + 1e-9);
+        fs.primed = true;
+    }
+    // Between steps *a.pos / *a.ep hold the committed state (x_n) and the
+    // alternate buffers the positions of the next step (x_{n+1}, computed by
+    // the prologue or by the previous contact kernel).  They become current
+    // here; the contact kernel then writes x_{n+2} into the old buffers.
+    std::swap(*a.pos, fs.pos_alt);
+    std::swap(*a.ep, fs.ep_alt);
+    // mesh spheres join the sort at entries np + first (xIntegratorVV.cpp:32-43)
+    for (unsigned int m = 0; m < a.nmesh; ++m)
+        ok(launch_hash(a.prm, a.k0, a.v0, a.tri_sphere + 4 * (size_t)a.mesh_first[m], np + a.mesh_first[m],
+                       a.mesh_ntri[m], a.status, st));
+    if (fs.have_prev) ok(launch_clear_cells(fs.skey_prev, n, a.cstart, a.cend, st));
+    unsigned int *sk = nullptr, *sv = nullptr;
+    ok(radix_sort_pairs(a.k0, a.v0, a.k1, a.v1, a.hist, n, a.sort_bits, &sk, &sv, st));
+    nl += 3 * ((a.sort_bits + 7) / 8) - 1;
+    // positions of this step are in *a.pos (x_{n+1}); *a.ep holds e_{n+1}
+    k_reorder<<<blocks_for(n), kThreads, 0, st>>>(sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev,
+                                                  *a.pos, *a.ep, a.vel, a.ev, a.mass, fs.snap_pos, fs.snap_vel,
+                                                  fs.snap_om, fs.snap_f, fs.frame_c[0], fs.frame_c[1], fs.frame_c[2],
+                                                  fs.frame_far2);
+    ok(cudaGetLastError());
+    fs.have_prev = true;
+
+    ContactLaunch c{};
+    c.prm = a.prm;
+    c.np = np;
+    c.nentry = n;
+    c.vel_compat = a.vel_compat;
+    c.snap_pos = fs.snap_pos; c.snap_vel = fs.snap_vel; c.snap_om = fs.snap_om; c.snap_f = fs.snap_f;
+    c.margin = fs.frame_margin;
+    c.sorted_index = a.sorted_index; c.cstart = a.cstart; c.cend = a.cend; c.skey = fs.skey_prev;
+    c.pos_cur = *a.pos; c.pos_next = fs.pos_alt; c.ep_cur = *a.ep; c.ep_next = fs.ep_alt;
+    c.vel = a.vel; c.acc = a.acc; c.ev = a.ev; c.ea = a.ea; c.mass = a.mass; c.inertia = a.inertia;
+    c.k_out = a.k0; c.v_out = a.v0;
+    c.has_pp = a.has_pp;
+    c.pp_count_old = *a.pp_count; c.pp_id_old = *a.pp_id; c.pp_tsd_old = *a.pp_tsd;
+    c.pp_count_new = fs.pp_count2; c.pp_id_new = fs.pp_id2; c.pp_tsd_new = fs.pp_tsd2;
+    c.planes = fs.planes; c.nplane = a.nplane; c.nmesh = a.nmesh;
+    for (unsigned int m = 0; m < a.nmesh && m < kMaxFusedMeshes; ++m) {
+        c.mesh_first[m] = a.mesh_first[m];
+        c.mesh_ntri[m] = a.mesh_ntri[m];
+        c.mesh_body[m] = a.mesh_body[m];
+    }
+    c.pl_count = a.pl_count; c.pl_id = a.pl_id; c.pl_tsd = a.pl_tsd;
+    c.tri = a.tri; c.ms_count = a.ms_count; c.ms_id = a.ms_id; c.ms_tsd = a.ms_tsd;
+    c.body = a.body; c.mp = a.mp;
+    c.nblocks = (n + kFusedThreads - 1) / kFusedThreads;
+    c.bsums = a.bsums;
+    c.status = a.status;
+    if (e0) cudaEventRecord(e0, st);
+    ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
+    if (e1) cudaEventRecord(e1, st);
+    if (a.nbody) {
+        const unsigned int warps = a.nbody * 6;
+        k_body_sums<<<(warps + 7) / 8, 256, 0, st>>>(a.bsums, c.nblocks, a.nbody, a.wrench);
+        ok(cudaGetLastError());
+    }
+    if (e != cudaSuccess) return XDEM_ERR_CUDA;
+    // state now: x_{n+1}, e_{n+1} and vel/acc/ev/ea of step n+1 committed;
+    // x_{n+2}, e_{n+2} in the alternate buffers (input of the next step); the
+    // new pair lists in the partner buffers
+    if (a.has_pp) {
+        std::swap(*a.pp_count, fs.pp_count2);
+        std::swap(*a.pp_id, fs.pp_id2);
+        std::swap(*a.pp_tsd, fs.pp_tsd2);
+    }
+    if (nlaunch) *nlaunch = nl;
+    return XDEM_OK;
+}
+
+int fused_energy(FusedState& fs, const double* vel, const double* ep, const double* ev, const double* mass,
+                 const double* inertia, unsigned int ns, const unsigned int* c0, const unsigned int* c1,
+                 const unsigned int* c2, unsigned int np, double* ke, unsigned int* ncontact, cudaStream_t st)
+{
+    double* d = fs.d_energy;
+    if (!d) return XDEM_ERR_ARG;
+    cudaError_t e = cudaMemsetAsync(d, 0, 16, st);
+    if (e == cudaSuccess) {
+        k_energy<<<304, 256, 0, st>>>(vel, ep, ev, mass, inertia, ns, c0, c1, c2, np, d,
+                                      reinterpret_cast<unsigned int*>(d + 1));
+        e = cudaGetLastError();
+    }
+    double h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return XDEM_ERR_CUDA;
+    *ke = h[0];
+    unsigned int c;
+    std::memcpy(&c, &h[1], sizeof(c));
+    *ncontact = c;
+    return XDEM_OK;
+}
+
+}  // namespace xdem

@@ -1,0 +1,781 @@
+// xdem_sim.cu -- scene handle: the whole DEM step on the GPU.
+//
+// The handle owns particle state (reference layout), pair lists, the cell
+// grid, planes and triangle meshes.  xdem_sim_step advances it in the order of
+// xIntegratorVV::OneStepSimulation (source/xdynamics_simulation/
+// xIntegratorVV.cpp:26-63): position update, hashing of particles and mesh
+// spheres, sort and cell ranges, particle-particle contact, planes in id
+// order, meshes, rolling resistance, velocity update.  Every allocation
+// happens in create / set / add; a step allocates nothing.
+//
+// Two step paths share the state:
+//  * launcher_path = 1: the launcher kernels (xdem_kernels.cu) one after the
+//    other, the reference's own structure;
+//  * launcher_path = 0: the fused sorted-order step (xdem_fused.cuh), one
+//    contact+integration kernel per step over a cell-sorted snapshot.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "xdem_device.cuh"
+#include "xdem_fused.h"
+#include "xdem_kernels.h"
+
+using namespace xdem;
+
+struct SimBody {
+    int kind;              // 0 plane, 1 mesh
+    int index;             // plane index or mesh index
+    double rec[15];
+};
+
+struct SimMesh {
+    unsigned int ntri, first;  // triangles [first, first + ntri) of the global arrays
+    int body;
+};
+
+struct xdem_sim {
+    xdem_sim_config cfg{};
+    device_dem_parameters prm{};
+    cudaStream_t st = 0;
+    unsigned int np = 0, ns = 0, nco = 0, nrloc = 0;
+    bool clusters = false;
+    unsigned int status_host = 0;
+    // state (reference layout)
+    double *pos = nullptr, *cpos = nullptr, *vel = nullptr, *acc = nullptr, *ep = nullptr, *ev = nullptr,
+           *ea = nullptr;
+    double *force = nullptr, *moment = nullptr, *mass = nullptr, *inertia = nullptr, *tmax = nullptr,
+           *rres = nullptr, *rloc = nullptr;
+    xClusterInformation* xci = nullptr;
+    // grid
+    unsigned int nentry = 0;
+    size_t ncell = 0;
+    unsigned int *k0 = nullptr, *v0 = nullptr, *k1 = nullptr, *v1 = nullptr, *hist = nullptr;
+    unsigned int *cstart = nullptr, *cend = nullptr, *sorted_index = nullptr;
+    unsigned int* skey = nullptr;  // sorted keys of the last step (k0 or k1)
+    bool cells_clean = false;
+    // contacts
+    bool has_pp = false;
+    device_contact_property pp_cp{};
+    mat_pair* d_mp = nullptr;  // [0] pp, then one per body
+    unsigned int *pp_count = nullptr, *pp_id = nullptr;
+    double* pp_tsd = nullptr;
+    unsigned int *pl_count = nullptr, *pl_id = nullptr;
+    double* pl_tsd = nullptr;
+    unsigned int *ms_count = nullptr, *ms_id = nullptr;
+    double* ms_tsd = nullptr;
+    std::vector<SimBody> bodies;
+    std::vector<device_plane_info> planes;
+    std::vector<device_contact_property> body_cp;
+    std::vector<SimMesh> meshes;
+    device_plane_info* d_planes = nullptr;
+    double* d_body = nullptr;      // 15 per body
+    unsigned int ntri_total = 0;
+    std::vector<double> h_vlist, h_dlocal, h_sphere;  // host copies for setup
+    std::vector<device_triangle_info> h_tri;
+    device_triangle_info* d_tri = nullptr;
+    double *d_vlist = nullptr, *d_dlocal = nullptr, *d_sphere = nullptr;
+    double* bsums = nullptr;       // per body: nblocks * 6
+    double* wrench = nullptr;      // per body: 6
+    unsigned int* d_status = nullptr;
+    bool dirty_bodies = true;      // device body tables need upload
+    bool dirty_alloc = true;       // contact tables need (re)allocation
+    // fused path
+    FusedState fs{};
+    bool precision_mixed() const;
+    // profiling: events around the contact kernel, a ring of kProfEvents
+    // pairs read once at the end of xdem_sim_step
+    static constexpr int kProfEvents = 64;
+    bool profiling = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t pe0[kProfEvents] = {}, pe1[kProfEvents] = {};
+    double prof_ms = 0.0;
+    unsigned int prof_launches = 0, prof_contact_launches = 0, launches = 0;
+};
+
+namespace {
+
+int cerr(cudaError_t e)
+{
+    if (e == cudaSuccess) return XDEM_OK;
+    fprintf(stderr, "xdem_sim: CUDA error %s\n", cudaGetErrorString(e));
+    return XDEM_ERR_CUDA;
+}
+
+template <class T>
+cudaError_t dalloc(T*& p, size_t n)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    return cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T));
+}
+
+template <class T>
+void dfree(T*& p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int bits_for(unsigned long long ncell)
+{
+    int b = 0;
+    while (b < 32 && (1ull << b) < ncell) ++b;
+    return b == 0 ? 1 : b;
+}
+
+// ---- host restatement of the mesh setup (xParticleMeshObjectContact.cpp:77-135)
+struct h3 { double x, y, z; };
+h3 hsub(h3 a, h3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+h3 hadd(h3 a, h3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+h3 hmul(double s, h3 a) { return {s * a.x, s * a.y, s * a.z}; }
+h3 hdiv(h3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+double hdot(h3 a, h3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+double hlen(h3 a) { return std::sqrt(hdot(a, a)); }
+h3 hcross(h3 a, h3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+void hrot(const double e[4], h3 r[3])
+{
+    r[0] = {2.0 * (e[0] * e[0] + e[1] * e[1] - 0.5), 2.0 * (e[1] * e[2] - e[0] * e[3]), 2.0 * (e[1] * e[3] + e[0] * e[2])};
+    r[1] = {2.0 * (e[1] * e[2] + e[0] * e[3]), 2.0 * (e[0] * e[0] + e[2] * e[2] - 0.5), 2.0 * (e[2] * e[3] - e[0] * e[1])};
+    r[2] = {2.0 * (e[1] * e[3] - e[0] * e[2]), 2.0 * (e[2] * e[3] + e[0] * e[1]), 2.0 * (e[0] * e[0] + e[3] * e[3] - 0.5)};
+}
+h3 hglobal(const h3 r[3], h3 v) { return {hdot(r[0], v), hdot(r[1], v), hdot(r[2], v)}; }
+h3 hlocal(const h3 r[3], h3 v)
+{
+    return {r[0].x * v.x + r[1].x * v.y + r[2].x * v.z, r[0].y * v.x + r[1].y * v.y + r[2].y * v.z,
+            r[0].z * v.x + r[1].z * v.y + r[2].z * v.z};
+}
+
+// FitSphereToTriangle (source/xdynamics_algebra/xUtilityFunction.cpp:379-416):
+// circumcentre of the triangle moved along the normal until the triangle
+// subtends the fraction ft of the sphere.
+void fit_sphere(h3 P, h3 Q, h3 R, double ft, double out[4])
+{
+    const h3 V = hsub(Q, P), W = hsub(R, P);
+    h3 N = hcross(V, W);
+    N = hdiv(N, hlen(N));
+    const h3 M1 = hdiv(hadd(Q, P), 2), M2 = hdiv(hadd(R, P), 2);
+    const h3 D1 = hcross(N, V), D2 = hcross(N, W);
+    double t = 0.0;
+    if (std::fabs(D1.x * D2.y - D1.y * D2.x) > 1E-13)
+        t = (D2.x * (M1.y - M2.y)) / (D1.x * D2.y - D1.y * D2.x) - (D2.y * (M1.x - M2.x)) / (D1.x * D2.y - D1.y * D2.x);
+    else if (std::fabs(D1.x * D2.z - D1.z * D2.x) > 1E-13)
+        t = (D2.x * (M1.z - M2.z)) / (D1.x * D2.z - D1.z * D2.x) - (D2.z * (M1.x - M2.x)) / (D1.x * D2.z - D1.z * D2.x);
+    else if (std::fabs(D1.y * D2.z - D1.z * D2.y) > 1E-13)
+        t = (D2.y * (M1.z - M2.z)) / (D1.y * D2.z - D1.z * D2.y) - (D2.z * (M1.y - M2.y)) / (D1.y * D2.z - D1.z * D2.y);
+    const h3 Ctri = hadd(M1, hmul(t, D1));
+    h3 Csph{0, 0, 0};
+    double fc = 0, r = hlen(hsub(P, Ctri));
+    for (int it = 0; std::fabs(fc - ft) > 1e-4 && it < 1000; ++it) {
+        const double d = ft * r;
+        const double p = d / hlen(N);
+        Csph = hsub(Ctri, hmul(p, N));
+        r = hlen(hsub(P, Csph));
+        fc = d / r;
+    }
+    out[0] = Csph.x; out[1] = Csph.y; out[2] = Csph.z; out[3] = r;
+}
+
+// (Re)allocates grid and contact tables after the body set changed.
+int ensure_tables(xdem_sim* s)
+{
+    if (!s->dirty_alloc) return XDEM_OK;
+    const unsigned int n = s->np;
+    s->nentry = n + s->ntri_total;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto*& p, size_t cnt) {
+        if (e == cudaSuccess) e = dalloc(p, cnt);
+    };
+    A(s->k0, s->nentry); A(s->v0, s->nentry); A(s->k1, s->nentry); A(s->v1, s->nentry);
+    A(s->hist, radix_hist_size(s->nentry));
+    A(s->sorted_index, s->nentry);
+    const unsigned int nb = blocks_for(s->nentry);
+    const size_t nbody = std::max<size_t>(s->bodies.size(), 1);
+    A(s->bsums, (size_t)nb * 6 * nbody);
+    A(s->wrench, 6 * nbody);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->wrench, 0, 6 * nbody * sizeof(double), s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->bsums, 0, (size_t)nb * 6 * nbody * sizeof(double), s->st);
+    if (e != cudaSuccess) return XDEM_ERR_ALLOC;
+    if (int r = fused_alloc(s->fs, n, s->nentry, s->precision_mixed(), s->st)) return r;
+    s->skey = nullptr;
+    s->cells_clean = false;
+    s->dirty_alloc = false;
+    return XDEM_OK;
+}
+
+int upload_bodies(xdem_sim* s)
+{
+    if (!s->dirty_bodies) return XDEM_OK;
+    cudaError_t e = cudaSuccess;
+    const size_t nb = s->bodies.size();
+    if (s->planes.size()) {
+        if (!s->d_planes) e = dalloc(s->d_planes, 64);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d_planes, s->planes.data(), s->planes.size() * sizeof(device_plane_info),
+                                cudaMemcpyHostToDevice, s->st);
+    }
+    std::vector<double> rec(std::max<size_t>(nb, 1) * 15, 0.0);
+    for (size_t i = 0; i < nb; ++i) std::memcpy(&rec[i * 15], s->bodies[i].rec, sizeof(double) * 15);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->d_body, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice, s->st);
+    // material constants: [0] particle-particle, [1 + b] body b
+    std::vector<mat_pair> mps(nb + 1);
+    mps[0] = make_mat_pair(s->pp_cp, s->prm.contact_model, false);
+    for (size_t i = 0; i < nb; ++i)
+        mps[i + 1] = make_mat_pair(s->body_cp[i], s->prm.contact_model,
+                                   s->clusters && s->bodies[i].kind == 0 /* cluster-plane swap */);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->d_mp, mps.data(), mps.size() * sizeof(mat_pair), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cerr(e);
+    s->dirty_bodies = false;
+    return fused_set_bodies(s->fs, s->d_planes, (unsigned int)s->planes.size(), s->d_body, s->d_mp);
+}
+
+// ---------------------------------------------------------------- launcher-order step
+int step_launcher(xdem_sim* s, cudaEvent_t e0, cudaEvent_t e1)
+{
+    const cudaStream_t st = s->st;
+    const device_dem_parameters& p = s->prm;
+    const unsigned int n = s->np;
+    cudaError_t e = cudaSuccess;
+    auto ok = [&](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+        s->launches++;
+    };
+    if (s->clusters)
+        ok(launch_vv_cluster_position(p, s->pos, s->cpos, s->ep, s->rloc, s->vel, s->acc, s->ev, s->ea, s->xci, s->ns, st));
+    else
+        ok(launch_vv_position(p, s->pos, s->ep, s->vel, s->ev, s->acc, s->ea, n, st));
+    // empty the cells the previous step filled, then hash, sort, cell ranges
+    if (!s->cells_clean) {
+        ok(launch_fill_u32(s->cstart, 0xffffffffu, s->ncell, st));
+        ok(cudaMemsetAsync(s->cend, 0, s->ncell * sizeof(unsigned int), st));
+        s->cells_clean = true;
+    } else if (s->skey) {
+        ok(launch_clear_cells(s->skey, s->nentry, s->cstart, s->cend, st));
+    }
+    ok(launch_hash(p, s->k0, s->v0, s->pos, 0, n, s->d_status, st));
+    for (const SimMesh& m : s->meshes)
+        ok(launch_hash(p, s->k0, s->v0, s->d_sphere + 4 * (size_t)m.first, n + m.first, m.ntri, s->d_status, st));
+    unsigned int *sk = nullptr, *sv = nullptr;
+    ok(radix_sort_pairs(s->k0, s->v0, s->k1, s->v1, s->hist, s->nentry, bits_for(s->ncell), &sk, &sv, st));
+    s->launches += 3 * ((bits_for(s->ncell) + 7) / 8) - 1;
+    ok(launch_cell_bounds(sk, sv, s->cstart, s->cend, s->sorted_index, s->nentry, st));
+    s->skey = sk;
+    // contacts (xContactManager.cpp:458-472)
+    const unsigned int nb = blocks_for(n);
+    if (e0) cudaEventRecord(e0, st);
+    if (s->has_pp) {
+        if (s->clusters)
+            ok(launch_clusters_p2p(p, s->pos, s->cpos, s->ep, s->vel, s->ev, s->force, s->moment, s->mass, s->tmax,
+                                   s->rres, s->pp_count, s->pp_id, s->pp_tsd, s->sorted_index, s->cstart, s->cend,
+                                   s->d_mp, s->xci, n, s->d_status, st));
+        else
+            ok(launch_p2p(p, s->pos, s->ep, s->vel, s->ev, s->force, s->moment, s->mass, s->tmax, s->rres,
+                          s->pp_count, s->pp_id, s->pp_tsd, s->sorted_index, s->cstart, s->cend, s->d_mp, n,
+                          s->d_status, st));
+    }
+    if (e1) cudaEventRecord(e1, st);
+    for (size_t b = 0; b < s->bodies.size(); ++b) {
+        const SimBody& bd = s->bodies[b];
+        BodyPartials bp{};
+        bp.block_sums = s->bsums + (size_t)b * nb * 6;
+        const double* dbi = s->d_body + 15 * b;
+        const mat_pair* mp = s->d_mp + 1 + b;
+        if (bd.kind == 0) {
+            const device_plane_info* pl = s->d_planes + bd.index;
+            if (s->clusters)
+                ok(launch_cluster_plane(p, pl, dbi, mp, bp, s->pos, s->cpos, s->ep, s->vel, s->ev, s->force,
+                                        s->moment, s->mass, s->tmax, s->rres, s->pl_count, s->pl_id, s->pl_tsd,
+                                        s->xci, n, s->d_status, st));
+            else
+                ok(launch_plane(p, pl, dbi, mp, bp, s->pos, s->ep, s->vel, s->ev, s->force, s->moment, s->mass,
+                                s->tmax, s->rres, s->pl_count, s->pl_id, s->pl_tsd, n, s->d_status, st));
+        } else {
+            const SimMesh& m = s->meshes[bd.index];
+            ok(launch_mesh(p, s->d_tri + m.first, n, s->clusters ? 2 : 1, dbi, mp, bp, s->pos,
+                           s->clusters ? s->cpos : nullptr, s->ep, s->vel, s->ev, s->force, s->moment, s->mass,
+                           s->tmax, s->rres, s->ms_count, s->ms_id, s->ms_tsd, s->sorted_index, s->cstart, s->cend,
+                           s->clusters ? s->xci : nullptr, n, m.ntri, s->d_status, st));
+        }
+        ok(launch_sum_block_partials(bp.block_sums, nb, s->wrench + 6 * b, st));
+    }
+    if (s->clusters)
+        ok(launch_cluster_rolling(p, s->tmax, s->rres, s->inertia, s->ep, s->ev, s->moment, s->xci, n, st));
+    else
+        ok(launch_rolling(p, s->tmax, s->rres, s->inertia, s->ep, s->ev, s->moment, n, st));
+    if (s->clusters)
+        ok(launch_vv_cluster_velocity(p, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass,
+                                      s->inertia, s->xci, s->ns, st));
+    else
+        ok(launch_vv_velocity(p, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass, s->inertia, n,
+                              s->cfg.velocity_compat, st));
+    return cerr(e);
+}
+
+FusedArgs fused_args(xdem_sim* s)
+{
+    FusedArgs a{};
+    a.prm = s->prm;
+    a.np = s->np;
+    a.nentry = s->nentry;
+    a.ncell = s->ncell;
+    a.sort_bits = bits_for(s->ncell);
+    a.vel_compat = s->cfg.velocity_compat;
+    a.pos = &s->pos; a.vel = s->vel; a.acc = s->acc; a.ep = &s->ep; a.ev = s->ev; a.ea = s->ea;
+    a.mass = s->mass; a.inertia = s->inertia; a.tmax = s->tmax; a.rres = s->rres;
+    a.k0 = s->k0; a.v0 = s->v0; a.k1 = s->k1; a.v1 = s->v1; a.hist = s->hist;
+    a.cstart = s->cstart; a.cend = s->cend; a.sorted_index = s->sorted_index;
+    a.has_pp = s->has_pp;
+    a.pp_count = &s->pp_count; a.pp_id = &s->pp_id; a.pp_tsd = &s->pp_tsd;
+    a.pl_count = s->pl_count; a.pl_id = s->pl_id; a.pl_tsd = s->pl_tsd;
+    a.nplane = (unsigned int)s->planes.size();
+    a.nbody = (unsigned int)s->bodies.size();
+    a.nmesh = (unsigned int)s->meshes.size();
+    for (unsigned int m = 0; m < a.nmesh && m < kMaxFusedMeshes; ++m) {
+        a.mesh_first[m] = s->meshes[m].first;
+        a.mesh_ntri[m] = s->meshes[m].ntri;
+        a.mesh_body[m] = s->meshes[m].body;
+    }
+    a.tri = s->d_tri; a.tri_sphere = s->d_sphere;
+    a.ms_count = s->ms_count; a.ms_id = s->ms_id; a.ms_tsd = s->ms_tsd;
+    a.body = s->d_body; a.mp = s->d_mp;
+    a.bsums = s->bsums; a.wrench = s->wrench;
+    a.status = s->d_status;
+    return a;
+}
+
+}  // namespace
+
+bool xdem_sim::precision_mixed() const { return cfg.precision == XDEM_MIXED; }
+
+// ============================================================================
+extern "C" {
+
+XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
+{
+    if (!cfg || !out || cfg->np == 0 || !(cfg->cell_size > 0) || !(cfg->dt > 0)) return XDEM_ERR_ARG;
+    if (cfg->precision != XDEM_FP64 && cfg->precision != XDEM_MIXED) return XDEM_ERR_ARG;
+    for (int i = 0; i < 3; ++i) {
+        const unsigned int g = cfg->grid_size[i];
+        if (!g || (g & (g - 1))) return XDEM_ERR_ARG;
+    }
+    const unsigned long long ncell =
+        (unsigned long long)cfg->grid_size[0] * cfg->grid_size[1] * cfg->grid_size[2];
+    if (ncell > (1ull << 31)) return XDEM_ERR_ARG;
+    xdem_sim* s = new (std::nothrow) xdem_sim();
+    if (!s) return XDEM_ERR_ALLOC;
+    s->cfg = *cfg;
+    s->np = cfg->np;
+    s->ns = cfg->ns ? cfg->ns : cfg->np;
+    s->clusters = s->ns != s->np;
+    device_dem_parameters& p = s->prm;
+    std::memset(&p, 0, sizeof(p));
+    p.contact_model = cfg->contact_model;
+    p.np = s->np;
+    p.nCluster = s->clusters ? s->ns : 0;
+    p.grid_size = xdem_uint3{cfg->grid_size[0], cfg->grid_size[1], cfg->grid_size[2]};
+    p.ncell = (unsigned int)ncell;
+    p.dt = cfg->dt;
+    p.half2dt = 0.5 * cfg->dt * cfg->dt;
+    p.cell_size = cfg->cell_size;
+    p.gravity = xdem_double3{cfg->gravity[0], cfg->gravity[1], cfg->gravity[2]};
+    p.world_origin = xdem_double3{cfg->world_origin[0], cfg->world_origin[1], cfg->world_origin[2]};
+    s->ncell = ncell;
+    const size_t n = s->np, ns = s->ns;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](auto*& q, size_t cnt) {
+        if (e == cudaSuccess) e = dalloc(q, cnt);
+    };
+    A(s->pos, n * 4); A(s->vel, ns * 3); A(s->acc, ns * 3); A(s->ep, ns * 4); A(s->ev, ns * 4); A(s->ea, ns * 4);
+    A(s->force, n * 3); A(s->moment, n * 3); A(s->mass, ns); A(s->inertia, ns * 3); A(s->tmax, n * 3);
+    A(s->rres, n);
+    A(s->pp_count, n); A(s->pp_id, n * MAX_P2P_COUNT); A(s->pp_tsd, n * MAX_P2P_COUNT * 2);
+    A(s->pl_count, n); A(s->pl_id, n * MAX_P2PL_COUNT); A(s->pl_tsd, n * MAX_P2PL_COUNT * 2);
+    A(s->ms_count, n); A(s->ms_id, n * MAX_P2MS_COUNT); A(s->ms_tsd, n * MAX_P2MS_COUNT * 2);
+    A(s->cstart, ncell); A(s->cend, ncell);
+    A(s->d_status, 1);
+    A(s->d_mp, 65);
+    A(s->d_body, 64 * 15);
+    if (s->clusters) A(s->cpos, ns * 4);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+    // zero everything that carries over between steps
+    auto Z = [&](void* q, size_t bytes) {
+        if (e == cudaSuccess && q) e = cudaMemsetAsync(q, 0, bytes, s->st);
+    };
+    Z(s->force, n * 24); Z(s->moment, n * 24); Z(s->tmax, n * 24); Z(s->rres, n * 8);
+    Z(s->pp_count, n * 4); Z(s->pp_id, n * 4 * MAX_P2P_COUNT); Z(s->pp_tsd, n * 16 * MAX_P2P_COUNT);
+    Z(s->pl_count, n * 4); Z(s->pl_id, n * 4 * MAX_P2PL_COUNT); Z(s->pl_tsd, n * 16 * MAX_P2PL_COUNT);
+    Z(s->ms_count, n * 4); Z(s->ms_id, n * 4 * MAX_P2MS_COUNT); Z(s->ms_tsd, n * 16 * MAX_P2MS_COUNT);
+    Z(s->d_status, 4);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        xdem_sim_destroy(s);
+        return XDEM_ERR_ALLOC;
+    }
+    *out = s;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_destroy(xdem_sim* s)
+{
+    if (!s) return XDEM_ERR_ARG;
+    if (s->st) cudaStreamSynchronize(s->st);
+    fused_free(s->fs);
+    double* dp[] = {s->pos, s->cpos, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass,
+                    s->inertia, s->tmax, s->rres, s->rloc, s->pp_tsd, s->pl_tsd, s->ms_tsd, s->d_body,
+                    s->d_vlist, s->d_dlocal, s->d_sphere, s->bsums, s->wrench};
+    for (double* q : dp)
+        if (q) cudaFree(q);
+    unsigned int* up[] = {s->k0, s->v0, s->k1, s->v1, s->hist, s->cstart, s->cend, s->sorted_index, s->pp_count,
+                          s->pp_id, s->pl_count, s->pl_id, s->ms_count, s->ms_id, s->d_status};
+    for (unsigned int* q : up)
+        if (q) cudaFree(q);
+    if (s->xci) cudaFree(s->xci);
+    if (s->d_mp) cudaFree(s->d_mp);
+    if (s->d_planes) cudaFree(s->d_planes);
+    if (s->d_tri) cudaFree(s->d_tri);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    for (int i = 0; i < xdem_sim::kProfEvents; ++i) {
+        if (s->pe0[i]) cudaEventDestroy(s->pe0[i]);
+        if (s->pe1[i]) cudaEventDestroy(s->pe1[i]);
+    }
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_set_stream(xdem_sim* s, void* stream)
+{
+    if (!s) return XDEM_ERR_ARG;
+    cudaStreamSynchronize(s->st);
+    s->st = reinterpret_cast<cudaStream_t>(stream);
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_set_state(xdem_sim* s, const double* pos, const double* vel, const double* acc,
+                                const double* ep, const double* ev, const double* ea, const double* mass,
+                                const double* inertia)
+{
+    if (!s || !pos || !mass || !inertia) return XDEM_ERR_ARG;
+    const size_t n = s->np, ns = s->ns;
+    cudaError_t e = cudaSuccess;
+    auto H = [&](double* d, const double* h, size_t cnt, double fill, int every, int off) {
+        if (e != cudaSuccess) return;
+        if (h) {
+            e = cudaMemcpyAsync(d, h, cnt * sizeof(double), cudaMemcpyHostToDevice, s->st);
+        } else {
+            std::vector<double> z(cnt, 0.0);
+            if (every)
+                for (size_t i = off; i < cnt; i += every) z[i] = fill;
+            e = cudaMemcpyAsync(d, z.data(), cnt * sizeof(double), cudaMemcpyHostToDevice, s->st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        }
+    };
+    H(s->pos, pos, n * 4, 0, 0, 0);
+    H(s->vel, vel, ns * 3, 0, 0, 0);
+    H(s->acc, acc, ns * 3, 0, 0, 0);
+    H(s->ep, ep, ns * 4, 1.0, 4, 0);
+    H(s->ev, ev, ns * 4, 0, 0, 0);
+    H(s->ea, ea, ns * 4, 0, 0, 0);
+    H(s->mass, mass, ns, 0, 0, 0);
+    H(s->inertia, inertia, ns * 3, 0, 0, 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    fused_invalidate(s->fs);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_set_clusters(xdem_sim* s, const double* cpos, const xClusterInformation* xci, unsigned int nco,
+                                   const double* rloc, unsigned int nrloc)
+{
+    if (!s || !s->clusters || !cpos || !xci || !nco || !rloc) return XDEM_ERR_ARG;
+    cudaError_t e = cudaMemcpyAsync(s->cpos, cpos, (size_t)s->ns * 4 * sizeof(double), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = dalloc(s->xci, nco);
+    if (e == cudaSuccess) e = dalloc(s->rloc, (size_t)nrloc * 3);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->xci, xci, nco * sizeof(xClusterInformation), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->rloc, rloc, (size_t)nrloc * 3 * sizeof(double), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    s->nco = nco;
+    s->nrloc = nrloc;
+    s->prm.nClusterObject = nco;
+    s->dirty_bodies = true;
+    fused_invalidate(s->fs);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_set_pp_contact(xdem_sim* s, const device_contact_property* cp)
+{
+    if (!s || !cp) return XDEM_ERR_ARG;
+    s->pp_cp = *cp;
+    s->has_pp = true;
+    s->dirty_bodies = true;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_add_plane(xdem_sim* s, const device_plane_info* plane, const double body[15],
+                                const device_contact_property* cp, int* body_index)
+{
+    if (!s || !plane || !body || !cp) return XDEM_ERR_ARG;
+    if (s->bodies.size() >= 64 || s->planes.size() >= 64) return XDEM_ERR_ARG;
+    if (!s->meshes.empty()) return XDEM_ERR_ARG;  // planes first, in id order, then meshes
+    SimBody b{};
+    b.kind = 0;
+    b.index = (int)s->planes.size();
+    std::memcpy(b.rec, body, sizeof(b.rec));
+    device_plane_info pl = *plane;
+    pl.id = (unsigned int)s->planes.size();  // ids in definition order (xParticlePlaneContact.cpp:53)
+    s->planes.push_back(pl);
+    s->bodies.push_back(b);
+    s->body_cp.push_back(*cp);
+    s->prm.nplane = (unsigned int)s->planes.size();
+    s->dirty_bodies = true;
+    s->dirty_alloc = true;
+    if (body_index) *body_index = (int)s->bodies.size() - 1;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_add_mesh(xdem_sim* s, unsigned int ntri, const double* vlist_local, const double body[15],
+                               const device_contact_property* cp, int* body_index)
+{
+    if (!s || !ntri || !vlist_local || !body || !cp) return XDEM_ERR_ARG;
+    if (s->bodies.size() >= 64 || s->meshes.size() >= kMaxFusedMeshes) return XDEM_ERR_ARG;
+    const unsigned int first = s->ntri_total;
+    const h3 bp{body[XDEM_PX], body[XDEM_PY], body[XDEM_PZ]};
+    h3 R[3];
+    hrot(body + XDEM_E0, R);
+    for (unsigned int i = 0; i < ntri; ++i) {
+        const double* v = vlist_local + 9 * (size_t)i;
+        const h3 P = hadd(bp, hglobal(R, h3{v[0], v[1], v[2]}));
+        const h3 Q = hadd(bp, hglobal(R, h3{v[3], v[4], v[5]}));
+        const h3 Rr = hadd(bp, hglobal(R, h3{v[6], v[7], v[8]}));
+        device_triangle_info t{};
+        t.id = (int)i;
+        t.tid = first + i;
+        t.P = xdem_double3{P.x, P.y, P.z};
+        t.Q = xdem_double3{Q.x, Q.y, Q.z};
+        t.R = xdem_double3{Rr.x, Rr.y, Rr.z};
+        s->h_tri.push_back(t);
+        double c[4];
+        fit_sphere(P, Q, Rr, 0.8, c);
+        for (int k = 0; k < 4; ++k) s->h_sphere.push_back(c[k]);
+        const h3 loc = hlocal(R, hsub(h3{c[0], c[1], c[2]}, bp));
+        s->h_dlocal.push_back(loc.x); s->h_dlocal.push_back(loc.y); s->h_dlocal.push_back(loc.z);
+        for (int k = 0; k < 9; ++k) s->h_vlist.push_back(v[k]);
+    }
+    s->ntri_total += ntri;
+    const size_t nt = s->ntri_total;
+    cudaError_t e = dalloc(s->d_tri, nt);
+    if (e == cudaSuccess) e = dalloc(s->d_sphere, nt * 4);
+    if (e == cudaSuccess) e = dalloc(s->d_dlocal, nt * 3);
+    if (e == cudaSuccess) e = dalloc(s->d_vlist, nt * 9);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_tri, s->h_tri.data(), nt * sizeof(device_triangle_info), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_sphere, s->h_sphere.data(), nt * 4 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_dlocal, s->h_dlocal.data(), nt * 3 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_vlist, s->h_vlist.data(), nt * 9 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return XDEM_ERR_ALLOC;
+    SimBody b{};
+    b.kind = 1;
+    b.index = (int)s->meshes.size();
+    std::memcpy(b.rec, body, sizeof(b.rec));
+    s->bodies.push_back(b);
+    s->body_cp.push_back(*cp);
+    s->meshes.push_back(SimMesh{ntri, first, (int)s->bodies.size() - 1});
+    s->dirty_bodies = true;
+    s->dirty_alloc = true;
+    if (body_index) *body_index = (int)s->bodies.size() - 1;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_get_mesh(xdem_sim* s, int body_index, device_triangle_info* tri, double* sphere,
+                               unsigned int* ntri)
+{
+    if (!s || body_index < 0 || body_index >= (int)s->bodies.size() || s->bodies[body_index].kind != 1)
+        return XDEM_ERR_ARG;
+    const SimMesh& m = s->meshes[s->bodies[body_index].index];
+    if (ntri) *ntri = m.ntri;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e == cudaSuccess && tri)
+        e = cudaMemcpy(tri, s->d_tri + m.first, m.ntri * sizeof(device_triangle_info), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && sphere)
+        e = cudaMemcpy(sphere, s->d_sphere + 4 * (size_t)m.first, m.ntri * 4 * sizeof(double), cudaMemcpyDeviceToHost);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_set_body(xdem_sim* s, int body_index, const double body[15], const device_plane_info* plane)
+{
+    if (!s || body_index < 0 || body_index >= (int)s->bodies.size() || !body) return XDEM_ERR_ARG;
+    SimBody& b = s->bodies[body_index];
+    std::memcpy(b.rec, body, sizeof(b.rec));
+    cudaError_t e = cudaMemcpyAsync(s->d_body + 15 * body_index, b.rec, sizeof(b.rec), cudaMemcpyHostToDevice, s->st);
+    if (b.kind == 0 && plane) {
+        device_plane_info pl = *plane;
+        pl.id = s->planes[b.index].id;
+        s->planes[b.index] = pl;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d_planes + b.index, &s->planes[b.index], sizeof(pl), cudaMemcpyHostToDevice, s->st);
+    }
+    if (b.kind == 1 && e == cudaSuccess) {
+        // xParticleMeshObjectContact::update -> cu_update_meshObjectData
+        const SimMesh& m = s->meshes[b.index];
+        e = launch_update_mesh(s->d_body + 15 * body_index, s->d_vlist + 9 * (size_t)m.first,
+                               s->d_sphere + 4 * (size_t)m.first, s->d_dlocal + 3 * (size_t)m.first,
+                               s->d_tri + m.first, m.ntri, s->st);
+    }
+    // the pinned-free host record must stay valid until the copy ran
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
+{
+    if (!s) return XDEM_ERR_ARG;
+    if (s->clusters && !s->xci) return XDEM_ERR_ARG;
+    if (int r = ensure_tables(s)) return r;
+    if (int r = upload_bodies(s)) return r;
+    s->launches = 0;
+    if (s->profiling && !s->pe0[0]) {
+        for (int i = 0; i < xdem_sim::kProfEvents; ++i) {
+            if (cudaEventCreate(&s->pe0[i]) != cudaSuccess || cudaEventCreate(&s->pe1[i]) != cudaSuccess)
+                return XDEM_ERR_CUDA;
+        }
+    }
+    unsigned int recorded = 0;
+    for (unsigned int i = 0; i < nsteps; ++i) {
+        int r;
+        const bool rec = s->profiling && recorded < (unsigned int)xdem_sim::kProfEvents;
+        cudaEvent_t e0 = rec ? s->pe0[recorded] : nullptr, e1 = rec ? s->pe1[recorded] : nullptr;
+        if (s->cfg.launcher_path || s->clusters) {
+            r = step_launcher(s, e0, e1);
+        } else {
+            FusedArgs a = fused_args(s);
+            unsigned int nl = 0;
+            r = fused_step(s->fs, a, s->st, e0, e1, &nl);
+            s->launches += nl;
+            s->cells_clean = true;
+        }
+        if (r) return r;
+        if (rec) recorded++;
+    }
+    double ms_total = 0.0;
+    if (recorded) {
+        cudaError_t e = cudaEventSynchronize(s->pe1[recorded - 1]);
+        for (unsigned int i = 0; e == cudaSuccess && i < recorded; ++i) {
+            float ms = 0.f;
+            e = cudaEventElapsedTime(&ms, s->pe0[i], s->pe1[i]);
+            ms_total += ms;
+        }
+        if (e != cudaSuccess) return cerr(e);
+    }
+    s->prof_ms = ms_total;
+    s->prof_contact_launches = recorded;
+    s->prof_launches = s->launches;
+    return cerr(cudaGetLastError());
+}
+
+XDEM_API int xdem_sim_body_wrench(xdem_sim* s, int body_index, double out6[6])
+{
+    if (!s || !out6 || body_index < 0 || body_index >= (int)s->bodies.size()) return XDEM_ERR_ARG;
+    cudaError_t e = cudaMemcpyAsync(out6, s->wrench + 6 * body_index, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_get_state(xdem_sim* s, double* pos, double* vel, double* acc, double* ep, double* ev,
+                                double* ea, double* cpos)
+{
+    if (!s) return XDEM_ERR_ARG;
+    const size_t n = s->np, ns = s->ns;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    auto D = [&](double* h, const double* d, size_t cnt) {
+        if (e == cudaSuccess && h && d) e = cudaMemcpy(h, d, cnt * sizeof(double), cudaMemcpyDeviceToHost);
+    };
+    D(pos, s->pos, n * 4); D(vel, s->vel, ns * 3); D(acc, s->acc, ns * 3); D(ep, s->ep, ns * 4);
+    D(ev, s->ev, ns * 4); D(ea, s->ea, ns * 4);
+    if (s->clusters) D(cpos, s->cpos, ns * 4);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_get_pairs(xdem_sim* s, int kind, unsigned int* count, unsigned int* ids, double* tsd)
+{
+    if (!s || kind < 0 || kind > 2) return XDEM_ERR_ARG;
+    const size_t n = s->np;
+    const unsigned int cap = kind == 0 ? MAX_P2P_COUNT : kind == 1 ? MAX_P2PL_COUNT : MAX_P2MS_COUNT;
+    const unsigned int* dc = kind == 0 ? s->pp_count : kind == 1 ? s->pl_count : s->ms_count;
+    const unsigned int* di = kind == 0 ? s->pp_id : kind == 1 ? s->pl_id : s->ms_id;
+    const double* dt = kind == 0 ? s->pp_tsd : kind == 1 ? s->pl_tsd : s->ms_tsd;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e == cudaSuccess && count) e = cudaMemcpy(count, dc, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && ids) e = cudaMemcpy(ids, di, n * 4 * cap, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && tsd) e = cudaMemcpy(tsd, dt, n * 16 * cap, cudaMemcpyDeviceToHost);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_set_pairs(xdem_sim* s, int kind, const unsigned int* count, const unsigned int* ids,
+                                const double* tsd)
+{
+    if (!s || kind < 0 || kind > 2 || !count || !ids || !tsd) return XDEM_ERR_ARG;
+    const size_t n = s->np;
+    const unsigned int cap = kind == 0 ? MAX_P2P_COUNT : kind == 1 ? MAX_P2PL_COUNT : MAX_P2MS_COUNT;
+    unsigned int* dc = kind == 0 ? s->pp_count : kind == 1 ? s->pl_count : s->ms_count;
+    unsigned int* di = kind == 0 ? s->pp_id : kind == 1 ? s->pl_id : s->ms_id;
+    double* dt = kind == 0 ? s->pp_tsd : kind == 1 ? s->pl_tsd : s->ms_tsd;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e == cudaSuccess) e = cudaMemcpy(dc, count, n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(di, ids, n * 4 * cap, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dt, tsd, n * 16 * cap, cudaMemcpyHostToDevice);
+    fused_invalidate(s->fs);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_energy(xdem_sim* s, double* ke, unsigned int* ncontact)
+{
+    if (!s) return XDEM_ERR_ARG;
+    double k = 0.0;
+    unsigned int c = 0;
+    if (int r = ensure_tables(s)) return r;
+    int r = fused_energy(s->fs, s->vel, s->ep, s->ev, s->mass, s->inertia, s->ns, s->pp_count, s->pl_count,
+                         s->ms_count, s->np, &k, &c, s->st);
+    if (ke) *ke = k;
+    if (ncontact) *ncontact = c;
+    return r;
+}
+
+XDEM_API int xdem_sim_status(xdem_sim* s)
+{
+    if (!s) return XDEM_ERR_ARG;
+    unsigned int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, s->d_status, 4, cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_status, 0, 4, s->st);
+    if (e != cudaSuccess) return XDEM_ERR_CUDA;
+    return (int)h;
+}
+
+XDEM_API int xdem_sim_set_profiling(xdem_sim* s, int on)
+{
+    if (!s) return XDEM_ERR_ARG;
+    s->profiling = on != 0;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_profile(xdem_sim* s, unsigned int* launches, double* contact_ms, unsigned int* contact_launches)
+{
+    if (!s) return XDEM_ERR_ARG;
+    if (launches) *launches = s->prof_launches;
+    if (contact_ms) *contact_ms = s->prof_ms;
+    if (contact_launches) *contact_launches = s->prof_contact_launches;
+    return XDEM_OK;
+}
+
+}  // extern "C"

@@ -160,9 +160,19 @@ def dam_break(n_target=1_000_000, r_min=1e-3, r_max=2e-3, rho=2500.0, E=1e7, nu=
     nx = int(np.floor((block_x - 2 * r_max) / sp)) + 1
     nz = int(np.floor((block_z - 2 * r_max) / sp)) + 1
     ny = int(np.ceil(n_target / (nx * nz)))
-    pts = jittered_lattice(nx, ny, nz, sp, (r_max + jit, r_max + jit, r_max + jit), jit, rng)[:n_target]
+    # columns on a jittered square pitch sp >= 2 r_max; inside a column each
+    # sphere rests on the one below it with an overlap of 1e-3 r_min, so the
+    # column carries its weight through contacts from the first step
+    radii = rng.uniform(r_min, r_max, size=(ny, nz, nx))
+    gap = -1e-3 * r_min
+    ys = np.cumsum(radii + np.roll(radii, 1, axis=0) + gap, axis=0) - radii[0:1] - gap
+    ys = ys - ys[0:1] + radii[0:1] + gap
+    xs = (r_max + jit + np.arange(nx) * sp)[None, None, :] + rng.uniform(-jit, jit, size=(1, nz, nx))
+    zs = (r_max + jit + np.arange(nz) * sp)[None, :, None] + rng.uniform(-jit, jit, size=(1, nz, nx))
+    pts = np.stack([np.broadcast_to(xs, radii.shape), ys, np.broadcast_to(zs, radii.shape)], axis=-1)
+    pts = pts.reshape(-1, 3)[:n_target]
+    radii = radii.reshape(-1)[:n_target]
     N = pts.shape[0]
-    radii = rng.uniform(r_min, r_max, size=N)
     pos = np.zeros((N, 4))
     pos[:, :3] = pts
     pos[:, 3] = radii
@@ -174,11 +184,13 @@ def dam_break(n_target=1_000_000, r_min=1e-3, r_max=2e-3, rho=2500.0, E=1e7, nu=
     planes = open_box_planes(0.0, box[0], 0.0, height + 0.01, 0.0, box[2])
     cs = 2.0 * r_max
     if grid == "domain":
-        gx = pow2_at_least(int(np.ceil((box[0] + 0.02) / cs)) + 2)
-        gy = pow2_at_least(int(np.ceil((height + 0.03) / cs)) + 2)
-        gz = pow2_at_least(int(np.ceil((box[2] + 0.02) / cs)) + 2)
+        # origin 1.25 cells below the box; one spare cell above it
+        o = -1.25 * cs
+        gx = pow2_at_least(int(np.ceil((box[0] - o) / cs)) + 1)
+        gy = pow2_at_least(int(np.ceil((height + 0.01 - o) / cs)) + 1)
+        gz = pow2_at_least(int(np.ceil((box[2] - o) / cs)) + 1)
         grid_dims = (gx, gy, gz)
-        origin = (-0.01, -0.01, -0.01)
+        origin = (o, o, o)
     else:
         grid_dims = (128, 128, 128)
         origin = (-1.0, -1.0, -1.0)

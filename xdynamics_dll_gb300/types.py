@@ -103,6 +103,7 @@ class SimConfig(C.Structure):
         ("world_origin", C.c_double * 3),
         ("cell_size", C.c_double),
         ("grid_size", C.c_uint * 3),
+        ("launcher_path", C.c_int),
     ]
 
 
