@@ -8,10 +8,17 @@
 // wrench sums.  The contact kernel reads only the snapshot for neighbours, so
 // it updates the particle's own state in place without racing other threads.
 //
-// Position and Euler parameters are double-buffered (the step writes the next
-// positions into the other buffer); particle-particle pair lists are
-// double-buffered (old list read, new list written).  Swapping pointers after
-// each step costs nothing.
+// Position and Euler parameters are double-buffered: between steps the
+// handle's buffers hold the committed state and the alternate buffers the
+// already computed positions of the next step.  Particle-particle pair lists
+// are double-buffered (old list read, new list written).
+//
+// FP64 form: the snapshot holds FP64 position / velocity / spin (exact
+// classification) plus an FP32 copy of the position for a conservative
+// prefilter.  Mixed form: the snapshot is FP32 only -- each sphere's position
+// as an offset from the corner of its own cell plus the cell's integer
+// coordinates, so the relative position of two neighbours is formed in FP32
+// to about 1e-9 m without FP64 arithmetic in the neighbour loop.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,6 +31,12 @@ struct mat_pair;
 constexpr unsigned int kMaxFusedMeshes = 8;
 constexpr unsigned int kMaxFusedBodies = 64;
 constexpr unsigned int kBboxBlocks = 1024;
+constexpr int kPlaneF = 16;  // floats per plane in the prefilter table
+
+// FP32 view of a plane for the conservative "is this sphere near the plane"
+// test: corner xw (relative to the grid origin), unit edges u1, u2, unit
+// normal, edge lengths.  Layout: xw[3], u1[3], u2[3], un[3], l1, l2, pad[2].
+struct PlaneF { float v[kPlaneF]; };
 
 struct FusedState {
     bool mixed = false;
@@ -32,19 +45,29 @@ struct FusedState {
     unsigned int np = 0, nentry = 0;
     double* pos_alt = nullptr;  // [np*4] other position buffer
     double* ep_alt = nullptr;   // [np*4] other Euler-parameter buffer
-    double* snap_pos = nullptr; // [nentry*4] x, y, z, r (sorted order)
+    // FP64 snapshot (sorted order)
+    double* snap_pos = nullptr; // [nentry*4] x, y, z, r
     double* snap_vel = nullptr; // [nentry*4] vx, vy, vz, mass
     double* snap_om = nullptr;  // [nentry*4] wx, wy, wz, 0
-    float* snap_f = nullptr;    // [nentry*4] x-c, y-c, z-c, r (FP32 prefilter)
+    float* snap_f = nullptr;    // [nentry*4] x-o, y-o, z-o, r (FP32 prefilter; w < 0: no filter)
+    // mixed snapshot (sorted order) and its per-sphere source (original order)
+    float* mA = nullptr;        // [nentry*4] offset from own cell corner, r
+    float* mB = nullptr;        // [nentry*4] vx, vy, vz, mass
+    float* mC = nullptr;        // [nentry*4] wx, wy, wz, 0
+    unsigned int* mT = nullptr; // [nentry] packed unwrapped cell coordinates
+    float* rA = nullptr;        // [np*4] next-step records written by the contact kernel
+    float* rB = nullptr;
+    float* rC = nullptr;
+    unsigned int* rT = nullptr; // [np]
     unsigned int* pp_count2 = nullptr;
     unsigned int* pp_id2 = nullptr;
     double* pp_tsd2 = nullptr;
     unsigned int* skey_prev = nullptr;  // [nentry] sorted keys of the last step
     double* d_energy = nullptr;
-    double* d_bbox = nullptr;        // [kBboxBlocks * 6] block min/max of positions
-    double frame_c[3] = {0, 0, 0};  // centre of the FP32 prefilter frame
-    double frame_far2 = 0.0;        // squared radius beyond which FP32 is not trusted
-    float frame_margin = 0.f;       // prefilter slack for FP32 rounding
+    double* d_bbox = nullptr;   // [kBboxBlocks * 6] block min/max of positions
+    PlaneF* d_planef = nullptr; // [kMaxFusedBodies]
+    double frame_far2 = 0.0;    // squared radius (from the grid origin) of the FP32 frame
+    float frame_margin = 0.f;   // prefilter slack for FP32 rounding
     const device_plane_info* planes = nullptr;
     unsigned int nplane = 0;
     const double* body = nullptr;
@@ -79,13 +102,15 @@ struct FusedArgs {
     const mat_pair* mp;
     double *bsums, *wrench;
     unsigned int* status;
+    bool rolling;              // any contact property with rolling friction
 };
 
 int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st);
 void fused_free(FusedState& fs);
 void fused_invalidate(FusedState& fs);
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
-                     const mat_pair* mp);
+                     const mat_pair* mp, const device_plane_info* host_planes, const double origin[3],
+                     cudaStream_t st);
 // Runs one step.  When e0/e1 are given they bracket the contact kernel.
 int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                unsigned int* nlaunch);
@@ -99,11 +124,21 @@ struct ContactLaunch {
     device_dem_parameters prm;
     unsigned int np, nentry;
     int vel_compat;
+    bool rolling;
     const double* snap_pos;
     const double* snap_vel;
     const double* snap_om;
     const float* snap_f;
     float margin;
+    const float* mA;
+    const float* mB;
+    const float* mC;
+    const unsigned int* mT;
+    float* rA;
+    float* rB;
+    float* rC;
+    unsigned int* rT;
+    const PlaneF* planef;
     const unsigned int* sorted_index;
     const unsigned int* cstart;
     const unsigned int* cend;
@@ -143,5 +178,13 @@ struct ContactLaunch {
 cudaError_t launch_fused_contact_fp64(const ContactLaunch& c, cudaStream_t st);
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st);
 constexpr int kFusedThreads = 128;
+
+// Packed unwrapped cell coordinates: 11 bits x, 11 bits y, 10 bits z, each
+// modulo its field size.  Two cells whose packed difference is within one
+// cell per axis are neighbours unless 2048 / 1024 cells apart.
+__host__ __device__ inline unsigned int pack_cell(int x, int y, int z)
+{
+    return ((unsigned int)x & 2047u) | (((unsigned int)y & 2047u) << 11) | (((unsigned int)z & 1023u) << 22);
+}
 
 }  // namespace xdem

@@ -27,20 +27,37 @@ cudaError_t dalloc(T*& p, size_t n)
     return cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T));
 }
 
+// FP32 snapshot record of one sphere for the mixed contact kernel: offset of
+// the centre from its cell corner, radius, packed cell, velocity, mass, spin.
+__device__ __forceinline__ void mixed_record(const device_dem_parameters& p, double inv_cs, d3 x, double r, d3 v,
+                                             double m, d3 w, float4& A, float4& B, float4& C, unsigned int& T)
+{
+    const double rx = x.x - p.world_origin.x, ry = x.y - p.world_origin.y, rz = x.z - p.world_origin.z;
+    const double fx = floor(rx * inv_cs), fy = floor(ry * inv_cs), fz = floor(rz * inv_cs);
+    A = make_float4((float)(rx - fx * p.cell_size), (float)(ry - fy * p.cell_size), (float)(rz - fz * p.cell_size),
+                    (float)r);
+    B = make_float4((float)v.x, (float)v.y, (float)v.z, (float)m);
+    C = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
+    T = pack_cell(__double2int_rz(fx), __double2int_rz(fy), __double2int_rz(fz));
+}
+
 // Position update of the first step (impl:135-147) into the alternate
-// buffers, and the cell hash of the new position (impl:290-302).
+// buffers, and the cell hash of the new position (impl:290-302).  For the
+// mixed form also the FP32 record of the first step.
 __global__ void k_prologue(device_dem_parameters p, const double* pos, const double* ep, const double* vel,
-                           const double* ev, const double* acc, const double* ea, double* pos_next,
-                           double* ep_next, unsigned int* key, unsigned int* val, unsigned int n,
-                           unsigned int* status)
+                           const double* ev, const double* acc, const double* ea, const double* mass,
+                           double* pos_next, double* ep_next, unsigned int* key, unsigned int* val, unsigned int n,
+                           unsigned int* status, float* rA, float* rB, float* rC, unsigned int* rT)
 {
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double dt = p.dt, h = p.half2dt;
     const d4 e = (ld4(ep, i) + dt * ld4(ev, i)) + h * ld4(ea, i);
     const double l = sqrt(dot(e, e));
-    st4(ep_next, i, mk4(e.x / l, e.y / l, e.z / l, e.w / l));
-    const d3 d = dt * ld3(vel, i) + h * ld3(acc, i);
+    const d4 en = mk4(e.x / l, e.y / l, e.z / l, e.w / l);
+    st4(ep_next, i, en);
+    const d3 v = ld3(vel, i);
+    const d3 d = dt * v + h * ld3(acc, i);
     const d4 q = ld4(pos, i);
     const d3 x = mk3(q.x + d.x, q.y + d.y, q.z + d.z);
     st4(pos_next, i, mk4(x.x, x.y, x.z, q.w));
@@ -48,6 +65,15 @@ __global__ void k_prologue(device_dem_parameters p, const double* pos, const dou
     const int3v g = grid_pos(p, x);
     key[i] = grid_hash(p, g.x, g.y, g.z);
     val[i] = i;
+    if (rA) {
+        float4 A, B, C;
+        unsigned int T;
+        mixed_record(p, 1.0 / p.cell_size, x, q.w, v, mass[i], ang_vel(en, ld4(ev, i)), A, B, C, T);
+        reinterpret_cast<float4*>(rA)[i] = A;
+        reinterpret_cast<float4*>(rB)[i] = B;
+        reinterpret_cast<float4*>(rC)[i] = C;
+        rT[i] = T;
+    }
 }
 
 // Bounding box of the positions: block min/max into out[block*6].
@@ -77,23 +103,30 @@ __global__ void k_bbox(const double* pos, unsigned int n, double* out)
     }
 }
 
-// Cell ranges of the sorted keys (impl:317-360) and the sorted snapshot the
-// contact kernel reads its neighbours from.
-__global__ void k_reorder(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
-                          unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index, unsigned int* skey,
-                          const double* pos, const double* ep, const double* vel, const double* ev,
-                          const double* mass, double* snap_pos, double* snap_vel, double* snap_om, float* snap_f,
-                          double cx, double cy, double cz, double far2)
+__device__ __forceinline__ void cell_bounds(const unsigned int* sk, unsigned int s, unsigned int n,
+                                            unsigned int* cstart, unsigned int* cend, unsigned int k)
 {
-    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const unsigned int k = sk[s];
     const unsigned int prev = s ? sk[s - 1] : 0u;
     if (s == 0 || k != prev) {
         cstart[k] = s;
         if (s > 0) cend[prev] = s;
     }
     if (s == n - 1) cend[k] = s + 1;
+}
+
+// FP64 form: cell ranges of the sorted keys (impl:317-360) and the sorted
+// FP64 snapshot, plus an FP32 copy of the position relative to the grid
+// origin for the prefilter.
+__global__ void k_reorder_fp64(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
+                               unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index,
+                               unsigned int* skey, const double* pos, const double* ep, const double* vel,
+                               const double* ev, const double* mass, double* snap_pos, double* snap_vel,
+                               double* snap_om, float* snap_f, double ox, double oy, double oz, double far2)
+{
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const unsigned int k = sk[s];
+    cell_bounds(sk, s, n, cstart, cend, k);
     const unsigned int oid = sv[s];
     sorted_index[s] = oid;
     skey[s] = k;
@@ -105,11 +138,34 @@ __global__ void k_reorder(const unsigned int* sk, const unsigned int* sv, unsign
         st4(snap_pos, s, x);
         st4(snap_vel, s, mk4(v.x, v.y, v.z, mass[oid]));
         st4(snap_om, s, mk4(w.x, w.y, w.z, 0.0));
-        const double dx = x.x - cx, dy = x.y - cy, dz = x.z - cz;
-        if (dx * dx + dy * dy + dz * dz < far2)
-            f = make_float4((float)dx, (float)dy, (float)dz, (float)x.w);
+        const double dx = x.x - ox, dy = x.y - oy, dz = x.z - oz;
+        if (dx * dx + dy * dy + dz * dz < far2) f = make_float4((float)dx, (float)dy, (float)dz, (float)x.w);
     }
     reinterpret_cast<float4*>(snap_f)[s] = f;
+}
+
+// Mixed form: cell ranges and the FP32 records permuted into sorted order.
+__global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
+                                unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index,
+                                unsigned int* skey, const float4* rA, const float4* rB, const float4* rC,
+                                const unsigned int* rT, float4* mA, float4* mB, float4* mC, unsigned int* mT)
+{
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const unsigned int k = sk[s];
+    cell_bounds(sk, s, n, cstart, cend, k);
+    const unsigned int oid = sv[s];
+    sorted_index[s] = oid;
+    skey[s] = k;
+    if (oid < np) {
+        mA[s] = rA[oid];
+        mB[s] = rB[oid];
+        mC[s] = rC[oid];
+        mT[s] = rT[oid];
+    } else {
+        mA[s] = make_float4(0.f, 0.f, 0.f, -1.f);
+        mT[s] = 0xffffffffu;
+    }
 }
 
 __global__ void k_body_sums(const double* bsums, unsigned int nblocks, unsigned int nbody, double* wrench)
@@ -162,16 +218,28 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
     fs.nentry = nentry;
     cudaError_t e = dalloc(fs.pos_alt, (size_t)np * 4);
     if (e == cudaSuccess) e = dalloc(fs.ep_alt, (size_t)np * 4);
-    if (e == cudaSuccess) e = dalloc(fs.snap_pos, (size_t)nentry * 4);
-    if (e == cudaSuccess) e = dalloc(fs.snap_vel, (size_t)nentry * 4);
-    if (e == cudaSuccess) e = dalloc(fs.snap_om, (size_t)nentry * 4);
-    if (e == cudaSuccess) e = dalloc(fs.snap_f, (size_t)nentry * 4);
+    if (mixed) {
+        if (e == cudaSuccess) e = dalloc(fs.mA, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.mB, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.mC, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.mT, nentry);
+        if (e == cudaSuccess) e = dalloc(fs.rA, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.rB, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.rC, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.rT, np);
+    } else {
+        if (e == cudaSuccess) e = dalloc(fs.snap_pos, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.snap_vel, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.snap_om, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.snap_f, (size_t)nentry * 4);
+    }
     if (e == cudaSuccess) e = dalloc(fs.pp_count2, np);
     if (e == cudaSuccess) e = dalloc(fs.pp_id2, (size_t)np * MAX_P2P_COUNT);
     if (e == cudaSuccess) e = dalloc(fs.pp_tsd2, (size_t)np * MAX_P2P_COUNT * 2);
     if (e == cudaSuccess) e = dalloc(fs.skey_prev, nentry);
     if (e == cudaSuccess) e = dalloc(fs.d_energy, 2);
     if (e == cudaSuccess) e = dalloc(fs.d_bbox, (size_t)kBboxBlocks * 6);
+    if (e == cudaSuccess && !fs.d_planef) e = dalloc(fs.d_planef, kMaxFusedBodies);
     if (e == cudaSuccess) e = cudaMemsetAsync(fs.pp_count2, 0, np * sizeof(unsigned int), st);
     fs.primed = false;
     fs.have_prev = false;
@@ -180,8 +248,9 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 
 void fused_free(FusedState& fs)
 {
-    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.pp_count2,
-                  fs.pp_id2, fs.pp_tsd2, fs.skey_prev, fs.d_energy, fs.d_bbox};
+    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mB, fs.mC,
+                  fs.mT, fs.rA, fs.rB, fs.rC, fs.rT, fs.pp_count2, fs.pp_id2, fs.pp_tsd2, fs.skey_prev,
+                  fs.d_energy, fs.d_bbox, fs.d_planef};
     for (void* q : ps)
         if (q) cudaFree(q);
     fs = FusedState{};
@@ -190,13 +259,32 @@ void fused_free(FusedState& fs)
 void fused_invalidate(FusedState& fs) { fs.primed = false; }
 
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
-                     const mat_pair* mp)
+                     const mat_pair* mp, const device_plane_info* host_planes, const double origin[3],
+                     cudaStream_t st)
 {
     fs.planes = planes;
     fs.nplane = nplane;
     fs.body = body;
     fs.mp = mp;
-    return XDEM_OK;
+    if (!nplane) return XDEM_OK;
+    if (!fs.d_planef) {
+        if (dalloc(fs.d_planef, kMaxFusedBodies) != cudaSuccess) return XDEM_ERR_ALLOC;
+    }
+    std::vector<PlaneF> pf(nplane);
+    for (unsigned int k = 0; k < nplane; ++k) {
+        const device_plane_info& pl = host_planes[k];
+        const double uw[3] = {pl.uw.x, pl.uw.y, pl.uw.z};
+        const double lw = std::sqrt(uw[0] * uw[0] + uw[1] * uw[1] + uw[2] * uw[2]);
+        float* v = pf[k].v;
+        v[0] = (float)(pl.xw.x - origin[0]); v[1] = (float)(pl.xw.y - origin[1]); v[2] = (float)(pl.xw.z - origin[2]);
+        v[3] = (float)pl.u1.x; v[4] = (float)pl.u1.y; v[5] = (float)pl.u1.z;
+        v[6] = (float)pl.u2.x; v[7] = (float)pl.u2.y; v[8] = (float)pl.u2.z;
+        v[9] = (float)(uw[0] / lw); v[10] = (float)(uw[1] / lw); v[11] = (float)(uw[2] / lw);
+        v[12] = (float)pl.l1; v[13] = (float)pl.l2; v[14] = 0.f; v[15] = 0.f;
+    }
+    cudaError_t e = cudaMemcpyAsync(fs.d_planef, pf.data(), nplane * sizeof(PlaneF), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
 }
 
 int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, unsigned int* nlaunch)
@@ -208,14 +296,16 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         nl++;
     };
     const unsigned int np = a.np, n = a.nentry;
+    const double* org = &a.prm.world_origin.x;
     if (!fs.primed) {
-        // empty cell table, first position update + hash, and the frame of
-        // the FP32 prefilter (centre and radius of the particle cloud)
+        // empty cell table, first position update + hash, and the extent of
+        // the FP32 frame (grid origin to the far side of the particle cloud)
         ok(launch_fill_u32(a.cstart, 0xffffffffu, a.ncell, st));
         ok(cudaMemsetAsync(a.cend, 0, a.ncell * sizeof(unsigned int), st));
         fs.have_prev = false;
-        k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, fs.pos_alt,
-                                                        fs.ep_alt, a.k0, a.v0, np, a.status);
+        k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, a.mass,
+                                                        fs.pos_alt, fs.ep_alt, a.k0, a.v0, np, a.status, fs.rA,
+                                                        fs.rB, fs.rC, fs.rT);
         ok(cudaGetLastError());
         const unsigned int nbb = std::min(kBboxBlocks, std::max(1u, blocks_for(np, 256)));
         k_bbox<<<nbb, 256, 0, st>>>(*a.pos, np, fs.d_bbox);
@@ -225,23 +315,22 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
             e = cudaMemcpyAsync(bb.data(), fs.d_bbox, bb.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return XDEM_ERR_CUDA;
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        for (unsigned int b = 0; b < nbb; ++b)
-            for (int c = 0; c < 3; ++c) {
-                lo[c] = std::min(lo[c], bb[b * 6 + c]);
-                hi[c] = std::max(hi[c], bb[b * 6 + 3 + c]);
-            }
         double r2 = 0.0;
         for (int c = 0; c < 3; ++c) {
-            if (!(hi[c] >= lo[c])) { lo[c] = 0.0; hi[c] = 0.0; }
-            fs.frame_c[c] = 0.5 * (lo[c] + hi[c]);
-            r2 += 0.25 * (hi[c] - lo[c]) * (hi[c] - lo[c]);
+            double lo = 1e300, hi = -1e300;
+            for (unsigned int b = 0; b < nbb; ++b) {
+                lo = std::min(lo, bb[b * 6 + c]);
+                hi = std::max(hi, bb[b * 6 + 3 + c]);
+            }
+            if (!(hi >= lo)) { lo = org[c]; hi = org[c]; }
+            const double far = std::max(std::fabs(lo - org[c]), std::fabs(hi - org[c]));
+            r2 += far * far;
         }
-        // particles may drift: the float frame covers the cloud plus 1 m
+        // particles may drift: the FP32 frame covers the cloud plus 1 m
         const double R = std::sqrt(r2) + 1.0;
         fs.frame_far2 = R * R;
-        // float rounding of two coordinates of size <= R, their difference
-        // and the sum of squares; 4x slack
+        // rounding of two FP32 coordinates of size <= R, their difference and
+        // the sum of squares, with 4x slack
         fs.frame_margin = (float)(16.0 * R * std::ldexp(1.0, -24) + 1e-9);
         fs.primed = true;
     }
@@ -259,11 +348,18 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     unsigned int *sk = nullptr, *sv = nullptr;
     ok(radix_sort_pairs(a.k0, a.v0, a.k1, a.v1, a.hist, n, a.sort_bits, &sk, &sv, st));
     nl += 3 * ((a.sort_bits + 7) / 8) - 1;
-    // positions of this step are in *a.pos (x_{n+1}); *a.ep holds e_{n+1}
-    k_reorder<<<blocks_for(n), kThreads, 0, st>>>(sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev,
-                                                  *a.pos, *a.ep, a.vel, a.ev, a.mass, fs.snap_pos, fs.snap_vel,
-                                                  fs.snap_om, fs.snap_f, fs.frame_c[0], fs.frame_c[1], fs.frame_c[2],
-                                                  fs.frame_far2);
+    if (fs.mixed) {
+        k_reorder_mixed<<<blocks_for(n), kThreads, 0, st>>>(
+            sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev, reinterpret_cast<const float4*>(fs.rA),
+            reinterpret_cast<const float4*>(fs.rB), reinterpret_cast<const float4*>(fs.rC), fs.rT,
+            reinterpret_cast<float4*>(fs.mA), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
+            fs.mT);
+    } else {
+        k_reorder_fp64<<<blocks_for(n), kThreads, 0, st>>>(sk, sv, n, np, a.cstart, a.cend, a.sorted_index,
+                                                           fs.skey_prev, *a.pos, *a.ep, a.vel, a.ev, a.mass,
+                                                           fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, org[0],
+                                                           org[1], org[2], fs.frame_far2);
+    }
     ok(cudaGetLastError());
     fs.have_prev = true;
 
@@ -272,8 +368,12 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.np = np;
     c.nentry = n;
     c.vel_compat = a.vel_compat;
+    c.rolling = a.rolling;
     c.snap_pos = fs.snap_pos; c.snap_vel = fs.snap_vel; c.snap_om = fs.snap_om; c.snap_f = fs.snap_f;
     c.margin = fs.frame_margin;
+    c.mA = fs.mA; c.mB = fs.mB; c.mC = fs.mC; c.mT = fs.mT;
+    c.rA = fs.rA; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
+    c.planef = fs.d_planef;
     c.sorted_index = a.sorted_index; c.cstart = a.cstart; c.cend = a.cend; c.skey = fs.skey_prev;
     c.pos_cur = *a.pos; c.pos_next = fs.pos_alt; c.ep_cur = *a.ep; c.ep_next = fs.ep_alt;
     c.vel = a.vel; c.acc = a.acc; c.ev = a.ev; c.ea = a.ea; c.mass = a.mass; c.inertia = a.inertia;

@@ -234,7 +234,9 @@ int upload_bodies(xdem_sim* s)
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) return cerr(e);
     s->dirty_bodies = false;
-    return fused_set_bodies(s->fs, s->d_planes, (unsigned int)s->planes.size(), s->d_body, s->d_mp);
+    const double org[3] = {s->prm.world_origin.x, s->prm.world_origin.y, s->prm.world_origin.z};
+    return fused_set_bodies(s->fs, s->d_planes, (unsigned int)s->planes.size(), s->d_body, s->d_mp,
+                            s->planes.data(), org, s->st);
 }
 
 // ---------------------------------------------------------------- launcher-order step
@@ -348,6 +350,8 @@ FusedArgs fused_args(xdem_sim* s)
     a.body = s->d_body; a.mp = s->d_mp;
     a.bsums = s->bsums; a.wrench = s->wrench;
     a.status = s->d_status;
+    a.rolling = s->has_pp && s->pp_cp.rfric != 0.0;
+    for (const device_contact_property& cp : s->body_cp) a.rolling = a.rolling || cp.rfric != 0.0;
     return a;
 }
 
