@@ -153,22 +153,23 @@ __device__ __forceinline__ int sext(unsigned int v, int bits)
 // whose unwrapped cells are more than one cell apart are aliases of the
 // wrapping hash and are skipped (the FP64 form skips them by distance).
 __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int oid, unsigned int gx,
-                                          unsigned int gy, unsigned int gz, float4 Ai, unsigned int Ti, d4 iv,
-                                          d4 io, d3& F, d3& M, d3& tma, double& res, unsigned int& bits)
+                                          unsigned int gy, unsigned int gz, float4 Ai, unsigned int Ti, float4 Bi,
+                                          float4 Ci, d3& F, d3& M, d3& tma, double& res, unsigned int& bits)
 {
     const device_dem_parameters& p = c.prm;
     const int model = p.contact_model;
     const double dt = p.dt;
     const mat_pair mp = c.mp[0];
     const MatR<float> mr = mat_r<float>(mp);
-    const float cs = (float)p.cell_size;
+    const bool coh = mr.coh;
+    const float cs = c.cs_f;
     const unsigned int sid = oid * MAX_P2P_COUNT;
     unsigned int old_count = c.pp_count_old[oid];
     if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
     const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
-    const float ir = Ai.w, im = (float)iv.w;
-    const V3<float> ivel = v3<float>((float)iv.x, (float)iv.y, (float)iv.z);
-    const V3<float> iom = v3<float>((float)io.x, (float)io.y, (float)io.z);
+    const float ir = Ai.w, im = Bi.w;
+    const V3<float> ivel = v3<float>(Bi.x, Bi.y, Bi.z);
+    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
     V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0), tm = v3<float>(0, 0, 0);
     CSum fx, fy, fz, mx, my, mz;
     float rs = 0.f;
@@ -180,23 +181,23 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                 const unsigned int start = c.cstart[h];
                 if (start == 0xffffffffu) continue;
                 const unsigned int end = c.cend[h];
+                // every entry of this cell that is not an alias of the wrapping
+                // hash lies exactly one stencil step (x, y, z) from our cell
+                const unsigned int want = pack_cell((int)ux + x, (int)uy + y, (int)uz + z);
+                const float sx = (float)x * cs - Ai.x, sy = (float)y * cs - Ai.y, sz = (float)z * cs - Ai.z;
                 for (unsigned int j = start; j < end; ++j) {
-                    const unsigned int k = c.sorted_index[j];
-                    if (k == oid || k >= c.np) continue;
-                    const unsigned int Tj = c.mT[j];
-                    const int dx = sext((Tj & 2047u) - ux, 11);
-                    const int dy = sext(((Tj >> 11) & 2047u) - uy, 11);
-                    const int dz = sext((Tj >> 22) - uz, 10);
-                    if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
+                    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
+                    if (it.y != want || it.x == oid || it.x >= c.np) continue;
+                    const unsigned int k = it.x;
                     const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
-                    const V3<float> rp = v3<float>((float)dx * cs + (Aj.x - Ai.x), (float)dy * cs + (Aj.y - Ai.y),
-                                                   (float)dz * cs + (Aj.z - Ai.z));
+                    const V3<float> rp = v3<float>(Aj.x + sx, Aj.y + sy, Aj.z + sz);
                     const float rr = ir + Aj.w;
                     const float d2 = tdot(rp, rp);
+                    if (!(d2 < rr * rr) && !coh) continue;
                     const float dist = sqrtf(d2);
                     const float cdist = rr - dist;
                     if (!(cdist > 0.f)) {
-                        if (!mp.coh) continue;
+                        if (!coh) continue;
                         const double csd = limit_cohesion_depth(mp, ir, Aj.w);
                         if (!(fabs((double)cdist) < fabs(csd))) continue;
                         const V3<float> unit = rp / dist;
@@ -229,7 +230,7 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                     const V3<float> rv = (jvel + tcross(jom, dcpr_j)) - (ivel + tcross(iom, dcpr));
                     const FC<float> fc = fconst_r<float>(mr, model, ir, Aj.w, im, Bj.w);
                     float fca = 0.f;
-                    if (mp.coh) {
+                    if (coh) {
                         const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
                         const double fdn = (double)fc.vn * (double)tdot(rv, unit);
                         fca = (float)(-cohesion_force(mp, ir, Aj.w, fsn + fdn));
@@ -306,12 +307,12 @@ __device__ __forceinline__ float4 f4(d4 a) { return make_float4((float)a.x, (flo
 // mass) are FP32.  Euler parameters are renormalised by the second-order
 // expansion of 1/sqrt(s) around s = 1 (|s - 1| ~ (dt |e_dot|)^2).  Writes the
 // FP32 record of the next step.
-__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, d4 iv, d3 F, d3 M,
+__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float4 Bi, d3 F, d3 M,
                                            unsigned int& bits)
 {
     const device_dem_parameters& p = c.prm;
     const double dt = p.dt, hdt = 0.5 * p.dt, h2 = p.half2dt;
-    const float inv_m = 1.0f / (float)iv.w;
+    const float inv_m = 1.0f / Bi.w;
     const d3 g3 = dv3(p.gravity);
     const d3 a_new = mk3(F.x * (double)inv_m + g3.x, F.y * (double)inv_m + g3.y, F.z * (double)inv_m + g3.z);
     const d4 e = ld4(c.ep_cur, oid);
@@ -337,18 +338,20 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
     const d3 xn = mk3(ip.x + (dt * v.x + h2 * a_new.x), ip.y + (dt * v.y + h2 * a_new.y),
                       ip.z + (dt * v.z + h2 * a_new.z));
     st4(c.pos_next, oid, mk4(xn.x, xn.y, xn.z, ip.w));
-    if (!(isfinite(xn.x) && isfinite(xn.y) && isfinite(xn.z))) bits |= XDEM_ERR_NONFINITE;
-    const double inv_cs = 1.0 / p.cell_size;
+    // cell of the new centre (FP64 floor: a sphere within 1e-7 m of a cell
+    // face must not be binned one cell off, or a contact at distance just
+    // under the cell size could fall outside the 27-cell stencil)
     const double rx = xn.x - p.world_origin.x, ry = xn.y - p.world_origin.y, rz = xn.z - p.world_origin.z;
-    const double fx = floor(rx * inv_cs), fy = floor(ry * inv_cs), fz = floor(rz * inv_cs);
+    const double fx = floor(rx * c.inv_cs), fy = floor(ry * c.inv_cs), fz = floor(rz * c.inv_cs);
     const int gxn = __double2int_rz(fx), gyn = __double2int_rz(fy), gzn = __double2int_rz(fz);
     c.k_out[oid] = grid_hash(p, gxn, gyn, gzn);
     c.v_out[oid] = oid;
     const float3 w = ang_vel_f(f4(e2), f4(av));
-    reinterpret_cast<float4*>(c.rA)[oid] =
-        make_float4((float)(rx - fx * p.cell_size), (float)(ry - fy * p.cell_size), (float)(rz - fz * p.cell_size),
-                    (float)ip.w);
-    reinterpret_cast<float4*>(c.rB)[oid] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)iv.w);
+    const float4 A = make_float4((float)(rx - fx * p.cell_size), (float)(ry - fy * p.cell_size),
+                                 (float)(rz - fz * p.cell_size), (float)ip.w);
+    if (!(isfinite(A.x) && isfinite(A.y) && isfinite(A.z))) bits |= XDEM_ERR_NONFINITE;
+    reinterpret_cast<float4*>(c.rA)[oid] = A;
+    reinterpret_cast<float4*>(c.rB)[oid] = make_float4((float)v.x, (float)v.y, (float)v.z, Bi.w);
     reinterpret_cast<float4*>(c.rC)[oid] = make_float4(w.x, w.y, w.z, 0.f);
     c.rT[oid] = pack_cell(gxn, gyn, gzn);
     if (bits) atomicOr(c.status, bits);
@@ -370,7 +373,7 @@ k_fused_contact(const ContactLaunch c)
     constexpr bool MIXED = sizeof(R) == sizeof(float);
     d4 ip = mk4(0, 0, 0, 0), iv = mk4(0, 0, 0, 0), io = mk4(0, 0, 0, 0);
     float4 ipf = make_float4(0.f, 0.f, 0.f, -1.f);
-    float4 mAi = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 mAi = make_float4(0.f, 0.f, 0.f, 0.f), mBi = mAi, mCi = mAi;
     unsigned int mTi = 0;
     unsigned int gx = 0, gy = 0, gz = 0;
     if (live) {
@@ -378,12 +381,11 @@ k_fused_contact(const ContactLaunch c)
             // FP32 record of the snapshot; the FP64 centre for plane/mesh
             // geometry and for the state update
             mAi = reinterpret_cast<const float4*>(c.mA)[s];
-            mTi = c.mT[s];
-            const float4 B = reinterpret_cast<const float4*>(c.mB)[s];
-            const float4 Cw = reinterpret_cast<const float4*>(c.mC)[s];
+            mTi = reinterpret_cast<const uint2*>(c.mIT)[s].y;
+            mBi = reinterpret_cast<const float4*>(c.mB)[s];
+            mCi = reinterpret_cast<const float4*>(c.mC)[s];
             ip = ld4(c.pos_cur, oid);
-            iv = mk4(B.x, B.y, B.z, B.w);
-            io = mk4(Cw.x, Cw.y, Cw.z, 0.0);
+            iv.w = mBi.w;
             if (c.nplane)
                 ipf = make_float4((float)(ip.x - p.world_origin.x), (float)(ip.y - p.world_origin.y),
                                   (float)(ip.z - p.world_origin.z), mAi.w);
@@ -402,15 +404,21 @@ k_fused_contact(const ContactLaunch c)
     }
     const d3 ipos = mk3(ip.x, ip.y, ip.z);
     const double ir = ip.w, im = iv.w;
-    const V3<R> ivel = cvt<R>(mk3(iv.x, iv.y, iv.z));
-    const V3<R> iom = cvt<R>(mk3(io.x, io.y, io.z));
+    V3<R> ivel, iom;
+    if constexpr (MIXED) {
+        ivel = v3<R>(mBi.x, mBi.y, mBi.z);
+        iom = v3<R>(mCi.x, mCi.y, mCi.z);
+    } else {
+        ivel = cvt<R>(mk3(iv.x, iv.y, iv.z));
+        iom = cvt<R>(mk3(io.x, io.y, io.z));
+    }
     d3 F = mk3(0, 0, 0), M = mk3(0, 0, 0), tma = mk3(0, 0, 0);
     double res = 0.0;
     unsigned int bits = 0;
 
     // ------------------------------------------------ particle-particle (impl:613-733)
     if constexpr (MIXED) {
-        if (live && c.has_pp) p2p_mixed(c, oid, gx, gy, gz, mAi, mTi, iv, io, F, M, tma, res, bits);
+        if (live && c.has_pp) p2p_mixed(c, oid, gx, gy, gz, mAi, mTi, mBi, mCi, F, M, tma, res, bits);
     } else if (live && c.has_pp) {
         const mat_pair mp = c.mp[0];
         const MatR<R> mr = mat_r<R>(mp);
@@ -743,7 +751,7 @@ k_fused_contact(const ContactLaunch c)
     const double Tr = res;
     if (Tr) {
         const double J = c.inertia[oid];  // scalar read of the double3 array, as impl:2434
-        const d3 om = mk3(io.x, io.y, io.z);
+        const d3 om = MIXED ? mk3(mCi.x, mCi.y, mCi.z) : mk3(io.x, io.y, io.z);
         const d3 T = (J * p.dt) * om - tma;
         const double lT = length(T);
         if (lT && Tr) {
@@ -754,7 +762,7 @@ k_fused_contact(const ContactLaunch c)
     }
 
     if constexpr (MIXED) {
-        mixed_tail(c, oid, ip, iv, F, M, bits);
+        mixed_tail(c, oid, ip, mBi, F, M, bits);
         return;
     }
 

@@ -54,7 +54,7 @@ struct FusedState {
     float* mA = nullptr;        // [nentry*4] offset from own cell corner, r
     float* mB = nullptr;        // [nentry*4] vx, vy, vz, mass
     float* mC = nullptr;        // [nentry*4] wx, wy, wz, 0
-    unsigned int* mT = nullptr; // [nentry] packed unwrapped cell coordinates
+    unsigned int* mIT = nullptr; // [nentry*2] (original id, packed unwrapped cell)
     float* rA = nullptr;        // [np*4] next-step records written by the contact kernel
     float* rB = nullptr;
     float* rC = nullptr;
@@ -133,12 +133,14 @@ struct ContactLaunch {
     const float* mA;
     const float* mB;
     const float* mC;
-    const unsigned int* mT;
+    const unsigned int* mIT;
     float* rA;
     float* rB;
     float* rC;
     unsigned int* rT;
     const PlaneF* planef;
+    double inv_cs;   // 1 / cell size
+    float cs_f;      // cell size in FP32
     const unsigned int* sorted_index;
     const unsigned int* cstart;
     const unsigned int* cend;

@@ -29,8 +29,8 @@ cudaError_t dalloc(T*& p, size_t n)
 
 // FP32 snapshot record of one sphere for the mixed contact kernel: offset of
 // the centre from its cell corner, radius, packed cell, velocity, mass, spin.
-__device__ __forceinline__ void mixed_record(const device_dem_parameters& p, double inv_cs, d3 x, double r, d3 v,
-                                             double m, d3 w, float4& A, float4& B, float4& C, unsigned int& T)
+__device__ __forceinline__ int3v mixed_record(const device_dem_parameters& p, double inv_cs, d3 x, double r, d3 v,
+                                              double m, d3 w, float4& A, float4& B, float4& C, unsigned int& T)
 {
     const double rx = x.x - p.world_origin.x, ry = x.y - p.world_origin.y, rz = x.z - p.world_origin.z;
     const double fx = floor(rx * inv_cs), fy = floor(ry * inv_cs), fz = floor(rz * inv_cs);
@@ -38,7 +38,9 @@ __device__ __forceinline__ void mixed_record(const device_dem_parameters& p, dou
                     (float)r);
     B = make_float4((float)v.x, (float)v.y, (float)v.z, (float)m);
     C = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
-    T = pack_cell(__double2int_rz(fx), __double2int_rz(fy), __double2int_rz(fz));
+    const int3v g{__double2int_rz(fx), __double2int_rz(fy), __double2int_rz(fz)};
+    T = pack_cell(g.x, g.y, g.z);
+    return g;
 }
 
 // Position update of the first step (impl:135-147) into the alternate
@@ -62,18 +64,21 @@ __global__ void k_prologue(device_dem_parameters p, const double* pos, const dou
     const d3 x = mk3(q.x + d.x, q.y + d.y, q.z + d.z);
     st4(pos_next, i, mk4(x.x, x.y, x.z, q.w));
     if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(status, (unsigned int)XDEM_ERR_NONFINITE);
-    const int3v g = grid_pos(p, x);
-    key[i] = grid_hash(p, g.x, g.y, g.z);
-    val[i] = i;
+    int3v g;
     if (rA) {
+        // mixed form: the key's cell is the cell the FP32 record is relative to
         float4 A, B, C;
         unsigned int T;
-        mixed_record(p, 1.0 / p.cell_size, x, q.w, v, mass[i], ang_vel(en, ld4(ev, i)), A, B, C, T);
+        g = mixed_record(p, 1.0 / p.cell_size, x, q.w, v, mass[i], ang_vel(en, ld4(ev, i)), A, B, C, T);
         reinterpret_cast<float4*>(rA)[i] = A;
         reinterpret_cast<float4*>(rB)[i] = B;
         reinterpret_cast<float4*>(rC)[i] = C;
         rT[i] = T;
+    } else {
+        g = grid_pos(p, x);
     }
+    key[i] = grid_hash(p, g.x, g.y, g.z);
+    val[i] = i;
 }
 
 // Bounding box of the positions: block min/max into out[block*6].
@@ -148,7 +153,7 @@ __global__ void k_reorder_fp64(const unsigned int* sk, const unsigned int* sv, u
 __global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
                                 unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index,
                                 unsigned int* skey, const float4* rA, const float4* rB, const float4* rC,
-                                const unsigned int* rT, float4* mA, float4* mB, float4* mC, unsigned int* mT)
+                                const unsigned int* rT, float4* mA, float4* mB, float4* mC, uint2* mIT)
 {
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -161,24 +166,29 @@ __global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, 
         mA[s] = rA[oid];
         mB[s] = rB[oid];
         mC[s] = rC[oid];
-        mT[s] = rT[oid];
+        mIT[s] = make_uint2(oid, rT[oid]);
     } else {
         mA[s] = make_float4(0.f, 0.f, 0.f, -1.f);
-        mT[s] = 0xffffffffu;
+        mIT[s] = make_uint2(oid, 0xffffffffu);
     }
 }
 
-__global__ void k_body_sums(const double* bsums, unsigned int nblocks, unsigned int nbody, double* wrench)
+// One block of 256 threads per (body, component): sum of the contact
+// kernel's per-block partials.
+__global__ void k_body_sums(const double* bsums, unsigned int nblocks, double* wrench)
 {
-    // one warp per (body, component)
-    const unsigned int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const unsigned int lane = threadIdx.x & 31;
-    if (w >= nbody * 6) return;
-    const unsigned int b = w / 6, c = w % 6;
+    __shared__ double sm[8];
+    const unsigned int b = blockIdx.x / 6, c = blockIdx.x % 6;
     double s = 0.0;
-    for (unsigned int i = lane; i < nblocks; i += 32) s += bsums[((size_t)b * nblocks + i) * 6 + c];
+    for (unsigned int i = threadIdx.x; i < nblocks; i += blockDim.x) s += bsums[((size_t)b * nblocks + i) * 6 + c];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) wrench[b * 6 + c] = s;
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += sm[w];
+        wrench[b * 6 + c] = t;
+    }
 }
 
 __global__ void k_energy(const double* vel, const double* ep, const double* ev, const double* mass,
@@ -222,7 +232,7 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.mA, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mB, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mC, (size_t)nentry * 4);
-        if (e == cudaSuccess) e = dalloc(fs.mT, nentry);
+        if (e == cudaSuccess) e = dalloc(fs.mIT, (size_t)nentry * 2);
         if (e == cudaSuccess) e = dalloc(fs.rA, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rC, (size_t)np * 4);
@@ -249,7 +259,7 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 void fused_free(FusedState& fs)
 {
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mB, fs.mC,
-                  fs.mT, fs.rA, fs.rB, fs.rC, fs.rT, fs.pp_count2, fs.pp_id2, fs.pp_tsd2, fs.skey_prev,
+                  fs.mIT, fs.rA, fs.rB, fs.rC, fs.rT, fs.pp_count2, fs.pp_id2, fs.pp_tsd2, fs.skey_prev,
                   fs.d_energy, fs.d_bbox, fs.d_planef};
     for (void* q : ps)
         if (q) cudaFree(q);
@@ -353,7 +363,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
             sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev, reinterpret_cast<const float4*>(fs.rA),
             reinterpret_cast<const float4*>(fs.rB), reinterpret_cast<const float4*>(fs.rC), fs.rT,
             reinterpret_cast<float4*>(fs.mA), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
-            fs.mT);
+            reinterpret_cast<uint2*>(fs.mIT));
     } else {
         k_reorder_fp64<<<blocks_for(n), kThreads, 0, st>>>(sk, sv, n, np, a.cstart, a.cend, a.sorted_index,
                                                            fs.skey_prev, *a.pos, *a.ep, a.vel, a.ev, a.mass,
@@ -371,9 +381,11 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.rolling = a.rolling;
     c.snap_pos = fs.snap_pos; c.snap_vel = fs.snap_vel; c.snap_om = fs.snap_om; c.snap_f = fs.snap_f;
     c.margin = fs.frame_margin;
-    c.mA = fs.mA; c.mB = fs.mB; c.mC = fs.mC; c.mT = fs.mT;
+    c.mA = fs.mA; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
     c.rA = fs.rA; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
     c.planef = fs.d_planef;
+    c.inv_cs = 1.0 / a.prm.cell_size;
+    c.cs_f = (float)a.prm.cell_size;
     c.sorted_index = a.sorted_index; c.cstart = a.cstart; c.cend = a.cend; c.skey = fs.skey_prev;
     c.pos_cur = *a.pos; c.pos_next = fs.pos_alt; c.ep_cur = *a.ep; c.ep_next = fs.ep_alt;
     c.vel = a.vel; c.acc = a.acc; c.ev = a.ev; c.ea = a.ea; c.mass = a.mass; c.inertia = a.inertia;
@@ -397,8 +409,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody) {
-        const unsigned int warps = a.nbody * 6;
-        k_body_sums<<<(warps + 7) / 8, 256, 0, st>>>(a.bsums, c.nblocks, a.nbody, a.wrench);
+        k_body_sums<<<a.nbody * 6, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench);
         ok(cudaGetLastError());
     }
     if (e != cudaSuccess) return XDEM_ERR_CUDA;

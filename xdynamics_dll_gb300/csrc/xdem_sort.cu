@@ -38,42 +38,64 @@ k_radix_upsweep(const unsigned int* keys, unsigned int n, int shift, unsigned in
     hist[threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of `len` counters by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_radix_scan(unsigned int* hist, unsigned int len)
+// Block-wide exclusive scan of one value per thread (256 threads); returns
+// the prefix and writes the block total to *total.
+__device__ __forceinline__ unsigned int block_exclusive_scan(unsigned int v, unsigned int* sm /* [8] */,
+                                                             unsigned int* total)
 {
-    __shared__ unsigned int part[1024];
-    const unsigned int per = (len + 1023) / 1024;
-    const unsigned int b = threadIdx.x * per;
-    const unsigned int e = b + per < len ? b + per : len;
-    unsigned int s = 0;
-    for (unsigned int i = b; i < e; ++i) s += hist[i];
-    part[threadIdx.x] = s;
+    const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    unsigned int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (unsigned int)o) x += y;
+    }
+    if (lane == 31) sm[warp] = x;
     __syncthreads();
-    // Hillis-Steele inclusive scan of the 1024 partial sums
-    for (int o = 1; o < 1024; o <<= 1) {
-        const unsigned int v = threadIdx.x >= (unsigned int)o ? part[threadIdx.x - o] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    unsigned int woff = 0, tot = 0;
+    for (unsigned int w = 0; w < kSortThreads / 32; ++w) {
+        const unsigned int c = sm[w];
+        woff += w < warp ? c : 0u;
+        tot += c;
     }
-    unsigned int run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-    for (unsigned int i = b; i < e; ++i) {
-        const unsigned int v = hist[i];
-        hist[i] = run;
-        run += v;
+    __syncthreads();
+    *total = tot;
+    return woff + x - v;
+}
+
+// One block per digit: exclusive scan of that digit's per-tile counts (one
+// row of the digit-major table), row total into totals[digit].
+__global__ void __launch_bounds__(kSortThreads) k_radix_scan(unsigned int* hist, unsigned int ntiles,
+                                                             unsigned int* totals)
+{
+    __shared__ unsigned int sm[kSortThreads / 32];
+    unsigned int* row = hist + (size_t)blockIdx.x * ntiles;
+    unsigned int carry = 0;
+    for (unsigned int base = 0; base < ntiles; base += kSortThreads) {
+        const unsigned int i = base + threadIdx.x;
+        const unsigned int v = i < ntiles ? row[i] : 0u;
+        unsigned int tot;
+        const unsigned int ex = block_exclusive_scan(v, sm, &tot);
+        if (i < ntiles) row[i] = carry + ex;
+        carry += tot;
     }
+    if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kSortThreads)
 k_radix_scatter(const unsigned int* kin, const unsigned int* vin, unsigned int* kout, unsigned int* vout,
-                unsigned int n, int shift, const unsigned int* hist, unsigned int ntiles)
+                unsigned int n, int shift, const unsigned int* hist, unsigned int ntiles, const unsigned int* totals)
 {
     constexpr int kWarps = kSortThreads / 32;
     __shared__ unsigned int base[kRadix];
     __shared__ unsigned int run[kRadix];
     __shared__ unsigned int wcnt[kWarps][kRadix + 1];
+    __shared__ unsigned int scan_sm[kSortThreads / 32];
     const unsigned int tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    base[tid] = hist[tid * ntiles + blockIdx.x];
+    // start of each digit = exclusive scan of the digit totals, plus this
+    // tile's offset within the digit
+    unsigned int tot;
+    const unsigned int dbase = block_exclusive_scan(totals[tid], scan_sm, &tot);
+    base[tid] = dbase + hist[tid * ntiles + blockIdx.x];
     run[tid] = 0;
     const unsigned int lt = (1u << lane) - 1u;
     const unsigned int tile = blockIdx.x * kTile;
@@ -113,7 +135,7 @@ k_radix_scatter(const unsigned int* kin, const unsigned int* vin, unsigned int* 
 size_t radix_hist_size(unsigned int n)
 {
     const size_t ntiles = (n + kTile - 1) / kTile;
-    return (ntiles ? ntiles : 1) * kRadix;
+    return (ntiles ? ntiles : 1) * kRadix + kRadix;  // table + digit totals
 }
 
 cudaError_t radix_sort_pairs(unsigned int* k0, unsigned int* v0, unsigned int* k1, unsigned int* v1,
@@ -124,11 +146,12 @@ cudaError_t radix_sort_pairs(unsigned int* k0, unsigned int* v0, unsigned int* k
     *out_v = v0;
     if (n < 2) return cudaSuccess;
     const unsigned int ntiles = (n + kTile - 1) / kTile;
+    unsigned int* totals = hist + (size_t)ntiles * kRadix;
     unsigned int *ki = k0, *vi = v0, *ko = k1, *vo = v1;
     for (int shift = 0; shift < bits; shift += 8) {
         k_radix_upsweep<<<ntiles, kSortThreads, 0, st>>>(ki, n, shift, hist, ntiles);
-        k_radix_scan<<<1, 1024, 0, st>>>(hist, ntiles * kRadix);
-        k_radix_scatter<<<ntiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, hist, ntiles);
+        k_radix_scan<<<kRadix, kSortThreads, 0, st>>>(hist, ntiles, totals);
+        k_radix_scatter<<<ntiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, hist, ntiles, totals);
         unsigned int* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
     }
