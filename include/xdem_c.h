@@ -193,6 +193,24 @@ XDEM_API int cu_reorderDataAndFindCellStart(unsigned int* hash,
                                             unsigned int* sorted_index,
                                             unsigned int np,
                                             unsigned int ncell);
+/* No counterpart in the reference.  Same arguments and result as
+ * cu_reorderDataAndFindCellStart, but it allocates no device memory: the sort
+ * scratch is a fixed array inside the library (about 2.2 MB on every GPU that
+ * loads the library, kept until the process exits), for callers that may not
+ * call cudaMalloc -- a step being recorded into a CUDA graph, a real-time
+ * loop, a host whose device memory belongs to an external pool.
+ * np (particles + mesh spheres) must not exceed 262144; larger calls return
+ * XDEM_ERR_ARG without touching the arrays.  The first call on a device looks
+ * up the array's device address; make that first call before any stream
+ * capture.  All calls share the array, so calls whose kernels overlap on the
+ * GPU (e.g. on two streams) race and must be serialised by the caller. */
+XDEM_API int cu_reorderDataAndFindCellStart_noalloc(unsigned int* hash,
+                                                    unsigned int* index,
+                                                    unsigned int* cstart,
+                                                    unsigned int* cend,
+                                                    unsigned int* sorted_index,
+                                                    unsigned int np,
+                                                    unsigned int ncell);
 /* decl:293-299, def:126-143 */
 XDEM_API int cu_calculate_p2p(double* pos, double* ep, double* vel,
                               double* omega, double* force, double* moment,

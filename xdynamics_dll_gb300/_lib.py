@@ -35,6 +35,7 @@ _SIGS = {
     "cu_calculateHashAndIndex": ([vp, vp, vp, u32, u32], i32),
     "cu_calculateHashAndIndexForPolygonSphere": ([vp, vp, u32, u32, vp], i32),
     "cu_reorderDataAndFindCellStart": ([vp] * 5 + [u32, u32], i32),
+    "cu_reorderDataAndFindCellStart_noalloc": ([vp] * 5 + [u32, u32], i32),
     "cu_calculate_p2p": ([vp] * 16 + [u32], i32),
     "cu_plane_contact_force": ([vp] * 15 + [u32], i32),
     "cu_particle_polygonObject_collision": ([vp] * 19 + [u32, u32], i32),

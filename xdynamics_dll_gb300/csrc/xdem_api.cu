@@ -154,6 +154,11 @@ int finish_wrench(DevCtx* c)
 
 }  // namespace
 
+namespace xdem {
+cudaStream_t launcher_stream() { return t_stream; }
+int launcher_set_status(int s) { return set_status(s); }
+}  // namespace xdem
+
 // ============================================================================
 // Library control
 // ============================================================================

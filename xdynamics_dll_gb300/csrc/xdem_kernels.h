@@ -103,6 +103,11 @@ cudaError_t launch_reduce_sum(const double* in, unsigned int n, double* tmp, dou
 // Sum of nblocks x 6 block partials into out[6] (device).
 cudaError_t launch_sum_block_partials(const double* partials, unsigned int nblocks, double* out6, cudaStream_t st);
 
+// Stream of the launcher surface on this host thread (xdem_set_stream) and
+// the per-thread status of its last call.
+cudaStream_t launcher_stream();
+int launcher_set_status(int s);
+
 // ---------------------------------------------------------------- radix sort
 // Stable LSD sort of (keys, vals) by the low `bits` bits of the keys.  Uses
 // ping-pong buffers k1/v1 (n each) and `hist` (radix_hist_size(n) uints).
