@@ -55,7 +55,7 @@ def load_peaks():
 
 def profile_traffic():
     """DRAM bytes per sphere of the contact kernel from the committed ncu
-    summary (profiles/*contact*.md, line 'dram_bytes_per_sphere: X')."""
+    summary (profiles/*contact*.md, line 'dram_bytes_per_sphere_mixed: X')."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
         return None, None
@@ -127,6 +127,21 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_totals(secs64, secsx, secs_e2e_per_unit, ws, n, steps, device):
+    """Whole-job numbers of N independent replicas: each rank timed its own
+    copy of the workload; the job ends with the slowest rank, so every time
+    is the MAX over ranks (one all_reduce after the timed region, none on
+    the data path).  Returns (value_mixed, value_fp64, e2e_value, secs64,
+    secsx) with the values summed over the ws replicas."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([secs64, secsx, secs_e2e_per_unit], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs64, secsx, secs_e2e_per_unit = t.tolist()
+    return (ws * n * steps / secsx, ws * n * steps / secs64, ws / secs_e2e_per_unit, secs64, secsx)
+
+
 def make_scene(n):
     from xdynamics_dll_gb300 import scenes
     return scenes.dam_break(n_target=n)
@@ -166,7 +181,7 @@ def new_sim(scene, precision):
     return sm
 
 
-def run_cpu_baseline(scene, budget_s=15.0, max_steps=40):
+def run_cpu_baseline(scene, budget_s=15.0, max_steps=400):
     """The CPU oracle (plain C restatement of the reference kernels, OpenMP
     over particles) on a bounded sample of the same workload: the full scene
     for as many steps as fit in `budget_s` seconds after one warm-up step."""
@@ -301,16 +316,9 @@ def main():
     e2e = bench_e2e(smx, scene, torch, min(args.steps, 200))
     smx.close()
 
-    secs64, secsx = r64["secs"], rmx["secs"]
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([secs64, secsx, 1.0 / e2e["value"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        secs64, secsx, inv_e2e = t.tolist()
-        e2e["value"] = ws / inv_e2e
     n = scene.np_
-    value = ws * n * args.steps / secsx
-    value64 = ws * n * args.steps / secs64
+    value, value64, e2e["value"], secs64, secsx = replica_totals(
+        r64["secs"], rmx["secs"], 1.0 / e2e["value"], ws, n, args.steps, torch.device("cuda", local))
     if rank != 0:
         return
 
