@@ -1,7 +1,7 @@
-// xdem_fused.cuh -- the fused contact + integration kernel, generic in the
-// arithmetic type of contact geometry and forces (R = double: plain FP64;
-// R = float: mixed precision with FP64 positions, velocities, history and
-// force/torque accumulation).
+// xdem_fused.cuh -- the fused contact + integration kernel of the plain FP64
+// form, and the contact-model helpers it shares with the mixed form
+// (xdem_fused_mixed.cu), which are generic in the arithmetic type R of the
+// contact geometry and forces.
 //
 // One thread per cell-sorted entry.  Neighbours are read from the sorted
 // snapshot (coalesced along a cell, cached across the 27-cell stencil); an
@@ -128,237 +128,8 @@ __device__ __forceinline__ void emit_body(double f6[6], bool any, double* out, d
         for (int c = 0; c < 6; ++c) out[c] = f6[c];
 }
 
-// Compensated FP32 sum (Knuth's TwoSum): hi + lo holds the running sum with
-// the rounding error of every addition kept, about 48 significant bits.
-struct CSum {
-    float hi = 0.f, lo = 0.f;
-    __device__ __forceinline__ void add(float b)
-    {
-        const float t = hi + b;
-        const float bp = t - hi;
-        lo += (hi - (t - bp)) + (b - bp);
-        hi = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-
-__device__ __forceinline__ int sext(unsigned int v, int bits)
-{
-    return ((int)(v << (32 - bits))) >> (32 - bits);
-}
-
-// Particle-particle contact of the mixed form (impl:613-733 in FP32).  The
-// relative position of a neighbour is (cell difference) * cell size +
-// (offset difference), both small, so FP32 resolves it to ~1e-9 m.  Entries
-// whose unwrapped cells are more than one cell apart are aliases of the
-// wrapping hash and are skipped (the FP64 form skips them by distance).
-__device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int oid, unsigned int gx,
-                                          unsigned int gy, unsigned int gz, float4 Ai, unsigned int Ti, float4 Bi,
-                                          float4 Ci, d3& F, d3& M, d3& tma, double& res, unsigned int& bits)
-{
-    const device_dem_parameters& p = c.prm;
-    const int model = p.contact_model;
-    const double dt = p.dt;
-    const mat_pair mp = c.mp[0];
-    const MatR<float> mr = mat_r<float>(mp);
-    const bool coh = mr.coh;
-    const float cs = c.cs_f;
-    const unsigned int sid = oid * MAX_P2P_COUNT;
-    unsigned int old_count = c.pp_count_old[oid];
-    if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
-    const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
-    const float ir = Ai.w, im = Bi.w;
-    const V3<float> ivel = v3<float>(Bi.x, Bi.y, Bi.z);
-    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
-    V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0), tm = v3<float>(0, 0, 0);
-    CSum fx, fy, fz, mx, my, mz;
-    float rs = 0.f;
-    unsigned int cnt = 0;
-    for (int z = -1; z <= 1; ++z)
-        for (int y = -1; y <= 1; ++y)
-            for (int x = -1; x <= 1; ++x) {
-                const unsigned int h = grid_hash(p, (int)gx + x, (int)gy + y, (int)gz + z);
-                const unsigned int start = c.cstart[h];
-                if (start == 0xffffffffu) continue;
-                const unsigned int end = c.cend[h];
-                // every entry of this cell that is not an alias of the wrapping
-                // hash lies exactly one stencil step (x, y, z) from our cell
-                const unsigned int want = pack_cell((int)ux + x, (int)uy + y, (int)uz + z);
-                const float sx = (float)x * cs - Ai.x, sy = (float)y * cs - Ai.y, sz = (float)z * cs - Ai.z;
-                for (unsigned int j = start; j < end; ++j) {
-                    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
-                    if (it.y != want || it.x == oid || it.x >= c.np) continue;
-                    const unsigned int k = it.x;
-                    const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
-                    const V3<float> rp = v3<float>(Aj.x + sx, Aj.y + sy, Aj.z + sz);
-                    const float rr = ir + Aj.w;
-                    const float d2 = tdot(rp, rp);
-                    if (!(d2 < rr * rr) && !coh) continue;
-                    const float dist = sqrtf(d2);
-                    const float cdist = rr - dist;
-                    if (!(cdist > 0.f)) {
-                        if (!coh) continue;
-                        const double csd = limit_cohesion_depth(mp, ir, Aj.w);
-                        if (!(fabs((double)cdist) < fabs(csd))) continue;
-                        const V3<float> unit = rp / dist;
-                        const double f = jkr_separation_force(mp, ir, Aj.w);
-                        const float cf = (float)cohesion_force(mp, ir, Aj.w, f);
-                        fx.add(-cf * unit.x); fy.add(-cf * unit.y); fz.add(-cf * unit.z);
-                        if (cnt < MAX_P2P_COUNT) {
-                            c.pp_id_new[sid + cnt] = k;
-                            reinterpret_cast<double2*>(c.pp_tsd_new)[sid + cnt] = make_double2(0.0, 0.0);
-                            cnt++;
-                        } else {
-                            bits |= XDEM_ERR_P2P_OVERFLOW;
-                        }
-                        continue;
-                    }
-                    double sd0 = 0.0, sd1 = 0.0;
-                    for (unsigned int q = 0; q < old_count; ++q)
-                        if (c.pp_id_old[sid + q] == k) {
-                            const double2 t = reinterpret_cast<const double2*>(c.pp_tsd_old)[sid + q];
-                            sd0 = t.x; sd1 = t.y;
-                            break;
-                        }
-                    const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
-                    const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
-                    const V3<float> unit = rp / dist;
-                    const V3<float> dcpr = ir * unit;
-                    const V3<float> dcpr_j = dcpr - rp;
-                    const V3<float> jvel = v3<float>(Bj.x, Bj.y, Bj.z);
-                    const V3<float> jom = v3<float>(Cj.x, Cj.y, Cj.z);
-                    const V3<float> rv = (jvel + tcross(jom, dcpr_j)) - (ivel + tcross(iom, dcpr));
-                    const FC<float> fc = fconst_r<float>(mr, model, ir, Aj.w, im, Bj.w);
-                    float fca = 0.f;
-                    if (coh) {
-                        const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
-                        const double fdn = (double)fc.vn * (double)tdot(rv, unit);
-                        fca = (float)(-cohesion_force(mp, ir, Aj.w, fsn + fdn));
-                    }
-                    model_r<float>(model, fc, dt, cdist, sd0, sd1, rv, unit, Ft, Fn, fca);
-                    const V3<float> fsum = Fn + Ft;
-                    const V3<float> mm = tcross(dcpr, fsum);
-                    fx.add(fsum.x); fy.add(fsum.y); fz.add(fsum.z);
-                    mx.add(mm.x); my.add(mm.y); mz.add(mm.z);
-                    if (c.rolling) {
-                        tm = tm + mm;
-                        const float Rij = ir * Aj.w / (ir + Aj.w);
-                        rs += Rij * mr.rfric * tlen(Fn);
-                    }
-                    if (cnt < MAX_P2P_COUNT) {
-                        c.pp_id_new[sid + cnt] = k;
-                        reinterpret_cast<double2*>(c.pp_tsd_new)[sid + cnt] = make_double2(sd0, sd1);
-                        cnt++;
-                    } else {
-                        bits |= XDEM_ERR_P2P_OVERFLOW;
-                    }
-                }
-            }
-    c.pp_count_new[oid] = cnt;
-    F = F + mk3(fx.value(), fy.value(), fz.value());
-    M = M + mk3(mx.value(), my.value(), mz.value());
-    if (c.rolling) {
-        tma = tma + cvt_back<float>(tm);
-        res += (double)rs;
-    }
-}
-
-// Euler-parameter acceleration (closed form of impl:74-133, see uceom) and
-// the frame rotations in FP32 for the mixed form.
-__device__ __forceinline__ float4 uceom_f(float3 J, float4 e, float4 ev, float3 n)
-{
-    const float T0 = J.x * (-e.y * ev.x + e.x * ev.y + e.w * ev.z - e.z * ev.w);
-    const float T1 = J.y * (-e.z * ev.x - e.w * ev.y + e.x * ev.z + e.y * ev.w);
-    const float T2 = J.z * (-e.w * ev.x + e.z * ev.y - e.y * ev.z + e.x * ev.w);
-    const float4 h = make_float4(4.f * (-ev.y * T0 - ev.z * T1 - ev.w * T2), 4.f * (ev.x * T0 - ev.w * T1 + ev.z * T2),
-                                 4.f * (ev.w * T0 + ev.x * T1 - ev.y * T2), 4.f * (-ev.z * T0 + ev.y * T1 + ev.x * T2));
-    const float r0 = n.x - (-e.y * h.x + e.x * h.y + e.w * h.z - e.z * h.w);
-    const float r1 = n.y - (-e.z * h.x - e.w * h.y + e.x * h.z + e.y * h.w);
-    const float r2 = n.z - (-e.w * h.x + e.z * h.y - e.y * h.z + e.x * h.w);
-    const float r3 = -(ev.x * ev.x + ev.y * ev.y + ev.z * ev.z + ev.w * ev.w);
-    const float ie2 = 1.f / (e.x * e.x + e.y * e.y + e.z * e.z + e.w * e.w);
-    const float a0 = r0 * ie2 / (2.f * J.x), a1 = r1 * ie2 / (2.f * J.y), a2 = r2 * ie2 / (2.f * J.z);
-    const float a3 = r3 * ie2;
-    return make_float4(-e.y * a0 - e.z * a1 - e.w * a2 + e.x * a3, e.x * a0 - e.w * a1 + e.z * a2 + e.y * a3,
-                       e.w * a0 + e.x * a1 - e.y * a2 + e.z * a3, -e.z * a0 + e.y * a1 + e.x * a2 + e.w * a3);
-}
-__device__ __forceinline__ float3 to_local_f(float3 v, float4 e)
-{
-    const float3 r0 = make_float3(2.f * (e.x * e.x + e.y * e.y - 0.5f), 2.f * (e.y * e.z - e.x * e.w),
-                                  2.f * (e.y * e.w + e.x * e.z));
-    const float3 r1 = make_float3(2.f * (e.y * e.z + e.x * e.w), 2.f * (e.x * e.x + e.z * e.z - 0.5f),
-                                  2.f * (e.z * e.w - e.x * e.y));
-    const float3 r2 = make_float3(2.f * (e.y * e.w - e.x * e.z), 2.f * (e.z * e.w + e.x * e.y),
-                                  2.f * (e.x * e.x + e.w * e.w - 0.5f));
-    return make_float3(r0.x * v.x + r1.x * v.y + r2.x * v.z, r0.y * v.x + r1.y * v.y + r2.y * v.z,
-                       r0.z * v.x + r1.z * v.y + r2.z * v.z);
-}
-__device__ __forceinline__ float3 ang_vel_f(float4 e, float4 d)
-{
-    return make_float3(2.f * (-e.y * d.x + e.x * d.y - e.w * d.z + e.z * d.w),
-                       2.f * (-e.z * d.x + e.w * d.y + e.x * d.z - e.y * d.w),
-                       2.f * (-e.w * d.x - e.z * d.y + e.y * d.z + e.x * d.w));
-}
-__device__ __forceinline__ float4 f4(d4 a) { return make_float4((float)a.x, (float)a.y, (float)a.z, (float)a.w); }
-
-// Velocity update and next position of the mixed form (impl:192-222,
-// 135-147): the state and its increments' accumulation stay FP64, the
-// increments that need no FP64 range (Euler-parameter acceleration, inverse
-// mass) are FP32.  Euler parameters are renormalised by the second-order
-// expansion of 1/sqrt(s) around s = 1 (|s - 1| ~ (dt |e_dot|)^2).  Writes the
-// FP32 record of the next step.
-__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float4 Bi, d3 F, d3 M,
-                                           unsigned int& bits)
-{
-    const device_dem_parameters& p = c.prm;
-    const double dt = p.dt, hdt = 0.5 * p.dt, h2 = p.half2dt;
-    const float inv_m = 1.0f / Bi.w;
-    const d3 g3 = dv3(p.gravity);
-    const d3 a_new = mk3(F.x * (double)inv_m + g3.x, F.y * (double)inv_m + g3.y, F.z * (double)inv_m + g3.z);
-    const d4 e = ld4(c.ep_cur, oid);
-    const d4 av0 = ld4(c.ev, oid);
-    const float4 ef = f4(e), evf = f4(av0);
-    const d3 Jd = ld3(c.inertia, oid);
-    const float3 Jf = make_float3((float)Jd.x, (float)Jd.y, (float)Jd.z);
-    const float4 qf = uceom_f(Jf, ef, evf, to_local_f(make_float3((float)M.x, (float)M.y, (float)M.z), ef));
-    const d4 q = mk4(qf.x, qf.y, qf.z, qf.w);
-    const d4 av = av0 + hdt * (ld4(c.ea, oid) + q);
-    d3 v = ld3(c.vel, oid);
-    if (!c.vel_compat) v = v + hdt * (ld3(c.acc, oid) + a_new);
-    st3(c.vel, oid, v);
-    st4(c.ev, oid, av);
-    st3(c.acc, oid, a_new);
-    st4(c.ea, oid, q);
-    // next position and Euler parameters
-    d4 e2 = (e + dt * av) + h2 * q;
-    const double eps = dot(e2, e2) - 1.0;
-    const double il = 1.0 + eps * (-0.5 + 0.375 * eps);
-    e2 = il * e2;
-    st4(c.ep_next, oid, e2);
-    const d3 xn = mk3(ip.x + (dt * v.x + h2 * a_new.x), ip.y + (dt * v.y + h2 * a_new.y),
-                      ip.z + (dt * v.z + h2 * a_new.z));
-    st4(c.pos_next, oid, mk4(xn.x, xn.y, xn.z, ip.w));
-    // cell of the new centre (FP64 floor: a sphere within 1e-7 m of a cell
-    // face must not be binned one cell off, or a contact at distance just
-    // under the cell size could fall outside the 27-cell stencil)
-    const double rx = xn.x - p.world_origin.x, ry = xn.y - p.world_origin.y, rz = xn.z - p.world_origin.z;
-    const double fx = floor(rx * c.inv_cs), fy = floor(ry * c.inv_cs), fz = floor(rz * c.inv_cs);
-    const int gxn = __double2int_rz(fx), gyn = __double2int_rz(fy), gzn = __double2int_rz(fz);
-    c.k_out[oid] = grid_hash(p, gxn, gyn, gzn);
-    c.v_out[oid] = oid;
-    const float3 w = ang_vel_f(f4(e2), f4(av));
-    const float4 A = make_float4((float)(rx - fx * p.cell_size), (float)(ry - fy * p.cell_size),
-                                 (float)(rz - fz * p.cell_size), (float)ip.w);
-    if (!(isfinite(A.x) && isfinite(A.y) && isfinite(A.z))) bits |= XDEM_ERR_NONFINITE;
-    reinterpret_cast<float4*>(c.rA)[oid] = A;
-    reinterpret_cast<float4*>(c.rB)[oid] = make_float4((float)v.x, (float)v.y, (float)v.z, Bi.w);
-    reinterpret_cast<float4*>(c.rC)[oid] = make_float4(w.x, w.y, w.z, 0.f);
-    c.rT[oid] = pack_cell(gxn, gyn, gzn);
-    if (bits) atomicOr(c.status, bits);
-}
-
 template <class R, bool MESH>
-__global__ void __launch_bounds__(kFusedThreads, sizeof(R) == sizeof(float) ? 4 : 1)
+__global__ void __launch_bounds__(kFusedThreads, 1)
 k_fused_contact(const ContactLaunch c)
 {
     __shared__ double sm[6 * 32];
@@ -370,56 +141,32 @@ k_fused_contact(const ContactLaunch c)
     const int model = p.contact_model;
     const double dt = p.dt;
 
-    constexpr bool MIXED = sizeof(R) == sizeof(float);
     d4 ip = mk4(0, 0, 0, 0), iv = mk4(0, 0, 0, 0), io = mk4(0, 0, 0, 0);
     float4 ipf = make_float4(0.f, 0.f, 0.f, -1.f);
-    float4 mAi = make_float4(0.f, 0.f, 0.f, 0.f), mBi = mAi, mCi = mAi;
-    unsigned int mTi = 0;
     unsigned int gx = 0, gy = 0, gz = 0;
     if (live) {
-        if constexpr (MIXED) {
-            // FP32 record of the snapshot; the FP64 centre for plane/mesh
-            // geometry and for the state update
-            mAi = reinterpret_cast<const float4*>(c.mA)[s];
-            mTi = reinterpret_cast<const uint2*>(c.mIT)[s].y;
-            mBi = reinterpret_cast<const float4*>(c.mB)[s];
-            mCi = reinterpret_cast<const float4*>(c.mC)[s];
-            ip = ld4(c.pos_cur, oid);
-            iv.w = mBi.w;
-            if (c.nplane)
-                ipf = make_float4((float)(ip.x - p.world_origin.x), (float)(ip.y - p.world_origin.y),
-                                  (float)(ip.z - p.world_origin.z), mAi.w);
-        } else {
-            ip = ld4(c.snap_pos, s);
-            iv = ld4(c.snap_vel, s);
-            io = ld4(c.snap_om, s);
-            ipf = reinterpret_cast<const float4*>(c.snap_f)[s];
-        }
+        ip = ld4(c.snap_pos, s);
+        iv = ld4(c.snap_vel, s);
+        io = ld4(c.snap_om, s);
+        ipf = reinterpret_cast<const float4*>(c.snap_f)[s];
         // own cell from the sorted key: (z * gy + y) * gx + x with power-of-two
         // extents; neighbour hashes only need the wrapped coordinates
         const unsigned int key = c.skey[s];
+        const unsigned int shx = __ffs(p.grid_size.x) - 1, shxy = shx + __ffs(p.grid_size.y) - 1;
         gx = key & (p.grid_size.x - 1);
-        gy = (key / p.grid_size.x) & (p.grid_size.y - 1);
-        gz = key / (p.grid_size.x * p.grid_size.y);
+        gy = (key >> shx) & (p.grid_size.y - 1);
+        gz = key >> shxy;
     }
     const d3 ipos = mk3(ip.x, ip.y, ip.z);
     const double ir = ip.w, im = iv.w;
-    V3<R> ivel, iom;
-    if constexpr (MIXED) {
-        ivel = v3<R>(mBi.x, mBi.y, mBi.z);
-        iom = v3<R>(mCi.x, mCi.y, mCi.z);
-    } else {
-        ivel = cvt<R>(mk3(iv.x, iv.y, iv.z));
-        iom = cvt<R>(mk3(io.x, io.y, io.z));
-    }
+    const V3<R> ivel = cvt<R>(mk3(iv.x, iv.y, iv.z));
+    const V3<R> iom = cvt<R>(mk3(io.x, io.y, io.z));
     d3 F = mk3(0, 0, 0), M = mk3(0, 0, 0), tma = mk3(0, 0, 0);
     double res = 0.0;
     unsigned int bits = 0;
 
     // ------------------------------------------------ particle-particle (impl:613-733)
-    if constexpr (MIXED) {
-        if (live && c.has_pp) p2p_mixed(c, oid, gx, gy, gz, mAi, mTi, mBi, mCi, F, M, tma, res, bits);
-    } else if (live && c.has_pp) {
+    if (live && c.has_pp) {
         const mat_pair mp = c.mp[0];
         const MatR<R> mr = mat_r<R>(mp);
         const unsigned int sid = oid * MAX_P2P_COUNT;
@@ -751,7 +498,7 @@ k_fused_contact(const ContactLaunch c)
     const double Tr = res;
     if (Tr) {
         const double J = c.inertia[oid];  // scalar read of the double3 array, as impl:2434
-        const d3 om = MIXED ? mk3(mCi.x, mCi.y, mCi.z) : mk3(io.x, io.y, io.z);
+        const d3 om = mk3(io.x, io.y, io.z);
         const d3 T = (J * p.dt) * om - tma;
         const double lT = length(T);
         if (lT && Tr) {
@@ -759,11 +506,6 @@ k_fused_contact(const ContactLaunch c)
             if (length(Tr3) >= lT) Tr3 = T;
             M = M + Tr3;
         }
-    }
-
-    if constexpr (MIXED) {
-        mixed_tail(c, oid, ip, mBi, F, M, bits);
-        return;
     }
 
     // ------------------------------------------------ velocity update (impl:192-222)

@@ -18,7 +18,8 @@
 // prefilter.  Mixed form: the snapshot is FP32 only -- each sphere's position
 // as an offset from the corner of its own cell plus the cell's integer
 // coordinates, so the relative position of two neighbours is formed in FP32
-// to about 1e-9 m without FP64 arithmetic in the neighbour loop.
+// to about 1e-9 m without FP64 arithmetic in the neighbour loop; the state
+// stays FP64 and only receives FP32 increments (xdem_fused_mixed.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -38,6 +39,28 @@ constexpr int kPlaneF = 16;  // floats per plane in the prefilter table
 // normal, edge lengths.  Layout: xw[3], u1[3], u2[3], un[3], l1, l2, pad[2].
 struct PlaneF { float v[kPlaneF]; };
 
+// Float-pair view of a plane for the mixed form's contact geometry: corner
+// xw, the frame rows u1, u2, unit normal, and the edge lengths, each as
+// hi + lo floats.  rect = 1 when the plane is an orthonormal rectangle
+// (w2 = xw + l1 u1, w4 = xw + l2 u2, w3 = w2 + l2 u2, normal = u1 x u2 of
+// unit length), which the local-coordinate contact test needs; other planes
+// use the FP64 test.  coh = 1 when the plane's contact has cohesion.
+struct PlaneDF {
+    float xw_hi[3], xw_lo[3];
+    float u_hi[9], u_lo[9];
+    float l1_hi, l1_lo, l2_hi, l2_lo;
+    int rect, coh, pad[2];
+};
+
+// Material constants of one contact pair in FP32 (the mixed form's copy of
+// mat_pair): equivalent Young's modulus, 8 G*, damping ratio beta, the
+// tangential damping factor, stiffness ratio, friction, rolling friction,
+// and whether cohesion is on.
+struct MatF {
+    float Eeq, Seq8, beta, vs1, sratio, fric, rfric;
+    int coh;
+};
+
 struct FusedState {
     bool mixed = false;
     bool primed = false;       // next positions + keys hold the next step's input
@@ -52,13 +75,16 @@ struct FusedState {
     float* snap_f = nullptr;    // [nentry*4] x-o, y-o, z-o, r (FP32 prefilter; w < 0: no filter)
     // mixed snapshot (sorted order) and its per-sphere source (original order)
     float* mA = nullptr;        // [nentry*4] offset from own cell corner, r
+    float* mL = nullptr;        // [nentry*4] low parts of mA (float pairs)
     float* mB = nullptr;        // [nentry*4] vx, vy, vz, mass
     float* mC = nullptr;        // [nentry*4] wx, wy, wz, 0
     unsigned int* mIT = nullptr; // [nentry*2] (original id, packed unwrapped cell)
     float* rA = nullptr;        // [np*4] next-step records written by the contact kernel
+    float* rL = nullptr;
     float* rB = nullptr;
     float* rC = nullptr;
     unsigned int* rT = nullptr; // [np]
+    MatF* d_mpf = nullptr;      // [kMaxFusedBodies + 1] FP32 material table
     unsigned int* pp_count2 = nullptr;
     unsigned int* pp_id2 = nullptr;
     double* pp_tsd2 = nullptr;
@@ -66,6 +92,10 @@ struct FusedState {
     double* d_energy = nullptr;
     double* d_bbox = nullptr;   // [kBboxBlocks * 6] block min/max of positions
     PlaneF* d_planef = nullptr; // [kMaxFusedBodies]
+    PlaneDF* d_planedf = nullptr; // [kMaxFusedBodies]
+    PlaneF h_planef[kMaxFusedBodies];     // host copies (sources of the uploads)
+    PlaneDF h_planedf[kMaxFusedBodies];
+    double origin[3] = {0.0, 0.0, 0.0};
     double frame_far2 = 0.0;    // squared radius (from the grid origin) of the FP32 frame
     float frame_margin = 0.f;   // prefilter slack for FP32 rounding
     const device_plane_info* planes = nullptr;
@@ -109,8 +139,12 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 void fused_free(FusedState& fs);
 void fused_invalidate(FusedState& fs);
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
-                     const mat_pair* mp, const device_plane_info* host_planes, const double origin[3],
-                     cudaStream_t st);
+                     const mat_pair* mp, const device_plane_info* host_planes, const mat_pair* host_mp,
+                     unsigned int nmp, const double origin[3], cudaStream_t st);
+// New frame of plane k (its body moved): refreshes the plane tables on the
+// stream; the host copy it uploads from stays owned by the state.
+int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh,
+                       cudaStream_t st);
 // Runs one step.  When e0/e1 are given they bracket the contact kernel.
 int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                unsigned int* nlaunch);
@@ -131,16 +165,24 @@ struct ContactLaunch {
     const float* snap_f;
     float margin;
     const float* mA;
+    const float* mL;
     const float* mB;
     const float* mC;
     const unsigned int* mIT;
     float* rA;
+    float* rL;
     float* rB;
     float* rC;
     unsigned int* rT;
     const PlaneF* planef;
+    const PlaneDF* planedf;
     double inv_cs;   // 1 / cell size
-    float cs_f;      // cell size in FP32
+    float cs_f;      // cell size in FP32 (hi of the float pair)
+    float cs_lo;     // cell size - cs_f
+    float inv_cs_f;
+    float o_hi[3], o_lo[3];  // grid origin as float pairs
+    float dt_f, hdt_f, h2_f; // dt, dt/2, dt^2/2
+    float g_f[3];            // gravity
     const unsigned int* sorted_index;
     const unsigned int* cstart;
     const unsigned int* cend;
@@ -172,6 +214,7 @@ struct ContactLaunch {
     double* ms_tsd;
     const double* body;
     const mat_pair* mp;
+    const MatF* mpf;
     double* bsums;  // [nbody][nblocks][6]
     unsigned int nblocks;
     unsigned int* status;

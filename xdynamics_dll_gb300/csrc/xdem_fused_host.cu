@@ -28,14 +28,18 @@ cudaError_t dalloc(T*& p, size_t n)
 }
 
 // FP32 snapshot record of one sphere for the mixed contact kernel: offset of
-// the centre from its cell corner, radius, packed cell, velocity, mass, spin.
+// the centre from its cell corner and radius as float pairs (A + L), packed
+// cell, velocity, mass, spin.
 __device__ __forceinline__ int3v mixed_record(const device_dem_parameters& p, double inv_cs, d3 x, double r, d3 v,
-                                              double m, d3 w, float4& A, float4& B, float4& C, unsigned int& T)
+                                              double m, d3 w, float4& A, float4& L, float4& B, float4& C,
+                                              unsigned int& T)
 {
     const double rx = x.x - p.world_origin.x, ry = x.y - p.world_origin.y, rz = x.z - p.world_origin.z;
     const double fx = floor(rx * inv_cs), fy = floor(ry * inv_cs), fz = floor(rz * inv_cs);
-    A = make_float4((float)(rx - fx * p.cell_size), (float)(ry - fy * p.cell_size), (float)(rz - fz * p.cell_size),
-                    (float)r);
+    const double ox = rx - fx * p.cell_size, oy = ry - fy * p.cell_size, oz = rz - fz * p.cell_size;
+    A = make_float4((float)ox, (float)oy, (float)oz, (float)r);
+    L = make_float4((float)(ox - (double)A.x), (float)(oy - (double)A.y), (float)(oz - (double)A.z),
+                    (float)(r - (double)A.w));
     B = make_float4((float)v.x, (float)v.y, (float)v.z, (float)m);
     C = make_float4((float)w.x, (float)w.y, (float)w.z, 0.f);
     const int3v g{__double2int_rz(fx), __double2int_rz(fy), __double2int_rz(fz)};
@@ -49,7 +53,7 @@ __device__ __forceinline__ int3v mixed_record(const device_dem_parameters& p, do
 __global__ void k_prologue(device_dem_parameters p, const double* pos, const double* ep, const double* vel,
                            const double* ev, const double* acc, const double* ea, const double* mass,
                            double* pos_next, double* ep_next, unsigned int* key, unsigned int* val, unsigned int n,
-                           unsigned int* status, float* rA, float* rB, float* rC, unsigned int* rT)
+                           unsigned int* status, float* rA, float* rL, float* rB, float* rC, unsigned int* rT)
 {
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -67,10 +71,11 @@ __global__ void k_prologue(device_dem_parameters p, const double* pos, const dou
     int3v g;
     if (rA) {
         // mixed form: the key's cell is the cell the FP32 record is relative to
-        float4 A, B, C;
+        float4 A, L, B, C;
         unsigned int T;
-        g = mixed_record(p, 1.0 / p.cell_size, x, q.w, v, mass[i], ang_vel(en, ld4(ev, i)), A, B, C, T);
+        g = mixed_record(p, 1.0 / p.cell_size, x, q.w, v, mass[i], ang_vel(en, ld4(ev, i)), A, L, B, C, T);
         reinterpret_cast<float4*>(rA)[i] = A;
+        reinterpret_cast<float4*>(rL)[i] = L;
         reinterpret_cast<float4*>(rB)[i] = B;
         reinterpret_cast<float4*>(rC)[i] = C;
         rT[i] = T;
@@ -152,8 +157,9 @@ __global__ void k_reorder_fp64(const unsigned int* sk, const unsigned int* sv, u
 // Mixed form: cell ranges and the FP32 records permuted into sorted order.
 __global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
                                 unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index,
-                                unsigned int* skey, const float4* rA, const float4* rB, const float4* rC,
-                                const unsigned int* rT, float4* mA, float4* mB, float4* mC, uint2* mIT)
+                                unsigned int* skey, const float4* rA, const float4* rL, const float4* rB,
+                                const float4* rC, const unsigned int* rT, float4* mA, float4* mL, float4* mB,
+                                float4* mC, uint2* mIT)
 {
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -164,6 +170,7 @@ __global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, 
     skey[s] = k;
     if (oid < np) {
         mA[s] = rA[oid];
+        mL[s] = rL[oid];
         mB[s] = rB[oid];
         mC[s] = rC[oid];
         mIT[s] = make_uint2(oid, rT[oid]);
@@ -230,10 +237,12 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
     if (e == cudaSuccess) e = dalloc(fs.ep_alt, (size_t)np * 4);
     if (mixed) {
         if (e == cudaSuccess) e = dalloc(fs.mA, (size_t)nentry * 4);
+        if (e == cudaSuccess) e = dalloc(fs.mL, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mB, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mC, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mIT, (size_t)nentry * 2);
         if (e == cudaSuccess) e = dalloc(fs.rA, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.rL, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rC, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rT, np);
@@ -258,9 +267,9 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 
 void fused_free(FusedState& fs)
 {
-    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mB, fs.mC,
-                  fs.mIT, fs.rA, fs.rB, fs.rC, fs.rT, fs.pp_count2, fs.pp_id2, fs.pp_tsd2, fs.skey_prev,
-                  fs.d_energy, fs.d_bbox, fs.d_planef};
+    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
+                  fs.mC, fs.mIT, fs.rA, fs.rL, fs.rB, fs.rC, fs.rT, fs.pp_count2, fs.pp_id2, fs.pp_tsd2,
+                  fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf};
     for (void* q : ps)
         if (q) cudaFree(q);
     fs = FusedState{};
@@ -268,32 +277,103 @@ void fused_free(FusedState& fs)
 
 void fused_invalidate(FusedState& fs) { fs.primed = false; }
 
+namespace {
+
+void split_host(double x, float& hi, float& lo)
+{
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+// Prefilter and float-pair tables of one plane.
+void plane_tables(const device_plane_info& pl, const double origin[3], bool coh, PlaneF& pf, PlaneDF& pd)
+{
+    const double xw[3] = {pl.xw.x, pl.xw.y, pl.xw.z};
+    const double u1[3] = {pl.u1.x, pl.u1.y, pl.u1.z}, u2[3] = {pl.u2.x, pl.u2.y, pl.u2.z};
+    const double uw[3] = {pl.uw.x, pl.uw.y, pl.uw.z};
+    const double lw = std::sqrt(uw[0] * uw[0] + uw[1] * uw[1] + uw[2] * uw[2]);
+    float* v = pf.v;
+    for (int i = 0; i < 3; ++i) {
+        v[i] = (float)(xw[i] - origin[i]);
+        v[3 + i] = (float)u1[i];
+        v[6 + i] = (float)u2[i];
+        v[9 + i] = (float)(uw[i] / lw);
+    }
+    v[12] = (float)pl.l1; v[13] = (float)pl.l2; v[14] = 0.f; v[15] = 0.f;
+
+    pd = PlaneDF{};
+    for (int i = 0; i < 3; ++i) {
+        split_host(xw[i], pd.xw_hi[i], pd.xw_lo[i]);
+        split_host(u1[i], pd.u_hi[i], pd.u_lo[i]);
+        split_host(u2[i], pd.u_hi[3 + i], pd.u_lo[3 + i]);
+        split_host(uw[i], pd.u_hi[6 + i], pd.u_lo[6 + i]);
+    }
+    split_host(pl.l1, pd.l1_hi, pd.l1_lo);
+    split_host(pl.l2, pd.l2_hi, pd.l2_lo);
+    // orthonormal rectangle: the local-coordinate contact test applies
+    auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    const double cr[3] = {u1[1] * u2[2] - u1[2] * u2[1], u1[2] * u2[0] - u1[0] * u2[2], u1[0] * u2[1] - u1[1] * u2[0]};
+    const double tol = 1e-12;
+    bool rect = std::fabs(dot(u1, u1) - 1.0) < tol && std::fabs(dot(u2, u2) - 1.0) < tol &&
+                std::fabs(dot(uw, uw) - 1.0) < tol && std::fabs(dot(u1, u2)) < tol;
+    for (int i = 0; i < 3; ++i) rect = rect && std::fabs(uw[i] - cr[i]) < tol;
+    const double w2[3] = {pl.w2.x, pl.w2.y, pl.w2.z}, w3[3] = {pl.w3.x, pl.w3.y, pl.w3.z};
+    const double w4[3] = {pl.w4.x, pl.w4.y, pl.w4.z};
+    const double scale = std::fabs(xw[0]) + std::fabs(xw[1]) + std::fabs(xw[2]) + pl.l1 + pl.l2 + 1.0;
+    for (int i = 0; i < 3; ++i) {
+        rect = rect && std::fabs(w2[i] - (xw[i] + pl.l1 * u1[i])) < tol * scale;
+        rect = rect && std::fabs(w4[i] - (xw[i] + pl.l2 * u2[i])) < tol * scale;
+        rect = rect && std::fabs(w3[i] - (xw[i] + pl.l1 * u1[i] + pl.l2 * u2[i])) < tol * scale;
+    }
+    pd.rect = rect ? 1 : 0;
+    pd.coh = coh ? 1 : 0;
+}
+
+}  // namespace
+
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
-                     const mat_pair* mp, const device_plane_info* host_planes, const double origin[3],
-                     cudaStream_t st)
+                     const mat_pair* mp, const device_plane_info* host_planes, const mat_pair* host_mp,
+                     unsigned int nmp, const double origin[3], cudaStream_t st)
 {
     fs.planes = planes;
     fs.nplane = nplane;
     fs.body = body;
     fs.mp = mp;
+    for (int i = 0; i < 3; ++i) fs.origin[i] = origin[i];
+    if (nmp > kMaxFusedBodies + 1) return XDEM_ERR_ARG;
+    if (!fs.d_mpf && dalloc(fs.d_mpf, kMaxFusedBodies + 1) != cudaSuccess) return XDEM_ERR_ALLOC;
+    MatF mf[kMaxFusedBodies + 1];
+    for (unsigned int i = 0; i < nmp; ++i) {
+        const mat_pair& m = host_mp[i];
+        mf[i] = MatF{(float)m.Eeq, (float)m.Seq8, (float)m.beta, (float)m.vs1, (float)m.sratio, (float)m.fric,
+                     (float)m.rfric, m.coh != 0.0 ? 1 : 0};
+    }
+    if (nmp) {
+        cudaError_t e = cudaMemcpyAsync(fs.d_mpf, mf, nmp * sizeof(MatF), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return XDEM_ERR_CUDA;
+    }
     if (!nplane) return XDEM_OK;
-    if (!fs.d_planef) {
-        if (dalloc(fs.d_planef, kMaxFusedBodies) != cudaSuccess) return XDEM_ERR_ALLOC;
-    }
-    std::vector<PlaneF> pf(nplane);
-    for (unsigned int k = 0; k < nplane; ++k) {
-        const device_plane_info& pl = host_planes[k];
-        const double uw[3] = {pl.uw.x, pl.uw.y, pl.uw.z};
-        const double lw = std::sqrt(uw[0] * uw[0] + uw[1] * uw[1] + uw[2] * uw[2]);
-        float* v = pf[k].v;
-        v[0] = (float)(pl.xw.x - origin[0]); v[1] = (float)(pl.xw.y - origin[1]); v[2] = (float)(pl.xw.z - origin[2]);
-        v[3] = (float)pl.u1.x; v[4] = (float)pl.u1.y; v[5] = (float)pl.u1.z;
-        v[6] = (float)pl.u2.x; v[7] = (float)pl.u2.y; v[8] = (float)pl.u2.z;
-        v[9] = (float)(uw[0] / lw); v[10] = (float)(uw[1] / lw); v[11] = (float)(uw[2] / lw);
-        v[12] = (float)pl.l1; v[13] = (float)pl.l2; v[14] = 0.f; v[15] = 0.f;
-    }
-    cudaError_t e = cudaMemcpyAsync(fs.d_planef, pf.data(), nplane * sizeof(PlaneF), cudaMemcpyHostToDevice, st);
+    if (nplane > kMaxFusedBodies) return XDEM_ERR_ARG;
+    if (!fs.d_planef && dalloc(fs.d_planef, kMaxFusedBodies) != cudaSuccess) return XDEM_ERR_ALLOC;
+    if (!fs.d_planedf && dalloc(fs.d_planedf, kMaxFusedBodies) != cudaSuccess) return XDEM_ERR_ALLOC;
+    for (unsigned int k = 0; k < nplane; ++k)
+        plane_tables(host_planes[k], origin, host_mp[1 + k].coh != 0.0, fs.h_planef[k], fs.h_planedf[k]);
+    cudaError_t e = cudaMemcpyAsync(fs.d_planef, fs.h_planef, nplane * sizeof(PlaneF), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(fs.d_planedf, fs.h_planedf, nplane * sizeof(PlaneDF), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
+}
+
+int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh,
+                       cudaStream_t st)
+{
+    if (k >= fs.nplane || !fs.d_planef || !fs.d_planedf) return XDEM_OK;  // tables not built yet
+    plane_tables(host_plane, fs.origin, coh, fs.h_planef[k], fs.h_planedf[k]);
+    cudaError_t e = cudaMemcpyAsync(fs.d_planef + k, &fs.h_planef[k], sizeof(PlaneF), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(fs.d_planedf + k, &fs.h_planedf[k], sizeof(PlaneDF), cudaMemcpyHostToDevice, st);
     return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
 }
 
@@ -315,7 +395,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         fs.have_prev = false;
         k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, a.mass,
                                                         fs.pos_alt, fs.ep_alt, a.k0, a.v0, np, a.status, fs.rA,
-                                                        fs.rB, fs.rC, fs.rT);
+                                                        fs.rL, fs.rB, fs.rC, fs.rT);
         ok(cudaGetLastError());
         const unsigned int nbb = std::min(kBboxBlocks, std::max(1u, blocks_for(np, 256)));
         k_bbox<<<nbb, 256, 0, st>>>(*a.pos, np, fs.d_bbox);
@@ -340,8 +420,10 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         const double R = std::sqrt(r2) + 1.0;
         fs.frame_far2 = R * R;
         // rounding of two FP32 coordinates of size <= R, their difference and
-        // the sum of squares, with 4x slack
-        fs.frame_margin = (float)(16.0 * R * std::ldexp(1.0, -24) + 1e-9);
+        // the sum of squares, with 4x slack; the mixed form rounds the centre
+        // and the origin separately, so the origin's size counts too
+        const double o_len = std::sqrt(org[0] * org[0] + org[1] * org[1] + org[2] * org[2]);
+        fs.frame_margin = (float)(16.0 * (R + o_len) * std::ldexp(1.0, -24) + 1e-9);
         fs.primed = true;
     }
     // Between steps *a.pos / *a.ep hold the committed state (x_n) and the
@@ -361,8 +443,9 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     if (fs.mixed) {
         k_reorder_mixed<<<blocks_for(n), kThreads, 0, st>>>(
             sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev, reinterpret_cast<const float4*>(fs.rA),
-            reinterpret_cast<const float4*>(fs.rB), reinterpret_cast<const float4*>(fs.rC), fs.rT,
-            reinterpret_cast<float4*>(fs.mA), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
+            reinterpret_cast<const float4*>(fs.rL), reinterpret_cast<const float4*>(fs.rB),
+            reinterpret_cast<const float4*>(fs.rC), fs.rT, reinterpret_cast<float4*>(fs.mA),
+            reinterpret_cast<float4*>(fs.mL), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
             reinterpret_cast<uint2*>(fs.mIT));
     } else {
         k_reorder_fp64<<<blocks_for(n), kThreads, 0, st>>>(sk, sv, n, np, a.cstart, a.cend, a.sorted_index,
@@ -381,11 +464,19 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.rolling = a.rolling;
     c.snap_pos = fs.snap_pos; c.snap_vel = fs.snap_vel; c.snap_om = fs.snap_om; c.snap_f = fs.snap_f;
     c.margin = fs.frame_margin;
-    c.mA = fs.mA; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
-    c.rA = fs.rA; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
+    c.mA = fs.mA; c.mL = fs.mL; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
+    c.rA = fs.rA; c.rL = fs.rL; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
+    c.mpf = fs.d_mpf;
     c.planef = fs.d_planef;
+    c.planedf = fs.d_planedf;
     c.inv_cs = 1.0 / a.prm.cell_size;
-    c.cs_f = (float)a.prm.cell_size;
+    split_host(a.prm.cell_size, c.cs_f, c.cs_lo);
+    c.inv_cs_f = (float)(1.0 / a.prm.cell_size);
+    for (int i = 0; i < 3; ++i) split_host(org[i], c.o_hi[i], c.o_lo[i]);
+    c.dt_f = (float)a.prm.dt;
+    c.hdt_f = (float)(0.5 * a.prm.dt);
+    c.h2_f = (float)a.prm.half2dt;
+    c.g_f[0] = (float)a.prm.gravity.x; c.g_f[1] = (float)a.prm.gravity.y; c.g_f[2] = (float)a.prm.gravity.z;
     c.sorted_index = a.sorted_index; c.cstart = a.cstart; c.cend = a.cend; c.skey = fs.skey_prev;
     c.pos_cur = *a.pos; c.pos_next = fs.pos_alt; c.ep_cur = *a.ep; c.ep_next = fs.ep_alt;
     c.vel = a.vel; c.acc = a.acc; c.ev = a.ev; c.ea = a.ea; c.mass = a.mass; c.inertia = a.inertia;

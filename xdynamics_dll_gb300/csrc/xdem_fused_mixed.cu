@@ -1,11 +1,829 @@
-// xdem_fused_mixed.cu -- mixed-precision instantiation of the fused contact
-// kernel: contact geometry and forces in FP32 (FMA contraction on); positions,
-// velocities, tangential history and force/torque accumulation in FP64.
+// xdem_fused_mixed.cu -- the fused contact + integration kernel of the mixed
+// form: contact geometry and forces in FP32, positions, velocities, Euler
+// parameters and their rates kept in FP64.
+//
+// GB300 runs FP64 arithmetic and FP64<->FP32 conversions at about 1/64 of the
+// FP32 rate, so the per-sphere FP64 work is held to the one operation that
+// needs it: adding an FP32 increment to an FP64 state value (14 additions per
+// sphere: velocity 3, Euler-parameter rates 4, Euler parameters 4, position
+// 3).  Conversions run on the integer pipes (xdem_df.cuh); quantities that
+// need more than FP32 (plane distances, the cell of the new centre, the norm
+// of the Euler parameters) are formed in float pairs.  Force and torque sums
+// are compensated FP32 sums (about 48 bits).  The tangential history keeps
+// the reference's FP64 storage; its per-step update is FP32.
+//
+// Physics and slot rules are those of the FP64 kernel (xdem_fused.cuh):
+// impl:613-733 (particle-particle), impl:735-1080 (planes), impl:1930-2109
+// (meshes; FP64 geometry here too), impl:2420-2454 (rolling), impl:192-222
+// and 135-147 (velocity and position update), impl:290-302 (next hash).
+#include "xdem_df.cuh"
 #include "xdem_fused.cuh"
 
 namespace xdem {
+namespace {
+
+__device__ __forceinline__ MatR<float> matr(const MatF& m)
+{
+    return MatR<float>{m.Eeq, m.Seq8, m.beta, m.vs1, m.sratio, m.fric, m.rfric, m.coh != 0};
+}
+__device__ __forceinline__ float3 d2f3(d3 a) { return make_float3(d2f_rn(a.x), d2f_rn(a.y), d2f_rn(a.z)); }
+
+// IEEE quotient a / b, skipping the division when a is zero (common: axis-
+// aligned contacts, no moment about an axis).  Bit-identical to a / b for
+// normal b; a reciprocal-multiply would not be: the unit vector of an
+// axis-aligned contact must come out exactly (0, 1, 0), or the tangential
+// model sees a spurious tangential velocity along the normal.
+__device__ __forceinline__ float qdiv(float a, float b) { return a == 0.f ? a : a / b; }
+__device__ __forceinline__ V3<float> qdiv(V3<float> a, float b)
+{
+    return v3<float>(qdiv(a.x, b), qdiv(a.y, b), qdiv(a.z, b));
+}
+
+// Float-pair square of a float pair, and the float-pair square root.
+__device__ __forceinline__ df df_sqr(df a)
+{
+    const df p = two_prod(a.hi, a.hi);
+    return fast_two_sum(p.hi, p.lo + 2.f * a.hi * a.lo);
+}
+__device__ __forceinline__ df df_sqrt(df a)
+{
+    const float s = sqrtf(a.hi);
+    if (!(s > 0.f)) return df{s, 0.f};
+    const df p = two_prod(s, s);
+    const float r = ((a.hi - p.hi) - p.lo) + a.lo;
+    return fast_two_sum(s, r * (0.5f / s));
+}
+// One component of the relative position of neighbour j from sphere i as a
+// float pair: (A_j + L_j) - (A_i + L_i) + step, with step = +-cell size or 0
+// (float pair step_hi + step_lo).
+__device__ __forceinline__ df rel_df(float aj, float lj, float ai, float li, float step_hi, float step_lo)
+{
+    df s = two_sum(aj, -ai);
+    s = df_add_f(s, step_hi);
+    return df_add_f(s, (lj - li) + step_lo);
+}
+__device__ __forceinline__ float4 d2f4(d4 a) { return make_float4(d2f_rn(a.x), d2f_rn(a.y), d2f_rn(a.z), d2f_rn(a.w)); }
+__device__ __forceinline__ V3<float> vf(float3 a) { return v3<float>(a.x, a.y, a.z); }
+
+// Euler-parameter acceleration (closed form of calculate_uceom, impl:74-133)
+// and the frame rotations in FP32.
+__device__ __forceinline__ float4 uceom_f(float3 J, float4 e, float4 ev, float3 n)
+{
+    const float T0 = J.x * (-e.y * ev.x + e.x * ev.y + e.w * ev.z - e.z * ev.w);
+    const float T1 = J.y * (-e.z * ev.x - e.w * ev.y + e.x * ev.z + e.y * ev.w);
+    const float T2 = J.z * (-e.w * ev.x + e.z * ev.y - e.y * ev.z + e.x * ev.w);
+    const float4 h = make_float4(4.f * (-ev.y * T0 - ev.z * T1 - ev.w * T2), 4.f * (ev.x * T0 - ev.w * T1 + ev.z * T2),
+                                 4.f * (ev.w * T0 + ev.x * T1 - ev.y * T2), 4.f * (-ev.z * T0 + ev.y * T1 + ev.x * T2));
+    const float r0 = n.x - (-e.y * h.x + e.x * h.y + e.w * h.z - e.z * h.w);
+    const float r1 = n.y - (-e.z * h.x - e.w * h.y + e.x * h.z + e.y * h.w);
+    const float r2 = n.z - (-e.w * h.x + e.z * h.y - e.y * h.z + e.x * h.w);
+    const float r3 = -(ev.x * ev.x + ev.y * ev.y + ev.z * ev.z + ev.w * ev.w);
+    const float ie2 = 1.f / (e.x * e.x + e.y * e.y + e.z * e.z + e.w * e.w);
+    const float a0 = qdiv(r0 * ie2, 2.f * J.x), a1 = qdiv(r1 * ie2, 2.f * J.y), a2 = qdiv(r2 * ie2, 2.f * J.z);
+    const float a3 = r3 * ie2;
+    return make_float4(-e.y * a0 - e.z * a1 - e.w * a2 + e.x * a3, e.x * a0 - e.w * a1 + e.z * a2 + e.y * a3,
+                       e.w * a0 + e.x * a1 - e.y * a2 + e.z * a3, -e.z * a0 + e.y * a1 + e.x * a2 + e.w * a3);
+}
+__device__ __forceinline__ float3 to_local_f(float3 v, float4 e)
+{
+    const float3 r0 = make_float3(2.f * (e.x * e.x + e.y * e.y - 0.5f), 2.f * (e.y * e.z - e.x * e.w),
+                                  2.f * (e.y * e.w + e.x * e.z));
+    const float3 r1 = make_float3(2.f * (e.y * e.z + e.x * e.w), 2.f * (e.x * e.x + e.z * e.z - 0.5f),
+                                  2.f * (e.z * e.w - e.x * e.y));
+    const float3 r2 = make_float3(2.f * (e.y * e.w - e.x * e.z), 2.f * (e.z * e.w + e.x * e.y),
+                                  2.f * (e.x * e.x + e.w * e.w - 0.5f));
+    return make_float3(r0.x * v.x + r1.x * v.y + r2.x * v.z, r0.y * v.x + r1.y * v.y + r2.y * v.z,
+                       r0.z * v.x + r1.z * v.y + r2.z * v.z);
+}
+__device__ __forceinline__ float3 ang_vel_f(float4 e, float4 d)
+{
+    return make_float3(2.f * (-e.y * d.x + e.x * d.y - e.w * d.z + e.z * d.w),
+                       2.f * (-e.z * d.x + e.w * d.y + e.x * d.z - e.y * d.w),
+                       2.f * (-e.w * d.x - e.z * d.y + e.y * d.z + e.x * d.w));
+}
+
+// Hertz-Mindlin / DHS (impl:432-474) in FP32 with the tangential history
+// (ds, previous s_dot) in FP32 registers.
+__device__ __forceinline__ void model_f(int model, const FC<float>& c, float dt, float cdist, float& ds_io,
+                                        float& dots_io, V3<float> dv, V3<float> unit, V3<float>& Ft, V3<float>& Fn,
+                                        float fca)
+{
+    const float fsn = -c.kn * (cdist * sqrtf(cdist));
+    const float dvn = tdot(dv, unit);
+    Fn = (fsn + fca + c.vn * dvn) * unit;
+    const V3<float> e = dv - dvn * unit;
+    const float mag_e = tlen(e);
+    if (mag_e != 0.f) {
+        const V3<float> s_hat = qdiv(e, mag_e);
+        const float s_dot = tdot(dv, s_hat);
+        const float ds = ds_io + dt * (s_dot + dots_io);
+        ds_io = ds;
+        dots_io = s_dot;
+        float a;
+        if (model == 1) {
+            const float S_t = c.ks * sqrtf(c.eq_r * cdist);
+            a = S_t * ds + c.vs * sqrtf(S_t * c.eq_m);
+        } else {
+            a = c.ks * ds + c.vs * s_dot;
+        }
+        const float b = c.mu * tlen(Fn);
+        Ft = (a < b ? a : b) * s_hat;
+    }
+}
+
+// Block sum of six per-thread FP32 values into out[0..5] (FP64): compensated
+// warp butterflies, then one compensated combine of the warps.  Skips the
+// reduction when no thread of the block contributed.  Two barriers; the
+// shared array is reused by the next call only after its first barrier.
+__device__ __forceinline__ void emit_body_f(const float f6[6], bool any, double* out, float* sm)
+{
+    if (!__syncthreads_or(any ? 1 : 0)) {
+        if (threadIdx.x == 0)
+            for (int c = 0; c < 6; ++c) out[c] = 0.0;
+        return;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        float hi = f6[c], lo = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+            const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            const df s = two_sum(hi, oh);
+            hi = s.hi;
+            lo = (lo + ol) + s.lo;
+        }
+        if (lane == 0) {
+            sm[(warp * 6 + c) * 2] = hi;
+            sm[(warp * 6 + c) * 2 + 1] = lo;
+        }
+    }
+    __syncthreads();
+    if (warp == 0 && lane < 6) {
+        const int nw = blockDim.x >> 5;
+        CSum s;
+        for (int w = 0; w < nw; ++w) {
+            s.add(sm[(w * 6 + lane) * 2]);
+            s.lo += sm[(w * 6 + lane) * 2 + 1];
+        }
+        out[lane] = f2d(s.hi) + f2d(s.lo);
+    }
+}
+
+// Per-sphere accumulators of the mixed kernel.
+struct Acc {
+    CSum f[3], m[3];
+    V3<float> tm;   // rolling: sum of contact moments (impl:476-483)
+    float rs;       // rolling: resistance
+};
+
+// Particle-particle contact (impl:613-733) over the FP32 snapshot.  The
+// relative position of a neighbour is (stencil step) * cell size + (offset
+// difference), both small, so FP32 screens candidates to ~1e-9 m wherever
+// the spheres are; a candidate that passes is measured again in float pairs
+// (offsets and radii carry their low parts), so the overlap -- which can be
+// 1e-6 of the radius -- keeps ~1e-16 m resolution and the contact test
+// classifies as the FP64 form does.  Entries whose packed unwrapped cell is
+// not the expected one are aliases of the wrapping hash and are skipped.
+__device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int oid, unsigned int gx,
+                                          unsigned int gy, unsigned int gz, float4 Ai, float4 Li, unsigned int Ti,
+                                          float4 Bi, float4 Ci, Acc& acc, unsigned int& bits)
+{
+    const device_dem_parameters& p = c.prm;
+    const int model = p.contact_model;
+    const float dt = c.dt_f;
+    const MatR<float> mr = matr(c.mpf[0]);
+    const bool coh = mr.coh;
+    const float cs = c.cs_f, cs_lo = c.cs_lo;
+    // FP32 screen: keep candidates whose squared distance is within 1 + 2^-11
+    // of the squared contact distance (FP32 rounding of d2 is below 2^-21)
+    const float screen = 1.0f + 0x1p-11f;
+    const df ri = df{Ai.w, Li.w};
+    const unsigned int sid = oid * MAX_P2P_COUNT;
+    unsigned int old_count = c.pp_count_old[oid];
+    if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
+    const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
+    const float ir = Ai.w, im = Bi.w;
+    const V3<float> ivel = v3<float>(Bi.x, Bi.y, Bi.z);
+    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
+    V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
+    unsigned int cnt = 0;
+    // The stencil as 9 rows of 3 cells: the six cell-range loads of a row are
+    // issued together, then the three cells are walked in order; each
+    // entry's packed cell gives its x step.
+    for (int z = -1; z <= 1; ++z)
+        for (int y = -1; y <= 1; ++y) {
+            unsigned int rs[3], re[3];
+#pragma unroll
+            for (int x = -1; x <= 1; ++x) {
+                const unsigned int h = grid_hash(p, (int)gx + x, (int)gy + y, (int)gz + z);
+                rs[x + 1] = c.cstart[h];
+                re[x + 1] = c.cend[h];
+            }
+            const unsigned int want_yz = pack_cell(0, (int)uy + y, (int)uz + z);
+            // stencil shift as a float pair, without int -> float conversions
+            const float shy = y < 0 ? -cs : (y > 0 ? cs : 0.f), shy_lo = y < 0 ? -cs_lo : (y > 0 ? cs_lo : 0.f);
+            const float shz = z < 0 ? -cs : (z > 0 ? cs : 0.f), shz_lo = z < 0 ? -cs_lo : (z > 0 ? cs_lo : 0.f);
+            const float sy = shy - Ai.y, sz = shz - Ai.z;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                if (rs[r] == 0xffffffffu) continue;
+                const unsigned int end = re[r];
+                for (unsigned int j = rs[r]; j < end; ++j) {
+                    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
+                    const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
+                    const unsigned int xs = (it.y - ux + 1u) & 2047u;  // x step + 1 when not an alias
+                    if ((it.y & ~2047u) != want_yz || xs > 2u || it.x == oid || it.x >= c.np) continue;
+                    const unsigned int k = it.x;
+                    const float shx = xs == 0u ? -cs : (xs == 2u ? cs : 0.f);
+                    const float shx_lo = xs == 0u ? -cs_lo : (xs == 2u ? cs_lo : 0.f);
+                    V3<float> rp = v3<float>(Aj.x + (shx - Ai.x), Aj.y + sy, Aj.z + sz);
+                    const float rr = ir + Aj.w;
+                    const float d2f = tdot(rp, rp);
+                    if (!(d2f < rr * rr * screen) && !coh) continue;
+                    // the same distance in float pairs
+                    const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
+                    const df rx = rel_df(Aj.x, Lj.x, Ai.x, Li.x, shx, shx_lo);
+                    const df ry = rel_df(Aj.y, Lj.y, Ai.y, Li.y, shy, shy_lo);
+                    const df rz = rel_df(Aj.z, Lj.z, Ai.z, Li.z, shz, shz_lo);
+                    const df dd = df_sqrt(df_add(df_add(df_sqr(rx), df_sqr(ry)), df_sqr(rz)));
+                    const float cdist = df_f(df_sub(df_add(ri, df{Aj.w, Lj.w}), dd));
+                    const float dist = df_f(dd);
+                    rp = v3<float>(df_f(rx), df_f(ry), df_f(rz));
+                    if (!(cdist > 0.f)) {
+                        if (!coh) continue;
+                        const mat_pair& mp = c.mp[0];
+                        const double csd = limit_cohesion_depth(mp, ir, Aj.w);
+                        if (!(fabs((double)cdist) < fabs(csd))) continue;
+                        const V3<float> unit = qdiv(rp, dist);
+                        const double f = jkr_separation_force(mp, ir, Aj.w);
+                        const float cf = (float)cohesion_force(mp, ir, Aj.w, f);
+                        acc.f[0].add(-cf * unit.x); acc.f[1].add(-cf * unit.y); acc.f[2].add(-cf * unit.z);
+                        if (cnt < MAX_P2P_COUNT) {
+                            c.pp_id_new[sid + cnt] = k;
+                            reinterpret_cast<double2*>(c.pp_tsd_new)[sid + cnt] = make_double2(0.0, 0.0);
+                            cnt++;
+                        } else {
+                            bits |= XDEM_ERR_P2P_OVERFLOW;
+                        }
+                        continue;
+                    }
+                    float sd0 = 0.f, sd1 = 0.f;
+                    for (unsigned int q = 0; q < old_count; ++q)
+                        if (c.pp_id_old[sid + q] == k) {
+                            const double2 t = reinterpret_cast<const double2*>(c.pp_tsd_old)[sid + q];
+                            sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
+                            break;
+                        }
+                    const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
+                    const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
+                    const V3<float> unit = qdiv(rp, dist);
+                    const V3<float> dcpr = ir * unit;
+                    const V3<float> dcpr_j = dcpr - rp;
+                    const V3<float> jvel = v3<float>(Bj.x, Bj.y, Bj.z);
+                    const V3<float> jom = v3<float>(Cj.x, Cj.y, Cj.z);
+                    const V3<float> rv = (jvel + tcross(jom, dcpr_j)) - (ivel + tcross(iom, dcpr));
+                    const FC<float> fc = fconst_r<float>(mr, model, ir, Aj.w, im, Bj.w);
+                    float fca = 0.f;
+                    if (coh) {
+                        const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
+                        const double fdn = (double)fc.vn * (double)tdot(rv, unit);
+                        fca = (float)(-cohesion_force(c.mp[0], ir, Aj.w, fsn + fdn));
+                    }
+                    model_f(model, fc, dt, cdist, sd0, sd1, rv, unit, Ft, Fn, fca);
+                    const V3<float> fsum = Fn + Ft;
+                    const V3<float> mm = tcross(dcpr, fsum);
+                    acc.f[0].add(fsum.x); acc.f[1].add(fsum.y); acc.f[2].add(fsum.z);
+                    acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
+                    if (c.rolling) {
+                        acc.tm = acc.tm + mm;
+                        const float Rij = ir * Aj.w / (ir + Aj.w);
+                        acc.rs += Rij * mr.rfric * tlen(Fn);
+                    }
+                    if (cnt < MAX_P2P_COUNT) {
+                        c.pp_id_new[sid + cnt] = k;
+                        reinterpret_cast<double2*>(c.pp_tsd_new)[sid + cnt] = make_double2(f2d(sd0), f2d(sd1));
+                        cnt++;
+                    } else {
+                        bits |= XDEM_ERR_P2P_OVERFLOW;
+                    }
+                }
+            }
+        }
+    c.pp_count_new[oid] = cnt;
+}
+
+// Plane contact region and depth (impl:735-815, plane_detection) for a plane
+// that is an orthonormal rectangle, in its local frame: the centre's local
+// coordinates are float-pair dot products of (x - xw) with u1, u2 and the
+// unit normal, so the depth keeps ~1e-15 m resolution however far the plane
+// reaches.  Returns the depth (0 when no region applies) and the unit vector
+// with the reference's orientation per region (corners: corner -> centre;
+// edges: centre -> edge; face: minus the normal).
+__device__ __forceinline__ float plane_rect(const PlaneDF& pd, const df xd[3], df rd, V3<float>& u)
+{
+    df dp[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) dp[i] = df_sub(xd[i], df{pd.xw_hi[i], pd.xw_lo[i]});
+    df w[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        w[a] =df_add(df_add(df_mul(dp[0], df{pd.u_hi[3 * a], pd.u_lo[3 * a]}),
+                             df_mul(dp[1], df{pd.u_hi[3 * a + 1], pd.u_lo[3 * a + 1]})),
+                      df_mul(dp[2], df{pd.u_hi[3 * a + 2], pd.u_lo[3 * a + 2]}));
+    }
+    const float wx = df_f(w[0]), wy = df_f(w[1]), wz = df_f(w[2]);
+    const float r = df_f(rd);
+    const df l1 = df{pd.l1_hi, pd.l1_lo}, l2 = df{pd.l2_hi, pd.l2_lo};
+    const float l1f = df_f(l1), l2f = df_f(l2);
+    const float dx1 = df_f(df_sub(w[0], l1)), dy2 = df_f(df_sub(w[1], l2));
+    const float sqa = wx * wx, sqb = wy * wy, sqc = wz * wz, sqr = r * r, a_l1 = dx1 * dx1, b_l2 = dy2 * dy2;
+    float lx = 0.f, ly = 0.f, lz = wz;
+    int kind = 0;  // 1 corner, 2 edge, 3 face
+    if (wx < 0 && wy < 0 && (sqa + sqb + sqc) < sqr) { lx = wx; ly = wy; kind = 1; }
+    else if (wx > l1f && wy < 0 && (a_l1 + sqb + sqc) < sqr) { lx = dx1; ly = wy; kind = 1; }
+    else if (wx > l1f && wy > l2f && (a_l1 + b_l2 + sqc) < sqr) { lx = dx1; ly = dy2; kind = 1; }
+    else if (wx < 0 && wy > l2f && (sqa + b_l2 + sqc) < sqr) { lx = wx; ly = dy2; kind = 1; }
+    else if ((wx > 0 && wx < l1f) && wy < 0 && (sqb + sqc) < sqr) { ly = wy; kind = 2; }
+    else if ((wx > 0 && wx < l1f) && wy > l2f && (b_l2 + sqc) < sqr) { ly = dy2; kind = 2; }
+    else if ((wx > 0 && wy < l2f) && wx > l1f && (a_l1 + sqc) < sqr) { lx = dx1; kind = 2; }
+    else if ((wx > 0 && wx < l1f) && (wy > 0 && wy < l2f)) kind = 3;
+    const V3<float> u1 = v3<float>(pd.u_hi[0], pd.u_hi[1], pd.u_hi[2]);
+    const V3<float> u2 = v3<float>(pd.u_hi[3], pd.u_hi[4], pd.u_hi[5]);
+    const V3<float> un = v3<float>(pd.u_hi[6], pd.u_hi[7], pd.u_hi[8]);
+    if (kind == 0) return 0.f;
+    if (kind == 3) {
+        u = -un;
+        const df awz = w[2].hi < 0.f ? df_neg(w[2]) : w[2];
+        return df_f(df_sub(rd, awz));
+    }
+    const float h = sqrtf(lx * lx + ly * ly + lz * lz);
+    const V3<float> X = (lx * u1 + ly * u2) + lz * un;
+    u = kind == 1 ? qdiv(X, h) : -qdiv(X, h);
+    return r - h;
+}
+
+// Rigid-body record (decl:20) in FP32: velocity and angular velocity; the
+// reference point as float pairs.
+struct BodyF {
+    df p[3];
+    V3<float> v, om;
+    float m;
+};
+__device__ __forceinline__ BodyF load_body_f(const double* dbi)
+{
+    BodyF b;
+    b.m = d2f_rn(dbi[XDEM_MM]);
+    b.p[0] = split_d(dbi[XDEM_PX]); b.p[1] = split_d(dbi[XDEM_PY]); b.p[2] = split_d(dbi[XDEM_PZ]);
+    b.v = v3<float>(d2f_rn(dbi[XDEM_VX]), d2f_rn(dbi[XDEM_VY]), d2f_rn(dbi[XDEM_VZ]));
+    const float4 e = make_float4(d2f_rn(dbi[XDEM_E0]), d2f_rn(dbi[XDEM_E1]), d2f_rn(dbi[XDEM_E2]), d2f_rn(dbi[XDEM_E3]));
+    const float4 d = make_float4(d2f_rn(dbi[XDEM_ED0]), d2f_rn(dbi[XDEM_ED1]), d2f_rn(dbi[XDEM_ED2]),
+                                 d2f_rn(dbi[XDEM_ED3]));
+    b.om = vf(ang_vel_f(e, d));
+    return b;
+}
+
+// Plane slots of one sphere (impl:950-1080 slot rule), loaded on first use.
+struct PlaneSlots {
+    unsigned int id[MAX_P2PL_COUNT];
+    float a[MAX_P2PL_COUNT], b[MAX_P2PL_COUNT];
+    unsigned int cnt = 0;
+    bool loaded = false;
+};
+
+// One sphere against plane k: contact force into `acc`, the body's share
+// into f6.  Returns true when the sphere touched the plane.
+__device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int k, unsigned int oid, d4 ip,
+                                            const df xd[3], df rd, V3<float> ivel, V3<float> iom, float im,
+                                            PlaneSlots& sl, Acc& acc, float f6[6], unsigned int& bits)
+{
+    const device_dem_parameters& p = c.prm;
+    const device_plane_info& pl = c.planes[k];
+    const PlaneDF& pd = c.planedf[k];
+    const unsigned int pid = pl.id;
+    const mat_pair& mp = c.mp[1 + k];  // FP64 constants: cohesion only
+    const MatR<float> mr = matr(c.mpf[1 + k]);
+    const unsigned int sid = oid * MAX_P2PL_COUNT;
+    if (!sl.loaded) {
+#pragma unroll
+        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q) {
+            sl.id[q] = c.pl_id[sid + q];
+            const double2 t = reinterpret_cast<const double2*>(c.pl_tsd)[sid + q];
+            sl.a[q] = d2f_rn(t.x); sl.b[q] = d2f_rn(t.y);
+        }
+        sl.loaded = true;
+    }
+    if (pid == 0) sl.cnt = 0;
+    const BodyF b = load_body_f(c.body + 15 * k);
+    float cd;
+    V3<float> un, rel;
+    bool hit;
+    double cdd = 0.0;
+    if (pd.rect && !mr.coh) {
+        cd = plane_rect(pd, xd, rd, un);
+        hit = cd > 0.f;
+        cdd = cd;
+        rel = v3<float>(df_f(df_sub(xd[0], b.p[0])), df_f(df_sub(xd[1], b.p[1])), df_f(df_sub(xd[2], b.p[2])));
+    } else {
+        // general parallelogram or cohesion: FP64 region test (rare)
+        const d3 ipos = mk3(ip.x, ip.y, ip.z);
+        const d3 dp = ipos - dv3(pl.xw);
+        d3 unit = mk3(0, 0, 0);
+        const d3 wp = mk3(dot(dp, dv3(pl.u1)), dot(dp, dv3(pl.u2)), dot(dp, dv3(pl.uw)));
+        cdd = plane_detection(pl, ipos, wp, unit, ip.w);
+        double csd = 0.0;
+        if (mr.coh) csd = limit_cohesion_depth(mp, ip.w, 0.0);
+        hit = cdd > 0 || (cdd <= 0 && fabs(cdd) < fabs(csd));
+        cd = (float)cdd;
+        un = cvt<float>(unit);
+        const double* bp = c.body + 15 * k;
+        rel = v3<float>(d2f_rn(ip.x - bp[XDEM_PX]), d2f_rn(ip.y - bp[XDEM_PY]), d2f_rn(ip.z - bp[XDEM_PZ]));
+    }
+    if (!hit) return false;
+    const float r = df_f(rd);
+    const V3<float> dcpr = r * un;
+    const V3<float> dcpr_j = rel + dcpr;
+    float sd0 = 0.f, sd1 = 0.f;
+    V3<float> mf;
+    if (cdd > 0) {
+#pragma unroll
+        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q)
+            if (sl.id[q] == pid) { sd0 = sl.a[q]; sd1 = sl.b[q]; break; }
+        const V3<float> dv = (b.v + tcross(b.om, dcpr_j)) - (ivel + tcross(iom, dcpr));
+        const FC<float> fc = fconst_r<float>(mr, p.contact_model, r, 0.f, im, 0.f);
+        float fca = 0.f;
+        if (mr.coh) {
+            const double fsn = -(double)fc.kn * (cdd * sqrt(cdd));
+            const double fdn = (double)fc.vn * (double)tdot(dv, un);
+            fca = (float)(-cohesion_force(mp, ip.w, 0.0, fsn + fdn));
+        }
+        V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
+        model_f(p.contact_model, fc, c.dt_f, cd, sd0, sd1, dv, un, Ft, Fn, fca);
+        mf = Fn + Ft;
+        const V3<float> mm = tcross(dcpr, mf);
+        acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
+        if (c.rolling) {
+            acc.tm = acc.tm + mm;
+            acc.rs += r * mr.rfric * tlen(Fn);
+        }
+    } else {
+        const double f = jkr_separation_force(mp, ip.w, 0.0);
+        const float cf = (float)cohesion_force(mp, ip.w, 0.0, f);
+        mf = (-cf) * un;
+    }
+    acc.f[0].add(mf.x); acc.f[1].add(mf.y); acc.f[2].add(mf.z);
+    const V3<float> bm = tcross(dcpr_j, mf);
+    f6[0] = -mf.x; f6[1] = -mf.y; f6[2] = -mf.z;
+    f6[3] = -bm.x; f6[4] = -bm.y; f6[5] = -bm.z;
+    if (sl.cnt < MAX_P2PL_COUNT) {
+        c.pl_id[sid + sl.cnt] = pid;
+        reinterpret_cast<double2*>(c.pl_tsd)[sid + sl.cnt] = make_double2(f2d(sd0), f2d(sd1));
+        // the next plane launch of the reference re-reads these slots
+#pragma unroll
+        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q)
+            if ((unsigned int)q == sl.cnt) { sl.id[q] = pid; sl.a[q] = sd0; sl.b[q] = sd1; }
+        sl.cnt++;
+    } else {
+        bits |= XDEM_ERR_P2PL_OVERFLOW;
+    }
+    return true;
+}
+
+// One sphere against mesh m (impl:1930-2109): triangle candidates from the
+// grid, FP64 closest-point geometry (the candidate classification and the
+// 1e-9 de-duplication need it), FP32 forces.  Returns true when touched.
+__device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int m, unsigned int oid, unsigned int gx,
+                                           unsigned int gy, unsigned int gz, d4 ip, V3<float> ivel, V3<float> iom,
+                                           float im, Acc& acc, float f6[6], unsigned int& bits)
+{
+    const device_dem_parameters& p = c.prm;
+    const d3 ipos = mk3(ip.x, ip.y, ip.z);
+    const double ir = ip.w;
+    const unsigned int lo = c.np + c.mesh_first[m], ntri = c.mesh_ntri[m];
+    const int bidx = c.mesh_body[m];
+    const mat_pair& mp = c.mp[1 + bidx];  // FP64 constants: cohesion only
+    const MatR<float> mr = matr(c.mpf[1 + bidx]);
+    const unsigned int sid = oid * MAX_P2MS_COUNT;
+    unsigned int o_id[MAX_P2MS_COUNT];
+    float o_a[MAX_P2MS_COUNT], o_b[MAX_P2MS_COUNT];
+#pragma unroll
+    for (int q = 0; q < (int)MAX_P2MS_COUNT; ++q) {
+        o_id[q] = c.ms_id[sid + q];
+        const double2 t = reinterpret_cast<const double2*>(c.ms_tsd)[sid + q];
+        o_a[q] = d2f_rn(t.x); o_b[q] = d2f_rn(t.y);
+    }
+    struct Hit { unsigned int id; d3 cpt; };
+    Hit hf[XDEM_MAX_TRI_CANDIDATES], hl[XDEM_MAX_TRI_CANDIDATES], hp[XDEM_MAX_TRI_CANDIDATES];
+    unsigned int nf = 0, nl = 0, npt = 0;
+    d3 prev_line = mk3(0, 0, 0), prev_point = mk3(0, 0, 0);
+    double cs = 0.0;
+    if (mr.coh) cs = limit_cohesion_depth(mp, ir, 0.0);
+    for (int z = -1; z <= 1; ++z)
+        for (int y = -1; y <= 1; ++y)
+            for (int x = -1; x <= 1; ++x) {
+                const unsigned int h = grid_hash(p, (int)gx + x, (int)gy + y, (int)gz + z);
+                const unsigned int start = c.cstart[h];
+                if (start == 0xffffffffu) continue;
+                const unsigned int end = c.cend[h];
+                for (unsigned int j = start; j < end; ++j) {
+                    unsigned int tk = c.sorted_index[j];
+                    if (!(tk >= lo && tk < lo + ntri)) continue;
+                    tk -= lo;
+                    int t = -1;
+                    const d3 cpt = closest_pt_triangle(c.tri[c.mesh_first[m] + tk], ipos, t);
+                    const double cd = ir - length(ipos - cpt);
+                    bool take = false;
+                    if (cd > 0) {
+                        if (t == 1) {
+                            if (check_overlap(prev_line, cpt)) continue;
+                            prev_line = cpt;
+                        } else if (t == 0) {
+                            if (check_overlap(prev_point, cpt)) continue;
+                            prev_point = cpt;
+                        }
+                        take = true;
+                    } else if (cd <= 0 && fabs(cd) < fabs(cs)) {
+                        take = true;
+                    }
+                    if (!take) continue;
+                    const Hit hit{tk, cpt};
+                    if (t == 2) { if (nf < XDEM_MAX_TRI_CANDIDATES) hf[nf++] = hit; else bits |= XDEM_ERR_TRI_CANDIDATES; }
+                    else if (t == 1) { if (nl < XDEM_MAX_TRI_CANDIDATES) hl[nl++] = hit; else bits |= XDEM_ERR_TRI_CANDIDATES; }
+                    else if (t == 0) { if (npt < XDEM_MAX_TRI_CANDIDATES) hp[npt++] = hit; else bits |= XDEM_ERR_TRI_CANDIDATES; }
+                }
+            }
+    const Hit* list = nf ? hf : (nl ? hl : hp);
+    const unsigned int nlist = nf ? nf : (nl ? nl : npt);
+    const BodyF b = load_body_f(c.body + 15 * bidx);
+    const d3 bpos = mk3(c.body[15 * bidx + XDEM_PX], c.body[15 * bidx + XDEM_PY], c.body[15 * bidx + XDEM_PZ]);
+    bool touched = false;
+    unsigned int cnt = 0;
+    for (unsigned int q = 0; q < nlist; ++q) {
+        const Hit hit = list[q];
+        float sd0 = 0.f, sd1 = 0.f;
+        const V3<float> po2cp = cvt<float>(hit.cpt - bpos);
+        const d3 rpd = hit.cpt - ipos;
+        const double dist = length(rpd);
+        const V3<float> un = cvt<float>(rpd / dist);
+        const double cd = ir - dist;
+        if (cd <= 0 && fabs(cd) < fabs(cs)) {
+            const double f = jkr_separation_force(mp, ir, 0.0);
+            const float cf = (float)cohesion_force(mp, ir, 0.0, f);
+            acc.f[0].add(-cf * un.x); acc.f[1].add(-cf * un.y); acc.f[2].add(-cf * un.z);
+        } else {
+            for (int r = 0; r < (int)MAX_P2MS_COUNT; ++r)
+                if (o_id[r] == hit.id) { sd0 = o_a[r]; sd1 = o_b[r]; break; }
+            const V3<float> rc = cvt<float>(rpd);
+            const V3<float> dv = (b.v + tcross(b.om, po2cp)) - (ivel + tcross(iom, rc));
+            const FC<float> fc = fconst_r<float>(mr, p.contact_model, (float)ir, 0.f, im, b.m);
+            float fca = 0.f;
+            if (mr.coh) {
+                const double fsn = -(double)fc.kn * (cd * sqrt(cd));
+                const double fdn = (double)fc.vn * (double)tdot(dv, un);
+                fca = (float)(-cohesion_force(mp, ir, 0.0, fsn + fdn));
+            }
+            V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
+            model_f(p.contact_model, fc, c.dt_f, (float)cd, sd0, sd1, dv, un, Ft, Fn, fca);
+            const V3<float> fsum = Fn + Ft;
+            const V3<float> mm = tcross(rc, fsum);
+            acc.tm = acc.tm + mm;
+            acc.rs += (float)ir * mr.rfric * tlen(Fn);
+            acc.f[0].add(fsum.x); acc.f[1].add(fsum.y); acc.f[2].add(fsum.z);
+            acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
+            const V3<float> bm = tcross(po2cp, fsum);
+            f6[0] -= fsum.x; f6[1] -= fsum.y; f6[2] -= fsum.z;
+            f6[3] -= bm.x; f6[4] -= bm.y; f6[5] -= bm.z;
+            touched = true;
+        }
+        if (cnt < MAX_P2MS_COUNT) {
+            c.ms_id[sid + cnt] = hit.id;
+            reinterpret_cast<double2*>(c.ms_tsd)[sid + cnt] = make_double2(f2d(sd0), f2d(sd1));
+            cnt++;
+        } else {
+            bits |= XDEM_ERR_P2MS_OVERFLOW;
+        }
+    }
+    c.ms_count[oid] = cnt;
+    return touched;
+}
+
+// Velocity update, next Euler parameters and position, the next cell and the
+// next step's FP32 records (impl:192-222, 135-147, 290-302).  FP64 work: the
+// 14 additions of FP32 increments to the FP64 state.  The Euler parameters
+// are renormalised to second order, 1/sqrt(1 + eps) ~ 1 - eps/2 + 3/8 eps^2,
+// with eps = |e + de|^2 - 1 formed in float pairs from the FP64 e.
+__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float4 Ai, float4 Li,
+                                           float4 Bi, V3<float> Ff, V3<float> Mf, unsigned int& bits)
+{
+    const device_dem_parameters& p = c.prm;
+    const float dt = c.dt_f, hdt = c.hdt_f, h2 = c.h2_f;
+    const float inv_m = 1.f / Bi.w;
+    const V3<float> a_new = v3<float>(Ff.x * inv_m + c.g_f[0], Ff.y * inv_m + c.g_f[1], Ff.z * inv_m + c.g_f[2]);
+    // translation
+    const d3 v = ld3(c.vel, oid);
+    V3<float> vn = vf(d2f3(v));
+    if (!c.vel_compat) {
+        const V3<float> dv = hdt * (vf(d2f3(ld3(c.acc, oid))) + a_new);
+        st3(c.vel, oid, mk3(v.x + f2d(dv.x), v.y + f2d(dv.y), v.z + f2d(dv.z)));
+        vn = vn + dv;
+    }
+    st3(c.acc, oid, mk3(f2d(a_new.x), f2d(a_new.y), f2d(a_new.z)));
+    // rotation
+    const d4 e = ld4(c.ep_cur, oid);
+    const df e0 = split_d(e.x), e1 = split_d(e.y), e2 = split_d(e.z), e3 = split_d(e.w);
+    const float4 ef = make_float4(df_f(e0), df_f(e1), df_f(e2), df_f(e3));
+    const d4 ev = ld4(c.ev, oid);
+    const float4 evf = d2f4(ev);
+    const float4 eaf = d2f4(ld4(c.ea, oid));
+    const float3 J = d2f3(ld3(c.inertia, oid));
+    const float4 q = uceom_f(J, ef, evf, to_local_f(make_float3(Mf.x, Mf.y, Mf.z), ef));
+    const float4 dev = make_float4(hdt * (eaf.x + q.x), hdt * (eaf.y + q.y), hdt * (eaf.z + q.z), hdt * (eaf.w + q.w));
+    st4(c.ev, oid, mk4(ev.x + f2d(dev.x), ev.y + f2d(dev.y), ev.z + f2d(dev.z), ev.w + f2d(dev.w)));
+    st4(c.ea, oid, mk4(f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w)));
+    const float4 evn = make_float4(evf.x + dev.x, evf.y + dev.y, evf.z + dev.z, evf.w + dev.w);
+    const float4 de = make_float4(dt * evn.x + h2 * q.x, dt * evn.y + h2 * q.y, dt * evn.z + h2 * q.z,
+                                  dt * evn.w + h2 * q.w);
+    // |e|^2 - 1 and e.de in float pairs (e is FP64; the terms cancel to ~1e-16)
+    df n2 = two_prod(e0.hi, e0.hi);
+    n2 = df_add(n2, two_prod(e1.hi, e1.hi));
+    n2 = df_add(n2, two_prod(e2.hi, e2.hi));
+    n2 = df_add(n2, two_prod(e3.hi, e3.hi));
+    n2 = df_add_f(n2, 2.f * (e0.hi * e0.lo + e1.hi * e1.lo + e2.hi * e2.lo + e3.hi * e3.lo));
+    n2 = df_add_f(n2, -1.f);
+    df ed = two_prod(e0.hi, de.x);
+    ed = df_add(ed, two_prod(e1.hi, de.y));
+    ed = df_add(ed, two_prod(e2.hi, de.z));
+    ed = df_add(ed, two_prod(e3.hi, de.w));
+    ed = df_add_f(ed, e0.lo * de.x + e1.lo * de.y + e2.lo * de.z + e3.lo * de.w);
+    const float eps = df_f(n2) + 2.f * df_f(ed) + (de.x * de.x + de.y * de.y + de.z * de.z + de.w * de.w);
+    const float kk = eps * (-0.5f + 0.375f * eps);
+    const float4 dn = make_float4(de.x + kk * (ef.x + de.x), de.y + kk * (ef.y + de.y), de.z + kk * (ef.z + de.z),
+                                  de.w + kk * (ef.w + de.w));
+    st4(c.ep_next, oid, mk4(e.x + f2d(dn.x), e.y + f2d(dn.y), e.z + f2d(dn.z), e.w + f2d(dn.w)));
+    const float4 en = make_float4(ef.x + dn.x, ef.y + dn.y, ef.z + dn.z, ef.w + dn.w);
+    // position
+    const V3<float> inc = dt * vn + h2 * a_new;
+    const d3 xn = mk3(ip.x + f2d(inc.x), ip.y + f2d(inc.y), ip.z + f2d(inc.z));
+    st4(c.pos_next, oid, mk4(xn.x, xn.y, xn.z, ip.w));
+    // cell of the new centre and the offset from its corner, in float pairs:
+    // the offset is exact to ~1e-15 m and in [0, cell size), so the binning
+    // agrees with the offsets the neighbour loop uses
+    const df csd = df{c.cs_f, c.cs_lo};
+    int cell[3];
+    df A[3];
+    bool fin = true;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double xi = i == 0 ? xn.x : (i == 1 ? xn.y : xn.z);
+        const df rx = df_sub(split_d(xi), df{c.o_hi[i], c.o_lo[i]});
+        if (!isfinite(rx.hi)) {
+            fin = false;
+            cell[i] = 0;
+            A[i] = df{rx.hi, 0.f};
+            continue;
+        }
+        int ci = __float2int_rd(rx.hi * c.inv_cs_f);
+        df off = df_sub(rx, df_mul_f(csd, (float)ci));
+        if (off.hi < 0.f) {
+            ci -= 1;
+            off = df_add(off, csd);
+        } else {
+            const df t = df_sub(off, csd);
+            if (t.hi >= 0.f) {
+                ci += 1;
+                off = t;
+            }
+        }
+        cell[i] = ci;
+        A[i] = off;
+    }
+    if (!fin) bits |= XDEM_ERR_NONFINITE;
+    c.k_out[oid] = grid_hash(p, cell[0], cell[1], cell[2]);
+    c.v_out[oid] = oid;
+    const float3 w = ang_vel_f(en, evn);
+    reinterpret_cast<float4*>(c.rA)[oid] = make_float4(A[0].hi, A[1].hi, A[2].hi, Ai.w);
+    reinterpret_cast<float4*>(c.rL)[oid] = make_float4(A[0].lo, A[1].lo, A[2].lo, Li.w);
+    reinterpret_cast<float4*>(c.rB)[oid] = make_float4(vn.x, vn.y, vn.z, Bi.w);
+    reinterpret_cast<float4*>(c.rC)[oid] = make_float4(w.x, w.y, w.z, 0.f);
+    c.rT[oid] = pack_cell(cell[0], cell[1], cell[2]);
+    if (bits) atomicOr(c.status, bits);
+}
+
+template <bool MESH>
+__global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactLaunch c)
+{
+    __shared__ float smf[(kFusedThreads / 32) * 6 * 2];
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned int oid = 0xffffffffu;
+    if (s < c.nentry) oid = c.sorted_index[s];
+    const bool live = oid < c.np;
+    const device_dem_parameters& p = c.prm;
+
+    float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
+    unsigned int Ti = 0, gx = 0, gy = 0, gz = 0;
+    d4 ip = mk4(0, 0, 0, 0);
+    if (live) {
+        Ai = reinterpret_cast<const float4*>(c.mA)[s];
+        Li = reinterpret_cast<const float4*>(c.mL)[s];
+        Ti = reinterpret_cast<const uint2*>(c.mIT)[s].y;
+        Bi = reinterpret_cast<const float4*>(c.mB)[s];
+        Ci = reinterpret_cast<const float4*>(c.mC)[s];
+        const unsigned int key = c.skey[s];
+        // (z * gy + y) * gx + x with power-of-two extents
+        const unsigned int shx = __ffs(p.grid_size.x) - 1, shxy = shx + __ffs(p.grid_size.y) - 1;
+        gx = key & (p.grid_size.x - 1);
+        gy = (key >> shx) & (p.grid_size.y - 1);
+        gz = key >> shxy;
+    }
+    Acc acc;
+    acc.tm = v3<float>(0.f, 0.f, 0.f);
+    acc.rs = 0.f;
+    unsigned int bits = 0;
+    const V3<float> ivel = v3<float>(Bi.x, Bi.y, Bi.z);
+    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
+
+    // ------------------------------------------------ particle-particle (impl:613-733)
+    if (live && c.has_pp) p2p_mixed(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, acc, bits);
+
+    // the FP64 centre: plane and mesh geometry, and the state update
+    if (live) ip = ld4(c.pos_cur, oid);
+
+    // ------------------------------------------------ planes in id order (impl:950-1080)
+    if (c.nplane) {
+        float4 ipf = make_float4(0.f, 0.f, 0.f, -1.f);
+        if (live)
+            ipf = make_float4(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2], Ai.w);
+        PlaneSlots sl;
+        df xd[3], rd{0.f, 0.f};
+        bool have_xd = false;
+        for (unsigned int k = 0; k < c.nplane; ++k) {
+            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool touched = false;
+            // conservative FP32 test: every region of the plane test needs the
+            // centre within r of the plane and of the rectangle's extent
+            bool near = true;
+            if (live && !c.planedf[k].coh) {
+                const PlaneF pf = c.planef[k];
+                const float dx = ipf.x - pf.v[0], dy = ipf.y - pf.v[1], dz = ipf.z - pf.v[2];
+                const float wx = dx * pf.v[3] + dy * pf.v[4] + dz * pf.v[5];
+                const float wy = dx * pf.v[6] + dy * pf.v[7] + dz * pf.v[8];
+                const float wz = dx * pf.v[9] + dy * pf.v[10] + dz * pf.v[11];
+                const float lim = ipf.w + c.margin;
+                near = fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
+            }
+            if (live && near) {
+                if (!have_xd) {
+                    xd[0] = split_d(ip.x); xd[1] = split_d(ip.y); xd[2] = split_d(ip.z);
+                    rd = split_d(ip.w);
+                    have_xd = true;
+                }
+                touched = plane_mixed(c, k, oid, ip, xd, rd, ivel, iom, Bi.w, sl, acc, f6, bits);
+            }
+            emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
+        }
+        if (live) c.pl_count[oid] = sl.cnt;
+    }
+
+    // ------------------------------------------------ triangle meshes (impl:1930-2109)
+    if (MESH) {
+        for (unsigned int m = 0; m < c.nmesh; ++m) {
+            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool touched = false;
+            if (live) touched = mesh_mixed(c, m, oid, gx, gy, gz, ip, ivel, iom, Bi.w, acc, f6, bits);
+            emit_body_f(f6, touched, c.bsums + ((size_t)(c.mesh_body[m]) * c.nblocks + blockIdx.x) * 6, smf);
+        }
+    }
+
+    if (!live) return;
+
+    // ------------------------------------------------ rolling resistance (impl:2420-2454)
+    V3<float> Mf = v3<float>(acc.m[0].value(), acc.m[1].value(), acc.m[2].value());
+    if (acc.rs != 0.f) {
+        const float J = d2f_rn(c.inertia[oid]);  // scalar read of the double3 array, as impl:2434
+        const V3<float> T = (J * c.dt_f) * iom - acc.tm;
+        const float lT = tlen(T);
+        if (lT != 0.f) {
+            V3<float> Tr3 = acc.rs * (T / lT);
+            if (tlen(Tr3) >= lT) Tr3 = T;
+            Mf = Mf + Tr3;
+        }
+    }
+    const V3<float> Ff = v3<float>(acc.f[0].value(), acc.f[1].value(), acc.f[2].value());
+    mixed_tail(c, oid, ip, Ai, Li, Bi, Ff, Mf, bits);
+}
+
+}  // namespace
+
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
 {
-    return launch_fused_contact_t<float>(c, st);
+    if (c.nentry == 0) return cudaSuccess;
+    const unsigned int nb = (c.nentry + kFusedThreads - 1) / kFusedThreads;
+    if (c.nmesh)
+        k_fused_mixed<true><<<nb, kFusedThreads, 0, st>>>(c);
+    else
+        k_fused_mixed<false><<<nb, kFusedThreads, 0, st>>>(c);
+    return cudaGetLastError();
 }
+
 }  // namespace xdem

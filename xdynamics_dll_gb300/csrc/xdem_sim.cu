@@ -236,7 +236,7 @@ int upload_bodies(xdem_sim* s)
     s->dirty_bodies = false;
     const double org[3] = {s->prm.world_origin.x, s->prm.world_origin.y, s->prm.world_origin.z};
     return fused_set_bodies(s->fs, s->d_planes, (unsigned int)s->planes.size(), s->d_body, s->d_mp,
-                            s->planes.data(), org, s->st);
+                            s->planes.data(), mps.data(), (unsigned int)mps.size(), org, s->st);
 }
 
 // ---------------------------------------------------------------- launcher-order step
@@ -628,6 +628,10 @@ XDEM_API int xdem_sim_set_body(xdem_sim* s, int body_index, const double body[15
         s->planes[b.index] = pl;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(s->d_planes + b.index, &s->planes[b.index], sizeof(pl), cudaMemcpyHostToDevice, s->st);
+        // the fused step's prefilter and float-pair tables follow the frame
+        if (e == cudaSuccess &&
+            fused_update_plane(s->fs, (unsigned int)b.index, pl, s->body_cp[body_index].coh != 0.0, s->st) != XDEM_OK)
+            e = cudaErrorUnknown;
     }
     if (b.kind == 1 && e == cudaSuccess) {
         // xParticleMeshObjectContact::update -> cu_update_meshObjectData
