@@ -84,6 +84,9 @@ struct FusedState {
     float* rB = nullptr;
     float* rC = nullptr;
     unsigned int* rT = nullptr; // [np]
+    float* fA = nullptr;        // [np*4] particle-particle force, rolling resistance (original order)
+    float* fB = nullptr;        // [np*4] particle-particle moment
+    float* fC = nullptr;        // [np*4] rolling: sum of contact moments
     MatF* d_mpf = nullptr;      // [kMaxFusedBodies + 1] FP32 material table
     unsigned int* pp_count2 = nullptr;
     unsigned int* pp_id2 = nullptr;
@@ -171,6 +174,9 @@ struct ContactLaunch {
     const unsigned int* mIT;
     float* rA;
     float* rL;
+    float* fA;
+    float* fB;
+    float* fC;
     float* rB;
     float* rC;
     unsigned int* rT;

@@ -243,6 +243,9 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.mIT, (size_t)nentry * 2);
         if (e == cudaSuccess) e = dalloc(fs.rA, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rL, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.fA, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.fB, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.fC, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rC, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rT, np);
@@ -268,7 +271,8 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 void fused_free(FusedState& fs)
 {
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
-                  fs.mC, fs.mIT, fs.rA, fs.rL, fs.rB, fs.rC, fs.rT, fs.pp_count2, fs.pp_id2, fs.pp_tsd2,
+                  fs.mC, fs.mIT, fs.rA, fs.rL, fs.rB, fs.rC, fs.rT, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
+                  fs.pp_tsd2,
                   fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf};
     for (void* q : ps)
         if (q) cudaFree(q);
@@ -466,6 +470,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.margin = fs.frame_margin;
     c.mA = fs.mA; c.mL = fs.mL; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
     c.rA = fs.rA; c.rL = fs.rL; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
+    c.fA = fs.fA; c.fB = fs.fB; c.fC = fs.fC;
     c.mpf = fs.d_mpf;
     c.planef = fs.d_planef;
     c.planedf = fs.d_planedf;

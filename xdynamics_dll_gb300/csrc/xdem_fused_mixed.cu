@@ -39,6 +39,17 @@ __device__ __forceinline__ V3<float> qdiv(V3<float> a, float b)
     return v3<float>(qdiv(a.x, b), qdiv(a.y, b), qdiv(a.z, b));
 }
 
+// Asynchronous global -> shared copies (cp.async, sm_80+): the thread's old
+// pair list is fetched while it walks its stencil.  Each thread copies and
+// later reads only its own shared slots, so a per-thread wait suffices.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+    const unsigned int s = (unsigned int)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Float-pair square of a float pair, and the float-pair square root.
 __device__ __forceinline__ df df_sqr(df a)
 {
@@ -112,7 +123,10 @@ __device__ __forceinline__ void model_f(int model, const FC<float>& c, float dt,
     const float dvn = tdot(dv, unit);
     Fn = (fsn + fca + c.vn * dvn) * unit;
     const V3<float> e = dv - dvn * unit;
-    const float mag_e = tlen(e);
+    // an exactly zero tangential velocity is common (stacked spheres); skip
+    // the square root's special-case path for it
+    const float me2 = tdot(e, e);
+    const float mag_e = me2 == 0.f ? 0.f : sqrtf(me2);
     if (mag_e != 0.f) {
         const V3<float> s_hat = qdiv(e, mag_e);
         const float s_dot = tdot(dv, s_hat);
@@ -178,139 +192,214 @@ struct Acc {
     float rs;       // rolling: resistance
 };
 
-// Particle-particle contact (impl:613-733) over the FP32 snapshot.  The
-// relative position of a neighbour is (stencil step) * cell size + (offset
-// difference), both small, so FP32 screens candidates to ~1e-9 m wherever
-// the spheres are; a candidate that passes is measured again in float pairs
-// (offsets and radii carry their low parts), so the overlap -- which can be
-// 1e-6 of the radius -- keeps ~1e-16 m resolution and the contact test
-// classifies as the FP64 form does.  Entries whose packed unwrapped cell is
-// not the expected one are aliases of the wrapping hash and are skipped.
+// Particle-particle contact (impl:613-733) over the FP32 snapshot, in two
+// passes so that the neighbour walk and the contact arithmetic do not hold
+// their registers at the same time:
+//  1. walk the 27-cell stencil (9 rows of 3 cells; the six cell-range loads
+//     of a row are issued together) and stage, in walk order, the sorted
+//     positions of the candidates whose FP32 squared distance is within
+//     1 + 2^-11 of the squared contact distance (its FP32 rounding is below
+//     2^-21).  The relative position of a neighbour is (stencil step) * cell
+//     size + (offset difference), both small, so FP32 resolves it to ~1e-9 m
+//     wherever the spheres are;
+//  2. measure each staged candidate again in float pairs (offsets and radii
+//     carry their low parts), so the overlap -- which can be 1e-6 of the
+//     radius -- keeps ~1e-16 m resolution and the contact test classifies as
+//     the FP64 form does; then the contact force.
+// The stage holds kStage entries per thread in shared memory; when more pass
+// the screen, the walk is repeated for the rest, in the same order.  Entries
+// whose packed unwrapped cell is not one of the stencil's are aliases of the
+// wrapping hash and are skipped.
+constexpr unsigned int kStage = 16;
+
+// Pass 2 for one staged candidate at sorted position j.
+__device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oid, unsigned int j, unsigned int ux,
+                                         unsigned int uy, unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
+                                         unsigned int sid, unsigned int old_count, const unsigned int* old_id,
+                                         bool coh, V3<float>& Ft, V3<float>& Fn,
+                                         unsigned int& cnt, Acc& acc, unsigned int& bits)
+{
+    const float cs = c.cs_f, cs_lo = c.cs_lo;
+    // every record of the candidate in one round trip (the screen is tight,
+    // so velocity and spin are nearly always needed)
+    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
+    const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
+    const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
+    const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
+    const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
+    const unsigned int k = it.x;
+    // stencil steps (+1) from the packed cells, and the shifts as float pairs
+    const unsigned int xs = (it.y - ux + 1u) & 2047u;
+    const unsigned int ys = ((it.y >> 11) - uy + 1u) & 2047u;
+    const unsigned int zs = ((it.y >> 22) - uz + 1u) & 1023u;
+    const float shx = xs == 0u ? -cs : (xs == 2u ? cs : 0.f), shx_lo = xs == 0u ? -cs_lo : (xs == 2u ? cs_lo : 0.f);
+    const float shy = ys == 0u ? -cs : (ys == 2u ? cs : 0.f), shy_lo = ys == 0u ? -cs_lo : (ys == 2u ? cs_lo : 0.f);
+    const float shz = zs == 0u ? -cs : (zs == 2u ? cs : 0.f), shz_lo = zs == 0u ? -cs_lo : (zs == 2u ? cs_lo : 0.f);
+    const df rx = rel_df(Aj.x, Lj.x, Ai.x, Li.x, shx, shx_lo);
+    const df ry = rel_df(Aj.y, Lj.y, Ai.y, Li.y, shy, shy_lo);
+    const df rz = rel_df(Aj.z, Lj.z, Ai.z, Li.z, shz, shz_lo);
+    const df dd = df_sqrt(df_add(df_add(df_sqr(rx), df_sqr(ry)), df_sqr(rz)));
+    const float cdist = df_f(df_sub(df_add(df{Ai.w, Li.w}, df{Aj.w, Lj.w}), dd));
+    const float dist = df_f(dd);
+    const V3<float> rp = v3<float>(df_f(rx), df_f(ry), df_f(rz));
+    const float ir = Ai.w;
+    const unsigned int slot = sid + cnt;
+    if (!(cdist > 0.f)) {
+        if (!coh) return;
+        const mat_pair& mp = c.mp[0];
+        const double csd = limit_cohesion_depth(mp, ir, Aj.w);
+        if (!(fabs((double)cdist) < fabs(csd))) return;
+        const V3<float> unit = qdiv(rp, dist);
+        const double f = jkr_separation_force(mp, ir, Aj.w);
+        const float cf = (float)cohesion_force(mp, ir, Aj.w, f);
+        acc.f[0].add(-cf * unit.x); acc.f[1].add(-cf * unit.y); acc.f[2].add(-cf * unit.z);
+        if (cnt < MAX_P2P_COUNT) {
+            c.pp_id_new[slot] = k;
+            reinterpret_cast<double2*>(c.pp_tsd_new)[slot] = make_double2(0.0, 0.0);
+            cnt++;
+        } else {
+            bits |= XDEM_ERR_P2P_OVERFLOW;
+        }
+        return;
+    }
+    // history (impl:683-690): partner ids from the shared-memory copy of the
+    // old list, the matching history from global memory
+    float sd0 = 0.f, sd1 = 0.f;
+    for (unsigned int q = 0; q < old_count; ++q)
+        if (old_id[q * kFusedThreads] == k) {
+            const double2 t = reinterpret_cast<const double2*>(c.pp_tsd_old)[sid + q];
+            sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
+            break;
+        }
+    const MatR<float> mr = matr(c.mpf[0]);
+    const V3<float> unit = qdiv(rp, dist);
+    const V3<float> dcpr = ir * unit;
+    const V3<float> dcpr_j = dcpr - rp;
+    const V3<float> rv = (v3<float>(Bj.x, Bj.y, Bj.z) + tcross(v3<float>(Cj.x, Cj.y, Cj.z), dcpr_j)) -
+                         (v3<float>(Bi.x, Bi.y, Bi.z) + tcross(v3<float>(Ci.x, Ci.y, Ci.z), dcpr));
+    const FC<float> fc = fconst_r<float>(mr, c.prm.contact_model, ir, Aj.w, Bi.w, Bj.w);
+    float fca = 0.f;
+    if (coh) {
+        const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
+        const double fdn = (double)fc.vn * (double)tdot(rv, unit);
+        fca = (float)(-cohesion_force(c.mp[0], ir, Aj.w, fsn + fdn));
+    }
+    model_f(c.prm.contact_model, fc, c.dt_f, cdist, sd0, sd1, rv, unit, Ft, Fn, fca);
+    const V3<float> fsum = Fn + Ft;
+    const V3<float> mm = tcross(dcpr, fsum);
+    acc.f[0].add(fsum.x); acc.f[1].add(fsum.y); acc.f[2].add(fsum.z);
+    acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
+    if (c.rolling) {
+        acc.tm = acc.tm + mm;
+        const float Rij = ir * Aj.w / (ir + Aj.w);
+        acc.rs += Rij * mr.rfric * tlen(Fn);
+    }
+    if (cnt < MAX_P2P_COUNT) {
+        c.pp_id_new[slot] = k;
+        reinterpret_cast<double2*>(c.pp_tsd_new)[slot] = make_double2(f2d(sd0), f2d(sd1));
+        cnt++;
+    } else {
+        bits |= XDEM_ERR_P2P_OVERFLOW;
+    }
+}
+
 __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int oid, unsigned int gx,
                                           unsigned int gy, unsigned int gz, float4 Ai, float4 Li, unsigned int Ti,
-                                          float4 Bi, float4 Ci, Acc& acc, unsigned int& bits)
+                                          float4 Bi, float4 Ci, unsigned int* stage, unsigned int* old_id,
+                                          Acc& acc, unsigned int& bits)
 {
     const device_dem_parameters& p = c.prm;
-    const int model = p.contact_model;
-    const float dt = c.dt_f;
-    const MatR<float> mr = matr(c.mpf[0]);
-    const bool coh = mr.coh;
-    const float cs = c.cs_f, cs_lo = c.cs_lo;
-    // FP32 screen: keep candidates whose squared distance is within 1 + 2^-11
-    // of the squared contact distance (FP32 rounding of d2 is below 2^-21)
+    const bool coh = c.mpf[0].coh != 0;
+    const float cs = c.cs_f;
     const float screen = 1.0f + 0x1p-11f;
-    const df ri = df{Ai.w, Li.w};
+    const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
     const unsigned int sid = oid * MAX_P2P_COUNT;
     unsigned int old_count = c.pp_count_old[oid];
     if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
-    const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
-    const float ir = Ai.w, im = Bi.w;
-    const V3<float> ivel = v3<float>(Bi.x, Bi.y, Bi.z);
-    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
+    // the old partner ids travel to shared memory while the stencil is walked
+    for (unsigned int q = 0; q < old_count; ++q) cp_async4(old_id + q * kFusedThreads, c.pp_id_old + sid + q);
+    cp_async_commit();
     V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
-    unsigned int cnt = 0;
-    // The stencil as 9 rows of 3 cells: the six cell-range loads of a row are
-    // issued together, then the three cells are walked in order; each
-    // entry's packed cell gives its x step.
-    for (int z = -1; z <= 1; ++z)
-        for (int y = -1; y <= 1; ++y) {
-            unsigned int rs[3], re[3];
+    unsigned int cnt = 0, done = 0;
+    bool more = true;
+    while (more) {
+        // ---- pass 1: screened candidates done, done + 1, ... of the walk
+        more = false;
+        unsigned int seen = 0, nc = 0;
+        // rows in walk order (z outer, y inner); software-pipelined: the next
+        // row's six cell-range loads and the first entry of each of this
+        // row's three cells are in flight together
+        unsigned int rs[3], re[3];
 #pragma unroll
-            for (int x = -1; x <= 1; ++x) {
-                const unsigned int h = grid_hash(p, (int)gx + x, (int)gy + y, (int)gz + z);
-                rs[x + 1] = c.cstart[h];
-                re[x + 1] = c.cend[h];
-            }
-            const unsigned int want_yz = pack_cell(0, (int)uy + y, (int)uz + z);
-            // stencil shift as a float pair, without int -> float conversions
-            const float shy = y < 0 ? -cs : (y > 0 ? cs : 0.f), shy_lo = y < 0 ? -cs_lo : (y > 0 ? cs_lo : 0.f);
-            const float shz = z < 0 ? -cs : (z > 0 ? cs : 0.f), shz_lo = z < 0 ? -cs_lo : (z > 0 ? cs_lo : 0.f);
-            const float sy = shy - Ai.y, sz = shz - Ai.z;
+        for (int x = -1; x <= 1; ++x) {
+            const unsigned int h = grid_hash(p, (int)gx + x, (int)gy - 1, (int)gz - 1);
+            rs[x + 1] = c.cstart[h];
+            re[x + 1] = c.cend[h];
+        }
+        for (int row = 0; row < 9 && !more; ++row) {
+            const int z = row / 3 - 1, y = row % 3 - 1;
+            uint2 it0[3];
+            float4 A0[3];
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
-                if (rs[r] == 0xffffffffu) continue;
-                const unsigned int end = re[r];
-                for (unsigned int j = rs[r]; j < end; ++j) {
-                    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
-                    const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
-                    const unsigned int xs = (it.y - ux + 1u) & 2047u;  // x step + 1 when not an alias
-                    if ((it.y & ~2047u) != want_yz || xs > 2u || it.x == oid || it.x >= c.np) continue;
-                    const unsigned int k = it.x;
-                    const float shx = xs == 0u ? -cs : (xs == 2u ? cs : 0.f);
-                    const float shx_lo = xs == 0u ? -cs_lo : (xs == 2u ? cs_lo : 0.f);
-                    V3<float> rp = v3<float>(Aj.x + (shx - Ai.x), Aj.y + sy, Aj.z + sz);
-                    const float rr = ir + Aj.w;
-                    const float d2f = tdot(rp, rp);
-                    if (!(d2f < rr * rr * screen) && !coh) continue;
-                    // the same distance in float pairs
-                    const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
-                    const df rx = rel_df(Aj.x, Lj.x, Ai.x, Li.x, shx, shx_lo);
-                    const df ry = rel_df(Aj.y, Lj.y, Ai.y, Li.y, shy, shy_lo);
-                    const df rz = rel_df(Aj.z, Lj.z, Ai.z, Li.z, shz, shz_lo);
-                    const df dd = df_sqrt(df_add(df_add(df_sqr(rx), df_sqr(ry)), df_sqr(rz)));
-                    const float cdist = df_f(df_sub(df_add(ri, df{Aj.w, Lj.w}), dd));
-                    const float dist = df_f(dd);
-                    rp = v3<float>(df_f(rx), df_f(ry), df_f(rz));
-                    if (!(cdist > 0.f)) {
-                        if (!coh) continue;
-                        const mat_pair& mp = c.mp[0];
-                        const double csd = limit_cohesion_depth(mp, ir, Aj.w);
-                        if (!(fabs((double)cdist) < fabs(csd))) continue;
-                        const V3<float> unit = qdiv(rp, dist);
-                        const double f = jkr_separation_force(mp, ir, Aj.w);
-                        const float cf = (float)cohesion_force(mp, ir, Aj.w, f);
-                        acc.f[0].add(-cf * unit.x); acc.f[1].add(-cf * unit.y); acc.f[2].add(-cf * unit.z);
-                        if (cnt < MAX_P2P_COUNT) {
-                            c.pp_id_new[sid + cnt] = k;
-                            reinterpret_cast<double2*>(c.pp_tsd_new)[sid + cnt] = make_double2(0.0, 0.0);
-                            cnt++;
-                        } else {
-                            bits |= XDEM_ERR_P2P_OVERFLOW;
+                it0[r] = make_uint2(0u, 0u);
+                A0[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (rs[r] != 0xffffffffu) {
+                    it0[r] = reinterpret_cast<const uint2*>(c.mIT)[rs[r]];
+                    A0[r] = reinterpret_cast<const float4*>(c.mA)[rs[r]];
+                }
+            }
+            unsigned int nrs[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, nre[3] = {0u, 0u, 0u};
+            if (row < 8) {
+                const int nz = (row + 1) / 3 - 1, ny = (row + 1) % 3 - 1;
+#pragma unroll
+                for (int x = -1; x <= 1; ++x) {
+                    const unsigned int h = grid_hash(p, (int)gx + x, (int)gy + ny, (int)gz + nz);
+                    nrs[x + 1] = c.cstart[h];
+                    nre[x + 1] = c.cend[h];
+                }
+            }
+            {
+                const unsigned int want_yz = pack_cell(0, (int)uy + y, (int)uz + z);
+                const float sy = (y < 0 ? -cs : (y > 0 ? cs : 0.f)) - Ai.y;
+                const float sz = (z < 0 ? -cs : (z > 0 ? cs : 0.f)) - Ai.z;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    if (rs[r] == 0xffffffffu || more) continue;
+                    const unsigned int end = re[r];
+                    for (unsigned int j = rs[r]; j < end; ++j) {
+                        const uint2 it = j == rs[r] ? it0[r] : reinterpret_cast<const uint2*>(c.mIT)[j];
+                        const float4 Aj = j == rs[r] ? A0[r] : reinterpret_cast<const float4*>(c.mA)[j];
+                        const unsigned int xs = (it.y - ux + 1u) & 2047u;  // x step + 1 unless an alias
+                        if ((it.y & ~2047u) != want_yz || xs > 2u || it.x == oid || it.x >= c.np) continue;
+                        if (!coh) {
+                            const float dx = Aj.x + ((xs == 0u ? -cs : (xs == 2u ? cs : 0.f)) - Ai.x);
+                            const float dy = Aj.y + sy, dz = Aj.z + sz;
+                            const float rr = Ai.w + Aj.w;
+                            if (!(dx * dx + dy * dy + dz * dz < rr * rr * screen)) continue;
                         }
-                        continue;
-                    }
-                    float sd0 = 0.f, sd1 = 0.f;
-                    for (unsigned int q = 0; q < old_count; ++q)
-                        if (c.pp_id_old[sid + q] == k) {
-                            const double2 t = reinterpret_cast<const double2*>(c.pp_tsd_old)[sid + q];
-                            sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
+                        if (seen++ < done) continue;
+                        if (nc == kStage) {
+                            more = true;
                             break;
                         }
-                    const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
-                    const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
-                    const V3<float> unit = qdiv(rp, dist);
-                    const V3<float> dcpr = ir * unit;
-                    const V3<float> dcpr_j = dcpr - rp;
-                    const V3<float> jvel = v3<float>(Bj.x, Bj.y, Bj.z);
-                    const V3<float> jom = v3<float>(Cj.x, Cj.y, Cj.z);
-                    const V3<float> rv = (jvel + tcross(jom, dcpr_j)) - (ivel + tcross(iom, dcpr));
-                    const FC<float> fc = fconst_r<float>(mr, model, ir, Aj.w, im, Bj.w);
-                    float fca = 0.f;
-                    if (coh) {
-                        const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
-                        const double fdn = (double)fc.vn * (double)tdot(rv, unit);
-                        fca = (float)(-cohesion_force(c.mp[0], ir, Aj.w, fsn + fdn));
-                    }
-                    model_f(model, fc, dt, cdist, sd0, sd1, rv, unit, Ft, Fn, fca);
-                    const V3<float> fsum = Fn + Ft;
-                    const V3<float> mm = tcross(dcpr, fsum);
-                    acc.f[0].add(fsum.x); acc.f[1].add(fsum.y); acc.f[2].add(fsum.z);
-                    acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
-                    if (c.rolling) {
-                        acc.tm = acc.tm + mm;
-                        const float Rij = ir * Aj.w / (ir + Aj.w);
-                        acc.rs += Rij * mr.rfric * tlen(Fn);
-                    }
-                    if (cnt < MAX_P2P_COUNT) {
-                        c.pp_id_new[sid + cnt] = k;
-                        reinterpret_cast<double2*>(c.pp_tsd_new)[sid + cnt] = make_double2(f2d(sd0), f2d(sd1));
-                        cnt++;
-                    } else {
-                        bits |= XDEM_ERR_P2P_OVERFLOW;
+                        stage[nc++ * kFusedThreads] = j;
                     }
                 }
             }
+#pragma unroll
+            for (int x = 0; x < 3; ++x) {
+                rs[x] = nrs[x];
+                re[x] = nre[x];
+            }
         }
+        done += nc;
+        cp_async_wait_all();
+        // ---- pass 2: float-pair overlap and contact force, in walk order
+        for (unsigned int q = 0; q < nc; ++q)
+            p2p_pair(c, oid, stage[q * kFusedThreads], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, coh, Ft,
+                     Fn, cnt, acc, bits);
+    }
     c.pp_count_new[oid] = cnt;
 }
 
@@ -385,18 +474,15 @@ __device__ __forceinline__ BodyF load_body_f(const double* dbi)
 }
 
 // Plane slots of one sphere (impl:950-1080 slot rule), loaded on first use.
-struct PlaneSlots {
-    unsigned int id[MAX_P2PL_COUNT];
-    float a[MAX_P2PL_COUNT], b[MAX_P2PL_COUNT];
-    unsigned int cnt = 0;
-    bool loaded = false;
-};
 
 // One sphere against plane k: contact force into `acc`, the body's share
 // into f6.  Returns true when the sphere touched the plane.
+// The plane slots (impl:950-1080 slot rule) are read from memory when a
+// plane needs them: the thread owns its slots and writes them as it goes, so
+// memory holds exactly what the reference's next plane launch re-reads.
 __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int k, unsigned int oid, d4 ip,
-                                            const df xd[3], df rd, V3<float> ivel, V3<float> iom, float im,
-                                            PlaneSlots& sl, Acc& acc, float f6[6], unsigned int& bits)
+                                            V3<float> ivel, V3<float> iom, float im, unsigned int& pl_cnt,
+                                            Acc& acc, float f6[6], unsigned int& bits)
 {
     const device_dem_parameters& p = c.prm;
     const device_plane_info& pl = c.planes[k];
@@ -405,16 +491,9 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
     const mat_pair& mp = c.mp[1 + k];  // FP64 constants: cohesion only
     const MatR<float> mr = matr(c.mpf[1 + k]);
     const unsigned int sid = oid * MAX_P2PL_COUNT;
-    if (!sl.loaded) {
-#pragma unroll
-        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q) {
-            sl.id[q] = c.pl_id[sid + q];
-            const double2 t = reinterpret_cast<const double2*>(c.pl_tsd)[sid + q];
-            sl.a[q] = d2f_rn(t.x); sl.b[q] = d2f_rn(t.y);
-        }
-        sl.loaded = true;
-    }
-    if (pid == 0) sl.cnt = 0;
+    if (pid == 0) pl_cnt = 0;
+    const df xd[3] = {split_d(ip.x), split_d(ip.y), split_d(ip.z)};
+    const df rd = split_d(ip.w);
     const BodyF b = load_body_f(c.body + 15 * k);
     float cd;
     V3<float> un, rel;
@@ -447,9 +526,12 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
     float sd0 = 0.f, sd1 = 0.f;
     V3<float> mf;
     if (cdd > 0) {
-#pragma unroll
-        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q)
-            if (sl.id[q] == pid) { sd0 = sl.a[q]; sd1 = sl.b[q]; break; }
+        for (unsigned int q = 0; q < MAX_P2PL_COUNT; ++q)
+            if (c.pl_id[sid + q] == pid) {
+                const double2 t = reinterpret_cast<const double2*>(c.pl_tsd)[sid + q];
+                sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
+                break;
+            }
         const V3<float> dv = (b.v + tcross(b.om, dcpr_j)) - (ivel + tcross(iom, dcpr));
         const FC<float> fc = fconst_r<float>(mr, p.contact_model, r, 0.f, im, 0.f);
         float fca = 0.f;
@@ -476,14 +558,10 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
     const V3<float> bm = tcross(dcpr_j, mf);
     f6[0] = -mf.x; f6[1] = -mf.y; f6[2] = -mf.z;
     f6[3] = -bm.x; f6[4] = -bm.y; f6[5] = -bm.z;
-    if (sl.cnt < MAX_P2PL_COUNT) {
-        c.pl_id[sid + sl.cnt] = pid;
-        reinterpret_cast<double2*>(c.pl_tsd)[sid + sl.cnt] = make_double2(f2d(sd0), f2d(sd1));
-        // the next plane launch of the reference re-reads these slots
-#pragma unroll
-        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q)
-            if ((unsigned int)q == sl.cnt) { sl.id[q] = pid; sl.a[q] = sd0; sl.b[q] = sd1; }
-        sl.cnt++;
+    if (pl_cnt < MAX_P2PL_COUNT) {
+        c.pl_id[sid + pl_cnt] = pid;
+        reinterpret_cast<double2*>(c.pl_tsd)[sid + pl_cnt] = make_double2(f2d(sd0), f2d(sd1));
+        pl_cnt++;
     } else {
         bits |= XDEM_ERR_P2PL_OVERFLOW;
     }
@@ -710,10 +788,51 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
     if (bits) atomicOr(c.status, bits);
 }
 
+// One sphere against plane k behind a call boundary: few spheres are near a
+// plane, and the float-pair plane geometry needs about 50 registers more than
+// the rest of the kernel, so it gets its own allocation instead of setting
+// the whole kernel's.  By value in and out; the force and moment come back
+// as one contact's FP32 values for the caller's compensated sums.
+struct PlaneOut {
+    float f[3], m[3], w[6], tm[3], rs;
+    unsigned int cnt, bits;
+    int touched;
+};
+__device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned int k, unsigned int oid, d4 ip,
+                                            float4 Bi, float4 Ci, unsigned int cnt)
+{
+    Acc a;
+    a.tm = v3<float>(0.f, 0.f, 0.f);
+    a.rs = 0.f;
+    float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    PlaneOut o;
+    o.bits = 0;
+    o.cnt = cnt;
+    o.touched = plane_mixed(*cp, k, oid, ip, v3<float>(Bi.x, Bi.y, Bi.z), v3<float>(Ci.x, Ci.y, Ci.z), Bi.w, o.cnt,
+                            a, f6, o.bits);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        o.f[i] = a.f[i].value();
+        o.m[i] = a.m[i].value();
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.w[i] = f6[i];
+    o.tm[0] = a.tm.x; o.tm[1] = a.tm.y; o.tm[2] = a.tm.z;
+    o.rs = a.rs;
+    return o;
+}
+
+// Kernel 1 of the mixed step: one thread per cell-sorted entry, particle-
+// particle contact (and triangle meshes, which need the grid too).  Writes
+// the sphere's force, moment and rolling sums (original order) for kernel 2.
+// It holds no plane or integration state, so it runs at twice the occupancy
+// of a kernel doing all of it -- the stencil walk is latency-bound.
 template <bool MESH>
-__global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactLaunch c)
+__global__ void __launch_bounds__(kFusedThreads, 6) k_mixed_pairs(const __grid_constant__ ContactLaunch c)
 {
     __shared__ float smf[(kFusedThreads / 32) * 6 * 2];
+    __shared__ unsigned int stage[kStage * kFusedThreads];  // p2p candidates, [slot][thread]
+    __shared__ unsigned int old_id[MAX_P2P_COUNT * kFusedThreads];  // old pair list, [slot][thread]
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned int oid = 0xffffffffu;
     if (s < c.nentry) oid = c.sorted_index[s];
@@ -722,7 +841,6 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactL
 
     float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
     unsigned int Ti = 0, gx = 0, gy = 0, gz = 0;
-    d4 ip = mk4(0, 0, 0, 0);
     if (live) {
         Ai = reinterpret_cast<const float4*>(c.mA)[s];
         Li = reinterpret_cast<const float4*>(c.mL)[s];
@@ -744,19 +862,66 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactL
     const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
 
     // ------------------------------------------------ particle-particle (impl:613-733)
-    if (live && c.has_pp) p2p_mixed(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, acc, bits);
+    if (live && c.has_pp)
+        p2p_mixed(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc, bits);
 
-    // the FP64 centre: plane and mesh geometry, and the state update
-    if (live) ip = ld4(c.pos_cur, oid);
+    // ------------------------------------------------ triangle meshes (impl:1930-2109)
+    if (MESH) {
+        d4 ip = mk4(0, 0, 0, 0);
+        if (live) ip = ld4(c.pos_cur, oid);
+        for (unsigned int m = 0; m < c.nmesh; ++m) {
+            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool touched = false;
+            if (live) touched = mesh_mixed(c, m, oid, gx, gy, gz, ip, ivel, iom, Bi.w, acc, f6, bits);
+            emit_body_f(f6, touched, c.bsums + ((size_t)(c.mesh_body[m]) * c.nblocks + blockIdx.x) * 6, smf);
+        }
+    }
+    if (!live) return;
+    reinterpret_cast<float4*>(c.fA)[oid] = make_float4(acc.f[0].value(), acc.f[1].value(), acc.f[2].value(), acc.rs);
+    reinterpret_cast<float4*>(c.fB)[oid] = make_float4(acc.m[0].value(), acc.m[1].value(), acc.m[2].value(), 0.f);
+    if (c.rolling) reinterpret_cast<float4*>(c.fC)[oid] = make_float4(acc.tm.x, acc.tm.y, acc.tm.z, 0.f);
+    if (bits) atomicOr(c.status, bits);
+}
+
+// Kernel 2 of the mixed step: one thread per sphere in original order, so
+// every state array is read and written coalesced.  Plane contact (planes in
+// id order), rolling resistance, the velocity and position update and the
+// next step's records, on top of kernel 1's particle-particle sums.
+__global__ void __launch_bounds__(kFusedThreads, 4) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
+{
+    __shared__ float smf[(kFusedThreads / 32) * 6 * 2];
+    const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = oid < c.np;
+    float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
+    d4 ip = mk4(0, 0, 0, 0);
+    Acc acc;
+    acc.tm = v3<float>(0.f, 0.f, 0.f);
+    acc.rs = 0.f;
+    if (live) {
+        Ai = reinterpret_cast<const float4*>(c.rA)[oid];
+        Li = reinterpret_cast<const float4*>(c.rL)[oid];
+        Bi = reinterpret_cast<const float4*>(c.rB)[oid];
+        Ci = reinterpret_cast<const float4*>(c.rC)[oid];
+        ip = ld4(c.pos_cur, oid);
+        const float4 fa = reinterpret_cast<const float4*>(c.fA)[oid];
+        const float4 fb = reinterpret_cast<const float4*>(c.fB)[oid];
+        acc.f[0].hi = fa.x; acc.f[1].hi = fa.y; acc.f[2].hi = fa.z;
+        acc.m[0].hi = fb.x; acc.m[1].hi = fb.y; acc.m[2].hi = fb.z;
+        acc.rs = fa.w;
+        if (c.rolling) {
+            const float4 fc = reinterpret_cast<const float4*>(c.fC)[oid];
+            acc.tm = v3<float>(fc.x, fc.y, fc.z);
+        }
+    }
+    unsigned int bits = 0;
+    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
 
     // ------------------------------------------------ planes in id order (impl:950-1080)
     if (c.nplane) {
         float4 ipf = make_float4(0.f, 0.f, 0.f, -1.f);
         if (live)
             ipf = make_float4(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2], Ai.w);
-        PlaneSlots sl;
-        df xd[3], rd{0.f, 0.f};
-        bool have_xd = false;
+        unsigned int pl_cnt = 0;
         for (unsigned int k = 0; k < c.nplane; ++k) {
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             bool touched = false;
@@ -764,7 +929,7 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactL
             // centre within r of the plane and of the rectangle's extent
             bool near = true;
             if (live && !c.planedf[k].coh) {
-                const PlaneF pf = c.planef[k];
+                const PlaneF& pf = c.planef[k];
                 const float dx = ipf.x - pf.v[0], dy = ipf.y - pf.v[1], dz = ipf.z - pf.v[2];
                 const float wx = dx * pf.v[3] + dy * pf.v[4] + dz * pf.v[5];
                 const float wy = dx * pf.v[6] + dy * pf.v[7] + dz * pf.v[8];
@@ -773,26 +938,25 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactL
                 near = fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
             }
             if (live && near) {
-                if (!have_xd) {
-                    xd[0] = split_d(ip.x); xd[1] = split_d(ip.y); xd[2] = split_d(ip.z);
-                    rd = split_d(ip.w);
-                    have_xd = true;
+                const PlaneOut o = plane_call(&c, k, oid, ip, Bi, Ci, pl_cnt);
+                touched = o.touched != 0;
+                pl_cnt = o.cnt;
+                bits |= o.bits;
+                if (touched) {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        acc.f[i].add(o.f[i]);
+                        acc.m[i].add(o.m[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) f6[i] = o.w[i];
+                    acc.tm = acc.tm + v3<float>(o.tm[0], o.tm[1], o.tm[2]);
+                    acc.rs += o.rs;
                 }
-                touched = plane_mixed(c, k, oid, ip, xd, rd, ivel, iom, Bi.w, sl, acc, f6, bits);
             }
             emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
         }
-        if (live) c.pl_count[oid] = sl.cnt;
-    }
-
-    // ------------------------------------------------ triangle meshes (impl:1930-2109)
-    if (MESH) {
-        for (unsigned int m = 0; m < c.nmesh; ++m) {
-            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            bool touched = false;
-            if (live) touched = mesh_mixed(c, m, oid, gx, gy, gz, ip, ivel, iom, Bi.w, acc, f6, bits);
-            emit_body_f(f6, touched, c.bsums + ((size_t)(c.mesh_body[m]) * c.nblocks + blockIdx.x) * 6, smf);
-        }
+        if (live) c.pl_count[oid] = pl_cnt;
     }
 
     if (!live) return;
@@ -802,7 +966,8 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactL
     if (acc.rs != 0.f) {
         const float J = d2f_rn(c.inertia[oid]);  // scalar read of the double3 array, as impl:2434
         const V3<float> T = (J * c.dt_f) * iom - acc.tm;
-        const float lT = tlen(T);
+        const float lT2 = tdot(T, T);
+        const float lT = lT2 == 0.f ? 0.f : sqrtf(lT2);
         if (lT != 0.f) {
             V3<float> Tr3 = acc.rs * (T / lT);
             if (tlen(Tr3) >= lT) Tr3 = T;
@@ -815,14 +980,19 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_fused_mixed(const ContactL
 
 }  // namespace
 
+// Both kernels use nblocks = ceil(nentry / 128) blocks, so each body's
+// wrench partials fill one [nblocks] row whichever kernel writes them.
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
 {
     if (c.nentry == 0) return cudaSuccess;
     const unsigned int nb = (c.nentry + kFusedThreads - 1) / kFusedThreads;
     if (c.nmesh)
-        k_fused_mixed<true><<<nb, kFusedThreads, 0, st>>>(c);
+        k_mixed_pairs<true><<<nb, kFusedThreads, 0, st>>>(c);
     else
-        k_fused_mixed<false><<<nb, kFusedThreads, 0, st>>>(c);
+        k_mixed_pairs<false><<<nb, kFusedThreads, 0, st>>>(c);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_mixed_bodies<<<nb, kFusedThreads, 0, st>>>(c);
     return cudaGetLastError();
 }
 
