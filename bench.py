@@ -33,13 +33,15 @@ for _p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
 
 METRIC = "particle-steps/s at 1M spheres, mixed vs plain FP64 on same GB300; % HBM peak"
 UNIT = "particle-steps/s"
-# Algorithmic bytes per sphere-step of the fused contact kernel: every state
-# array read once (pos 32, vel 24, acc 24, ep 32, ev 32, ea 32, mass 8,
+# Algorithmic bytes per sphere-step of the contact stage (the pair kernel and
+# the plane/integration kernel of the mixed form, bracketed together): every
+# state array read once (pos 32, vel 24, acc 24, ep 32, ev 32, ea 32, mass 8,
 # inertia 24 = 208) and written once (pos 32, vel 24, acc 24, ep 32, ev 32,
 # ea 32 = 176), the next cell hash + index (8), the pair count (read + write
 # 8) and 40 bytes per stored contact (id 4 + history 16, read + write).  The
 # whole step adds the grid's 28 bytes (sort pass 16, sorted index 4, cell
-# ranges 8): 428 + 40 c.
+# ranges 8): 428 + 40 c.  The force hand-off between the two kernels
+# (32 B written, 32 B read) is an implementation cost, not counted.
 B_CONTACT_FIXED = 400.0
 B_STEP_FIXED = 428.0
 B_PER_CONTACT = 40.0
@@ -216,20 +218,26 @@ def time_device(sim, torch, steps, stream):
 
 
 def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None):
+    """Times `steps` steps replayed from the handle's CUDA graph (the way a
+    user runs it), then times the contact stage alone with CUDA events over
+    up to 64 further, eagerly launched steps."""
     sm = new_sim(scene, precision)
     stream = torch.cuda.Stream(device=dev)
     sm.L.xdem_sim_set_stream(sm.h, stream.cuda_stream)
+    sm.set_graph(True)
     sm.step(warmup)
     torch.cuda.synchronize()
-    sm.set_profiling(True)
     if sampler:
         with sampler:
             secs = time_device(sm, torch, steps, stream)
     else:
         secs = time_device(sm, torch, steps, stream)
-    launches, contact_ms, contact_n = sm.profile()
-    sm.set_profiling(False)
+    launches, _, _ = sm.profile()
     ke, ncontact = sm.energy()
+    sm.set_profiling(True)
+    sm.step(min(steps, 64))
+    _, contact_ms, contact_n = sm.profile()
+    sm.set_profiling(False)
     st = sm.status()
     return sm, stream, {"secs": secs, "launches": launches, "contact_ms": contact_ms / max(contact_n, 1),
                         "contact_launches": contact_n, "ncontact": ncontact, "ke": ke, "status": st}
@@ -327,7 +335,7 @@ def main():
     b_contact = (B_CONTACT_FIXED + B_PER_CONTACT * cbar) * n
     achieved = b_contact / (rmx["contact_ms"] * 1e-3) / 1e9
     traffic_per_sphere, tfile = profile_traffic()
-    roof = {"bound": "hbm", "kernel": "k_fused_contact<float> (mixed)", "achieved": achieved, "peak": peak,
+    roof = {"bound": "hbm", "kernel": "k_mixed_pairs + k_mixed_bodies (mixed contact stage)", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "traffic": traffic_per_sphere * n if traffic_per_sphere else None,
             "algorithmic_bytes_per_launch": b_contact,

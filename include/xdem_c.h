@@ -387,6 +387,12 @@ XDEM_API int xdem_sim_set_stream(xdem_sim* sim, void* stream);
  * time of the particle-particle contact kernel, in milliseconds, from CUDA
  * events recorded on the handle's stream when profiling is on. */
 XDEM_API int xdem_sim_set_profiling(xdem_sim* sim, int on);
+/* Replays the fused step from CUDA graphs (one per arrangement of the
+ * double-buffered arrays, captured on first use and again after any change
+ * of state arrays, bodies or contact tables), one graph launch per step
+ * instead of about 14 kernel launches.  Profiling (xdem_sim_set_profiling)
+ * runs the steps eagerly.  Results are identical either way. */
+XDEM_API int xdem_sim_set_graph(xdem_sim* sim, int on);
 XDEM_API int xdem_sim_profile(xdem_sim* sim, unsigned int* launches,
                               double* contact_ms, unsigned int* contact_launches);
 

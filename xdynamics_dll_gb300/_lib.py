@@ -66,6 +66,7 @@ _SIGS = {
     "xdem_sim_status": ([vp], i32),
     "xdem_sim_set_stream": ([vp, vp], i32),
     "xdem_sim_set_profiling": ([vp, i32], i32),
+    "xdem_sim_set_graph": ([vp, i32], i32),
     "xdem_sim_profile": ([vp, vp, vp, vp], i32),
 }
 

@@ -503,6 +503,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.status = a.status;
     if (e0) cudaEventRecord(e0, st);
     ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
+    if (fs.mixed) nl++;  // the mixed contact stage is two kernels (pairs, bodies)
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody) {
         k_body_sums<<<a.nbody * 6, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench);

@@ -96,6 +96,16 @@ struct xdem_sim {
     cudaEvent_t pe0[kProfEvents] = {}, pe1[kProfEvents] = {};
     double prof_ms = 0.0;
     unsigned int prof_launches = 0, prof_contact_launches = 0, launches = 0;
+    // CUDA graphs of one fused step, one per arrangement of the double-
+    // buffered arrays (they alternate between two); key is the arrangement
+    // the graph starts from
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        const void* key[8] = {};
+        unsigned int launches = 0;
+    };
+    bool use_graph = false;
+    StepGraph graphs[2];
 };
 
 namespace {
@@ -355,6 +365,82 @@ FusedArgs fused_args(xdem_sim* s)
     return a;
 }
 
+// ---- CUDA graphs of the fused step
+void drop_graph(xdem_sim* s)
+{
+    for (auto& g : s->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = xdem_sim::StepGraph{};
+    }
+}
+
+void graph_key(const xdem_sim* s, const void* k[8])
+{
+    k[0] = s->pos; k[1] = s->fs.pos_alt; k[2] = s->ep; k[3] = s->fs.ep_alt;
+    k[4] = s->pp_count; k[5] = s->fs.pp_count2; k[6] = s->pp_id; k[7] = s->pp_tsd;
+}
+
+int find_graph(const xdem_sim* s)
+{
+    const void* k[8];
+    graph_key(s, k);
+    for (int g = 0; g < 2; ++g) {
+        if (!s->graphs[g].exec) continue;
+        bool same = true;
+        for (int i = 0; i < 8; ++i) same = same && k[i] == s->graphs[g].key[i];
+        if (same) return g;
+    }
+    return -1;
+}
+
+// The host side of one primed fused step: its buffer swaps (fused_step).
+void step_swaps(xdem_sim* s)
+{
+    std::swap(s->pos, s->fs.pos_alt);
+    std::swap(s->ep, s->fs.ep_alt);
+    if (s->has_pp) {
+        std::swap(s->pp_count, s->fs.pp_count2);
+        std::swap(s->pp_id, s->fs.pp_id2);
+        std::swap(s->pp_tsd, s->fs.pp_tsd2);
+    }
+}
+
+// Records one fused step into graph slot `slot`.  Nothing runs during the
+// capture, but the host side of the step (its swaps) does: on success the
+// caller must launch the graph; on failure the arrangement is restored.
+int capture_step_graph(xdem_sim* s, int slot)
+{
+    xdem_sim::StepGraph& sg = s->graphs[slot];
+    if (sg.exec) cudaGraphExecDestroy(sg.exec);
+    sg = xdem_sim::StepGraph{};
+    const void* key[8];
+    graph_key(s, key);
+    double *pos = s->pos, *pos_alt = s->fs.pos_alt, *ep = s->ep, *ep_alt = s->fs.ep_alt;
+    unsigned int *c0 = s->pp_count, *c1 = s->fs.pp_count2, *i0 = s->pp_id, *i1 = s->fs.pp_id2;
+    double *t0 = s->pp_tsd, *t1 = s->fs.pp_tsd2;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return XDEM_ERR_CUDA;
+    FusedArgs a = fused_args(s);
+    unsigned int nl = 0;
+    int r = fused_step(s->fs, a, s->st, nullptr, nullptr, &nl);
+    const cudaError_t ec = cudaStreamEndCapture(s->st, &g);
+    if (r == XDEM_OK && (ec != cudaSuccess || !g || cudaGraphInstantiate(&sg.exec, g, 0) != cudaSuccess)) {
+        sg.exec = nullptr;
+        r = XDEM_ERR_CUDA;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (r != XDEM_OK) {
+        s->pos = pos; s->fs.pos_alt = pos_alt; s->ep = ep; s->fs.ep_alt = ep_alt;
+        s->pp_count = c0; s->fs.pp_count2 = c1; s->pp_id = i0; s->fs.pp_id2 = i1;
+        s->pp_tsd = t0; s->fs.pp_tsd2 = t1;
+        cudaGetLastError();
+        return r;
+    }
+    for (int i = 0; i < 8; ++i) sg.key[i] = key[i];
+    sg.launches = nl;
+    return XDEM_OK;
+}
+
 }  // namespace
 
 bool xdem_sim::precision_mixed() const { return cfg.precision == XDEM_MIXED; }
@@ -433,6 +519,7 @@ XDEM_API int xdem_sim_destroy(xdem_sim* s)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->st) cudaStreamSynchronize(s->st);
+    drop_graph(s);
     fused_free(s->fs);
     double* dp[] = {s->pos, s->cpos, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass,
                     s->inertia, s->tmax, s->rres, s->rloc, s->pp_tsd, s->pl_tsd, s->ms_tsd, s->d_body,
@@ -649,6 +736,9 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->clusters && !s->xci) return XDEM_ERR_ARG;
+    // the graph bakes in the tables' pointers, the body set and the values
+    // computed when the step is primed: any of those changing drops it
+    if (s->dirty_alloc || s->dirty_bodies || !s->fs.primed) drop_graph(s);
     if (int r = ensure_tables(s)) return r;
     if (int r = upload_bodies(s)) return r;
     s->launches = 0;
@@ -659,6 +749,47 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
         }
     }
     unsigned int recorded = 0;
+    const bool fused = !s->cfg.launcher_path && !s->clusters;
+    if (s->use_graph && fused && !s->profiling) {
+        // eager steps until the step has been primed, then one graph per
+        // arrangement of the double buffers, each replayed with the host
+        // side of the step (its swaps) applied by hand
+        unsigned int i = 0;
+        while (i < nsteps) {
+            if (s->fs.primed && s->fs.have_prev) {
+                int g = find_graph(s);
+                bool captured = false;
+                if (g < 0) {
+                    g = s->graphs[0].exec ? 1 : 0;
+                    if (s->graphs[g].exec) {  // neither arrangement matches: start over
+                        drop_graph(s);
+                        g = 0;
+                    }
+                    captured = capture_step_graph(s, g) == XDEM_OK;
+                    if (!captured) g = -1;
+                }
+                if (g >= 0) {
+                    const cudaError_t e = cudaGraphLaunch(s->graphs[g].exec, s->st);
+                    if (e != cudaSuccess) return cerr(e);
+                    if (!captured) step_swaps(s);
+                    s->launches += s->graphs[g].launches;
+                    s->cells_clean = true;
+                    ++i;
+                    continue;
+                }
+            }
+            FusedArgs a = fused_args(s);
+            unsigned int nl = 0;
+            if (int r = fused_step(s->fs, a, s->st, nullptr, nullptr, &nl)) return r;
+            s->launches += nl;
+            s->cells_clean = true;
+            ++i;
+        }
+        s->prof_ms = 0.0;
+        s->prof_contact_launches = 0;
+        s->prof_launches = s->launches;
+        return cerr(cudaGetLastError());
+    }
     for (unsigned int i = 0; i < nsteps; ++i) {
         int r;
         const bool rec = s->profiling && recorded < (unsigned int)xdem_sim::kProfEvents;
@@ -774,6 +905,14 @@ XDEM_API int xdem_sim_set_profiling(xdem_sim* s, int on)
 {
     if (!s) return XDEM_ERR_ARG;
     s->profiling = on != 0;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_set_graph(xdem_sim* s, int on)
+{
+    if (!s) return XDEM_ERR_ARG;
+    s->use_graph = on != 0;
+    if (!s->use_graph) drop_graph(s);
     return XDEM_OK;
 }
 

@@ -137,6 +137,10 @@ class Sim:
     def set_profiling(self, on):
         self.L.xdem_sim_set_profiling(self.h, int(on))
 
+    def set_graph(self, on):
+        """Replay the step from a captured CUDA graph (identical results)."""
+        _lib.check(self.L.xdem_sim_set_graph(self.h, int(on)), "xdem_sim_set_graph")
+
     def profile(self):
         nl = C.c_uint()
         ms = C.c_double()
