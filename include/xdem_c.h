@@ -339,6 +339,24 @@ XDEM_API int xdem_sim_set_clusters(xdem_sim* sim, const double* cpos,
                                    unsigned int nrloc);
 XDEM_API int xdem_sim_set_pp_contact(xdem_sim* sim,
                                      const device_contact_property* cp);
+/* Batched scenes (parameter sweeps): declares that the handle's particles
+ * form nscene independent scenes -- particles [first[s], first[s+1]) with
+ * particle-particle contact property pp_cp[s] and planes
+ * [plane_first[s], plane_first[s+1]) (plane indices in the order of
+ * xdem_sim_add_plane; planes must all be added before the next step).
+ * Particles of different scenes never form contacts; each scene's first
+ * plane starts its plane list as plane 0 does in a single scene.  A batch
+ * runs the fused step only (no clusters, meshes or launcher_path) and keeps
+ * no body wrenches (xdem_sim_body_wrench returns XDEM_ERR_ARG).  For speed
+ * the scenes should sit apart in space (the same grid serves all of them). */
+XDEM_API int xdem_sim_set_scenes(xdem_sim* sim, unsigned int nscene,
+                                 const unsigned int* first,
+                                 const device_contact_property* pp_cp,
+                                 const unsigned int* plane_first);
+/* Kinetic energy and stored particle-particle + particle-plane contacts of
+ * every scene of a batch (host arrays of nscene entries). */
+XDEM_API int xdem_sim_scene_energy(xdem_sim* sim, double* ke,
+                                   unsigned int* ncontact);
 /* Adds a plane; returns its body index through *body (planes and meshes
  * share one body numbering). */
 XDEM_API int xdem_sim_add_plane(xdem_sim* sim, const device_plane_info* plane,

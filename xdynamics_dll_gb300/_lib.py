@@ -53,6 +53,8 @@ _SIGS = {
     "xdem_sim_set_state": ([vp] * 9, i32),
     "xdem_sim_set_clusters": ([vp, vp, vp, u32, vp, u32], i32),
     "xdem_sim_set_pp_contact": ([vp, vp], i32),
+    "xdem_sim_set_scenes": ([vp, u32, vp, vp, vp], i32),
+    "xdem_sim_scene_energy": ([vp, vp, vp], i32),
     "xdem_sim_add_plane": ([vp] * 5, i32),
     "xdem_sim_add_mesh": ([vp, u32, vp, vp, vp, vp], i32),
     "xdem_sim_get_mesh": ([vp, i32, vp, vp, vp], i32),

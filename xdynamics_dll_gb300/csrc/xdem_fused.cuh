@@ -164,10 +164,11 @@ k_fused_contact(const ContactLaunch c)
     d3 F = mk3(0, 0, 0), M = mk3(0, 0, 0), tma = mk3(0, 0, 0);
     double res = 0.0;
     unsigned int bits = 0;
+    const unsigned int scene = live ? scene_index(c, oid) : 0u;
 
     // ------------------------------------------------ particle-particle (impl:613-733)
     if (live && c.has_pp) {
-        const mat_pair mp = c.mp[0];
+        const mat_pair mp = c.mp[scene];
         const MatR<R> mr = mat_r<R>(mp);
         const unsigned int sid = oid * MAX_P2P_COUNT;
         unsigned int old_count = c.pp_count_old[oid];
@@ -187,6 +188,7 @@ k_fused_contact(const ContactLaunch c)
                     for (unsigned int j = start; j < end; ++j) {
                         const unsigned int k = c.sorted_index[j];
                         if (k == oid || k >= c.np) continue;
+                        if (c.scene_of && c.scene_of[k] != scene) continue;  // another scene of the batch
                         if (filt) {
                             const float4 jf = reinterpret_cast<const float4*>(c.snap_f)[j];
                             if (rr_i >= 0.f && jf.w >= 0.f) {
@@ -289,14 +291,19 @@ k_fused_contact(const ContactLaunch c)
                 sl_a[q] = t.x; sl_b[q] = t.y;
             }
         }
-        for (unsigned int k = 0; k < c.nplane; ++k) {
+        // a batched scene sees only its own planes and keeps no wrenches (no
+        // block reduction, so threads may walk different plane ranges)
+        const bool batched = c.scene_plane_first != nullptr;
+        const unsigned int kbeg = batched ? c.scene_plane_first[scene] : 0u;
+        const unsigned int kend = batched ? (live ? c.scene_plane_first[scene + 1] : kbeg) : c.nplane;
+        for (unsigned int k = kbeg; k < kend; ++k) {
             double f6[6] = {0, 0, 0, 0, 0, 0};
             bool touched = false;
             // Conservative FP32 test: every region of the plane test (corner,
             // edge, face; impl:735-815) needs the centre within r of the
             // plane and of the rectangle's extent, up to the cohesion range.
             bool near = true;
-            if (live && ipf.w >= 0.f && c.mp[1 + k].coh == 0.0) {
+            if (live && ipf.w >= 0.f && c.mp[c.nscene + k].coh == 0.0) {
                 const PlaneF pf = c.planef[k];
                 const float dx = ipf.x - pf.v[0], dy = ipf.y - pf.v[1], dz = ipf.z - pf.v[2];
                 const float wx = dx * pf.v[3] + dy * pf.v[4] + dz * pf.v[5];
@@ -308,10 +315,10 @@ k_fused_contact(const ContactLaunch c)
             if (live && near) {
                 const device_plane_info& pl = c.planes[k];
                 const unsigned int pid = pl.id;
-                const mat_pair mp = c.mp[1 + k];
+                const mat_pair mp = c.mp[c.nscene + k];
                 const MatR<R> mr = mat_r<R>(mp);
                 const body_state b = load_body(c.body + 15 * k);
-                if (pid == 0) cnt = 0;
+                if (k == kbeg) cnt = 0;  // the scene's first plane restarts the list (impl:989)
                 const d3 dp = ipos - dv3(pl.xw);
                 d3 unit = mk3(0, 0, 0);
                 const d3 wp = mk3(dot(dp, dv3(pl.u1)), dot(dp, dv3(pl.u2)), dot(dp, dv3(pl.uw)));
@@ -369,7 +376,7 @@ k_fused_contact(const ContactLaunch c)
                     }
                 }
             }
-            emit_body(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, sm);
+            if (!batched) emit_body(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, sm);
         }
         if (live) c.pl_count[oid] = cnt;
     }
@@ -382,7 +389,7 @@ k_fused_contact(const ContactLaunch c)
             if (live) {
                 const unsigned int lo = c.np + c.mesh_first[m], ntri = c.mesh_ntri[m];
                 const int bidx = c.mesh_body[m];
-                const mat_pair mp = c.mp[1 + bidx];
+                const mat_pair mp = c.mp[c.nscene + bidx];
                 const MatR<R> mr = mat_r<R>(mp);
                 const unsigned int sid = oid * MAX_P2MS_COUNT;
                 unsigned int o_id[MAX_P2MS_COUNT];

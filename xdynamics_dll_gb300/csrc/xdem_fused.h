@@ -20,9 +20,16 @@
 // coordinates, so the relative position of two neighbours is formed in FP32
 // to about 1e-9 m without FP64 arithmetic in the neighbour loop; the state
 // stays FP64 and only receives FP32 increments (xdem_fused_mixed.cu).
+//
+// Batched scenes: a handle may hold several independent scenes (particles
+// tagged by scene, each scene with its own particle-particle material and
+// its own range of planes); contacts between particles of different scenes
+// are not formed.  Batched handles produce no body wrenches.
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <vector>
 
 #include "../../include/xdem_c.h"
 
@@ -30,7 +37,6 @@ namespace xdem {
 
 struct mat_pair;
 constexpr unsigned int kMaxFusedMeshes = 8;
-constexpr unsigned int kMaxFusedBodies = 64;
 constexpr unsigned int kBboxBlocks = 1024;
 constexpr int kPlaneF = 16;  // floats per plane in the prefilter table
 
@@ -87,17 +93,19 @@ struct FusedState {
     float* fA = nullptr;        // [np*4] particle-particle force, rolling resistance (original order)
     float* fB = nullptr;        // [np*4] particle-particle moment
     float* fC = nullptr;        // [np*4] rolling: sum of contact moments
-    MatF* d_mpf = nullptr;      // [kMaxFusedBodies + 1] FP32 material table
+    MatF* d_mpf = nullptr;      // FP32 material table (scenes' particle pairs, then bodies)
+    size_t mpf_cap = 0;
     unsigned int* pp_count2 = nullptr;
     unsigned int* pp_id2 = nullptr;
     double* pp_tsd2 = nullptr;
     unsigned int* skey_prev = nullptr;  // [nentry] sorted keys of the last step
     double* d_energy = nullptr;
     double* d_bbox = nullptr;   // [kBboxBlocks * 6] block min/max of positions
-    PlaneF* d_planef = nullptr; // [kMaxFusedBodies]
-    PlaneDF* d_planedf = nullptr; // [kMaxFusedBodies]
-    PlaneF h_planef[kMaxFusedBodies];     // host copies (sources of the uploads)
-    PlaneDF h_planedf[kMaxFusedBodies];
+    PlaneF* d_planef = nullptr; // [plane_cap]
+    PlaneDF* d_planedf = nullptr; // [plane_cap]
+    size_t plane_cap = 0;
+    std::vector<PlaneF> h_planef;     // host copies (sources of the uploads)
+    std::vector<PlaneDF> h_planedf;
     double origin[3] = {0.0, 0.0, 0.0};
     double frame_far2 = 0.0;    // squared radius (from the grid origin) of the FP32 frame
     float frame_margin = 0.f;   // prefilter slack for FP32 rounding
@@ -136,14 +144,19 @@ struct FusedArgs {
     double *bsums, *wrench;
     unsigned int* status;
     bool rolling;              // any contact property with rolling friction
+    // batched scenes (nscene == 1: a single scene, scene_of unused)
+    unsigned int nscene = 1;
+    const unsigned int* scene_of = nullptr;          // [np]
+    const unsigned int* scene_plane_first = nullptr; // [nscene + 1]
 };
 
 int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st);
 void fused_free(FusedState& fs);
 void fused_invalidate(FusedState& fs);
+// host_mp holds nscene particle-pair entries followed by one per body.
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
                      const mat_pair* mp, const device_plane_info* host_planes, const mat_pair* host_mp,
-                     unsigned int nmp, const double origin[3], cudaStream_t st);
+                     unsigned int nmp, unsigned int nscene, const double origin[3], cudaStream_t st);
 // New frame of plane k (its body moved): refreshes the plane tables on the
 // stream; the host copy it uploads from stays owned by the state.
 int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh,
@@ -151,6 +164,11 @@ int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& 
 // Runs one step.  When e0/e1 are given they bracket the contact kernel.
 int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                unsigned int* nlaunch);
+// Kinetic energy and stored particle-particle + plane contacts of each scene
+// of a batch (d_first [nscene + 1] particle ranges, d_out [2 * nscene]).
+int fused_scene_energy(const double* vel, const double* ep, const double* ev, const double* mass,
+                       const double* inertia, const unsigned int* d_first, unsigned int nscene, const unsigned int* c0,
+                       const unsigned int* c1, double* d_out, double* ke, unsigned int* ncontact, cudaStream_t st);
 // Kinetic energy (translational + rotational) and number of stored contacts.
 int fused_energy(FusedState& fs, const double* vel, const double* ep, const double* ev, const double* mass,
                  const double* inertia, unsigned int ns, const unsigned int* c0, const unsigned int* c1,
@@ -224,7 +242,18 @@ struct ContactLaunch {
     double* bsums;  // [nbody][nblocks][6]
     unsigned int nblocks;
     unsigned int* status;
+    // batched scenes: material tables hold nscene particle-pair entries, then
+    // one per body; a particle only meets particles and planes of its scene
+    unsigned int nscene;
+    const unsigned int* scene_of;          // [np] or null (one scene)
+    const unsigned int* scene_plane_first; // [nscene + 1] or null
 };
+
+// Scene of a particle and the range of planes it sees.
+__host__ __device__ inline unsigned int scene_index(const ContactLaunch& c, unsigned int oid)
+{
+    return c.scene_of ? c.scene_of[oid] : 0u;
+}
 
 cudaError_t launch_fused_contact_fp64(const ContactLaunch& c, cudaStream_t st);
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st);

@@ -226,7 +226,67 @@ __global__ void k_energy(const double* vel, const double* ep, const double* ev, 
     }
 }
 
+// Kinetic energy and stored contacts per scene of a batch: one block per
+// scene over its particle range [first[s], first[s + 1]) (free spheres).
+__global__ void k_scene_energy(const double* vel, const double* ep, const double* ev, const double* mass,
+                               const double* inertia, const unsigned int* first, const unsigned int* c0,
+                               const unsigned int* c1, double* out)
+{
+    __shared__ double sk[8];
+    __shared__ unsigned int sc[8];
+    const unsigned int s = blockIdx.x;
+    double ke = 0.0;
+    unsigned int cnt = 0;
+    for (unsigned int i = first[s] + threadIdx.x; i < first[s + 1]; i += blockDim.x) {
+        const d3 v = ld3(vel, i);
+        const d4 e = ld4(ep, i), d = ld4(ev, i);
+        const double w0 = 2.0 * (-e.y * d.x + e.x * d.y + e.w * d.z - e.z * d.w);
+        const double w1 = 2.0 * (-e.z * d.x - e.w * d.y + e.x * d.z + e.y * d.w);
+        const double w2 = 2.0 * (-e.w * d.x + e.z * d.y - e.y * d.z + e.x * d.w);
+        const d3 J = ld3(inertia, i);
+        ke += 0.5 * mass[i] * dot(v, v) + 0.5 * (J.x * w0 * w0 + J.y * w1 * w1 + J.z * w2 * w2);
+        cnt += c0[i] + c1[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ke += __shfl_down_sync(0xffffffffu, ke, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sk[threadIdx.x >> 5] = ke;
+        sc[threadIdx.x >> 5] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double k = 0.0;
+        unsigned int n = 0;
+        for (unsigned int w = 0; w < (blockDim.x >> 5); ++w) {
+            k += sk[w];
+            n += sc[w];
+        }
+        out[2 * s] = k;
+        out[2 * s + 1] = (double)n;
+    }
+}
+
 }  // namespace
+
+int fused_scene_energy(const double* vel, const double* ep, const double* ev, const double* mass,
+                       const double* inertia, const unsigned int* d_first, unsigned int nscene, const unsigned int* c0,
+                       const unsigned int* c1, double* d_out, double* ke, unsigned int* ncontact, cudaStream_t st)
+{
+    if (!nscene) return XDEM_OK;
+    k_scene_energy<<<nscene, 256, 0, st>>>(vel, ep, ev, mass, inertia, d_first, c0, c1, d_out);
+    cudaError_t e = cudaGetLastError();
+    std::vector<double> h((size_t)nscene * 2);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return XDEM_ERR_CUDA;
+    for (unsigned int s = 0; s < nscene; ++s) {
+        if (ke) ke[s] = h[2 * s];
+        if (ncontact) ncontact[s] = (unsigned int)h[2 * s + 1];
+    }
+    return XDEM_OK;
+}
 
 int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st)
 {
@@ -261,7 +321,6 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
     if (e == cudaSuccess) e = dalloc(fs.skey_prev, nentry);
     if (e == cudaSuccess) e = dalloc(fs.d_energy, 2);
     if (e == cudaSuccess) e = dalloc(fs.d_bbox, (size_t)kBboxBlocks * 6);
-    if (e == cudaSuccess && !fs.d_planef) e = dalloc(fs.d_planef, kMaxFusedBodies);
     if (e == cudaSuccess) e = cudaMemsetAsync(fs.pp_count2, 0, np * sizeof(unsigned int), st);
     fs.primed = false;
     fs.have_prev = false;
@@ -337,35 +396,43 @@ void plane_tables(const device_plane_info& pl, const double origin[3], bool coh,
 
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
                      const mat_pair* mp, const device_plane_info* host_planes, const mat_pair* host_mp,
-                     unsigned int nmp, const double origin[3], cudaStream_t st)
+                     unsigned int nmp, unsigned int nscene, const double origin[3], cudaStream_t st)
 {
     fs.planes = planes;
     fs.nplane = nplane;
     fs.body = body;
     fs.mp = mp;
     for (int i = 0; i < 3; ++i) fs.origin[i] = origin[i];
-    if (nmp > kMaxFusedBodies + 1) return XDEM_ERR_ARG;
-    if (!fs.d_mpf && dalloc(fs.d_mpf, kMaxFusedBodies + 1) != cudaSuccess) return XDEM_ERR_ALLOC;
-    MatF mf[kMaxFusedBodies + 1];
+    if (nmp < nscene + nplane) return XDEM_ERR_ARG;
+    if (nmp > fs.mpf_cap) {
+        if (dalloc(fs.d_mpf, nmp) != cudaSuccess) return XDEM_ERR_ALLOC;
+        fs.mpf_cap = nmp;
+    }
+    std::vector<MatF> mf(nmp);
     for (unsigned int i = 0; i < nmp; ++i) {
         const mat_pair& m = host_mp[i];
         mf[i] = MatF{(float)m.Eeq, (float)m.Seq8, (float)m.beta, (float)m.vs1, (float)m.sratio, (float)m.fric,
                      (float)m.rfric, m.coh != 0.0 ? 1 : 0};
     }
     if (nmp) {
-        cudaError_t e = cudaMemcpyAsync(fs.d_mpf, mf, nmp * sizeof(MatF), cudaMemcpyHostToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(fs.d_mpf, mf.data(), nmp * sizeof(MatF), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return XDEM_ERR_CUDA;
     }
     if (!nplane) return XDEM_OK;
-    if (nplane > kMaxFusedBodies) return XDEM_ERR_ARG;
-    if (!fs.d_planef && dalloc(fs.d_planef, kMaxFusedBodies) != cudaSuccess) return XDEM_ERR_ALLOC;
-    if (!fs.d_planedf && dalloc(fs.d_planedf, kMaxFusedBodies) != cudaSuccess) return XDEM_ERR_ALLOC;
+    if (nplane > fs.plane_cap) {
+        if (dalloc(fs.d_planef, nplane) != cudaSuccess || dalloc(fs.d_planedf, nplane) != cudaSuccess)
+            return XDEM_ERR_ALLOC;
+        fs.plane_cap = nplane;
+    }
+    fs.h_planef.assign(nplane, PlaneF{});
+    fs.h_planedf.assign(nplane, PlaneDF{});
     for (unsigned int k = 0; k < nplane; ++k)
-        plane_tables(host_planes[k], origin, host_mp[1 + k].coh != 0.0, fs.h_planef[k], fs.h_planedf[k]);
-    cudaError_t e = cudaMemcpyAsync(fs.d_planef, fs.h_planef, nplane * sizeof(PlaneF), cudaMemcpyHostToDevice, st);
+        plane_tables(host_planes[k], origin, host_mp[nscene + k].coh != 0.0, fs.h_planef[k], fs.h_planedf[k]);
+    cudaError_t e =
+        cudaMemcpyAsync(fs.d_planef, fs.h_planef.data(), nplane * sizeof(PlaneF), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(fs.d_planedf, fs.h_planedf, nplane * sizeof(PlaneDF), cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(fs.d_planedf, fs.h_planedf.data(), nplane * sizeof(PlaneDF), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
 }
@@ -501,11 +568,14 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.nblocks = (n + kFusedThreads - 1) / kFusedThreads;
     c.bsums = a.bsums;
     c.status = a.status;
+    c.nscene = a.nscene ? a.nscene : 1;
+    c.scene_of = c.nscene > 1 ? a.scene_of : nullptr;
+    c.scene_plane_first = c.nscene > 1 ? a.scene_plane_first : nullptr;
     if (e0) cudaEventRecord(e0, st);
     ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
     if (fs.mixed) nl++;  // the mixed contact stage is two kernels (pairs, bodies)
     if (e1) cudaEventRecord(e1, st);
-    if (a.nbody) {
+    if (a.nbody && c.nscene == 1) {  // batched handles keep no body wrenches
         k_body_sums<<<a.nbody * 6, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench);
         ok(cudaGetLastError());
     }

@@ -216,13 +216,14 @@ constexpr unsigned int kStage = 16;
 __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oid, unsigned int j, unsigned int ux,
                                          unsigned int uy, unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
                                          unsigned int sid, unsigned int old_count, const unsigned int* old_id,
-                                         bool coh, V3<float>& Ft, V3<float>& Fn,
+                                         unsigned int scene, bool coh, V3<float>& Ft, V3<float>& Fn,
                                          unsigned int& cnt, Acc& acc, unsigned int& bits)
 {
     const float cs = c.cs_f, cs_lo = c.cs_lo;
     // every record of the candidate in one round trip (the screen is tight,
     // so velocity and spin are nearly always needed)
     const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
+    if (c.scene_of && c.scene_of[it.x] != scene) return;  // another scene of the batch
     const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
     const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
     const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
@@ -246,7 +247,7 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
     const unsigned int slot = sid + cnt;
     if (!(cdist > 0.f)) {
         if (!coh) return;
-        const mat_pair& mp = c.mp[0];
+        const mat_pair& mp = c.mp[scene];
         const double csd = limit_cohesion_depth(mp, ir, Aj.w);
         if (!(fabs((double)cdist) < fabs(csd))) return;
         const V3<float> unit = qdiv(rp, dist);
@@ -271,7 +272,7 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
             sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
             break;
         }
-    const MatR<float> mr = matr(c.mpf[0]);
+    const MatR<float> mr = matr(c.mpf[scene]);
     const V3<float> unit = qdiv(rp, dist);
     const V3<float> dcpr = ir * unit;
     const V3<float> dcpr_j = dcpr - rp;
@@ -282,7 +283,7 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
     if (coh) {
         const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
         const double fdn = (double)fc.vn * (double)tdot(rv, unit);
-        fca = (float)(-cohesion_force(c.mp[0], ir, Aj.w, fsn + fdn));
+        fca = (float)(-cohesion_force(c.mp[scene], ir, Aj.w, fsn + fdn));
     }
     model_f(c.prm.contact_model, fc, c.dt_f, cdist, sd0, sd1, rv, unit, Ft, Fn, fca);
     const V3<float> fsum = Fn + Ft;
@@ -309,7 +310,8 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                                           Acc& acc, unsigned int& bits)
 {
     const device_dem_parameters& p = c.prm;
-    const bool coh = c.mpf[0].coh != 0;
+    const unsigned int scene = scene_index(c, oid);
+    const bool coh = c.mpf[scene].coh != 0;
     const float cs = c.cs_f;
     const float screen = 1.0f + 0x1p-11f;
     const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
@@ -397,8 +399,8 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
         cp_async_wait_all();
         // ---- pass 2: float-pair overlap and contact force, in walk order
         for (unsigned int q = 0; q < nc; ++q)
-            p2p_pair(c, oid, stage[q * kFusedThreads], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, coh, Ft,
-                     Fn, cnt, acc, bits);
+            p2p_pair(c, oid, stage[q * kFusedThreads], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
+                     coh, Ft, Fn, cnt, acc, bits);
     }
     c.pp_count_new[oid] = cnt;
 }
@@ -480,18 +482,18 @@ __device__ __forceinline__ BodyF load_body_f(const double* dbi)
 // The plane slots (impl:950-1080 slot rule) are read from memory when a
 // plane needs them: the thread owns its slots and writes them as it goes, so
 // memory holds exactly what the reference's next plane launch re-reads.
-__device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int k, unsigned int oid, d4 ip,
-                                            V3<float> ivel, V3<float> iom, float im, unsigned int& pl_cnt,
-                                            Acc& acc, float f6[6], unsigned int& bits)
+__device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int k, unsigned int kbeg,
+                                            unsigned int oid, d4 ip, V3<float> ivel, V3<float> iom, float im,
+                                            unsigned int& pl_cnt, Acc& acc, float f6[6], unsigned int& bits)
 {
     const device_dem_parameters& p = c.prm;
     const device_plane_info& pl = c.planes[k];
     const PlaneDF& pd = c.planedf[k];
     const unsigned int pid = pl.id;
-    const mat_pair& mp = c.mp[1 + k];  // FP64 constants: cohesion only
-    const MatR<float> mr = matr(c.mpf[1 + k]);
+    const mat_pair& mp = c.mp[c.nscene + k];  // FP64 constants: cohesion only
+    const MatR<float> mr = matr(c.mpf[c.nscene + k]);
     const unsigned int sid = oid * MAX_P2PL_COUNT;
-    if (pid == 0) pl_cnt = 0;
+    if (k == kbeg) pl_cnt = 0;  // the scene's first plane restarts the list (impl:989)
     const df xd[3] = {split_d(ip.x), split_d(ip.y), split_d(ip.z)};
     const df rd = split_d(ip.w);
     const BodyF b = load_body_f(c.body + 15 * k);
@@ -580,8 +582,8 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
     const double ir = ip.w;
     const unsigned int lo = c.np + c.mesh_first[m], ntri = c.mesh_ntri[m];
     const int bidx = c.mesh_body[m];
-    const mat_pair& mp = c.mp[1 + bidx];  // FP64 constants: cohesion only
-    const MatR<float> mr = matr(c.mpf[1 + bidx]);
+    const mat_pair& mp = c.mp[c.nscene + bidx];  // FP64 constants: cohesion only
+    const MatR<float> mr = matr(c.mpf[c.nscene + bidx]);
     const unsigned int sid = oid * MAX_P2MS_COUNT;
     unsigned int o_id[MAX_P2MS_COUNT];
     float o_a[MAX_P2MS_COUNT], o_b[MAX_P2MS_COUNT];
@@ -798,8 +800,8 @@ struct PlaneOut {
     unsigned int cnt, bits;
     int touched;
 };
-__device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned int k, unsigned int oid, d4 ip,
-                                            float4 Bi, float4 Ci, unsigned int cnt)
+__device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned int k, unsigned int kbeg,
+                                            unsigned int oid, d4 ip, float4 Bi, float4 Ci, unsigned int cnt)
 {
     Acc a;
     a.tm = v3<float>(0.f, 0.f, 0.f);
@@ -808,8 +810,8 @@ __device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned in
     PlaneOut o;
     o.bits = 0;
     o.cnt = cnt;
-    o.touched = plane_mixed(*cp, k, oid, ip, v3<float>(Bi.x, Bi.y, Bi.z), v3<float>(Ci.x, Ci.y, Ci.z), Bi.w, o.cnt,
-                            a, f6, o.bits);
+    o.touched = plane_mixed(*cp, k, kbeg, oid, ip, v3<float>(Bi.x, Bi.y, Bi.z), v3<float>(Ci.x, Ci.y, Ci.z), Bi.w,
+                            o.cnt, a, f6, o.bits);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         o.f[i] = a.f[i].value();
@@ -922,7 +924,13 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_mixed_bodies(const __grid_
         if (live)
             ipf = make_float4(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2], Ai.w);
         unsigned int pl_cnt = 0;
-        for (unsigned int k = 0; k < c.nplane; ++k) {
+        // a batched scene sees only its own planes and keeps no wrenches (no
+        // block reduction, so threads may walk different plane ranges)
+        const bool batched = c.scene_plane_first != nullptr;
+        const unsigned int scene = live ? scene_index(c, oid) : 0u;
+        const unsigned int kbeg = batched ? c.scene_plane_first[scene] : 0u;
+        const unsigned int kend = batched ? (live ? c.scene_plane_first[scene + 1] : kbeg) : c.nplane;
+        for (unsigned int k = kbeg; k < kend; ++k) {
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             bool touched = false;
             // conservative FP32 test: every region of the plane test needs the
@@ -938,7 +946,7 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_mixed_bodies(const __grid_
                 near = fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
             }
             if (live && near) {
-                const PlaneOut o = plane_call(&c, k, oid, ip, Bi, Ci, pl_cnt);
+                const PlaneOut o = plane_call(&c, k, kbeg, oid, ip, Bi, Ci, pl_cnt);
                 touched = o.touched != 0;
                 pl_cnt = o.cnt;
                 bits |= o.bits;
@@ -954,7 +962,7 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_mixed_bodies(const __grid_
                     acc.rs += o.rs;
                 }
             }
-            emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
+            if (!batched) emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
         }
         if (live) c.pl_count[oid] = pl_cnt;
     }

@@ -28,6 +28,10 @@
 
 using namespace xdem;
 
+// Planes and meshes a handle can hold (batched scenes bring several planes
+// each).
+constexpr size_t kMaxBodies = 1u << 16;
+
 struct SimBody {
     int kind;              // 0 plane, 1 mesh
     int index;             // plane index or mesh index
@@ -62,7 +66,7 @@ struct xdem_sim {
     // contacts
     bool has_pp = false;
     device_contact_property pp_cp{};
-    mat_pair* d_mp = nullptr;  // [0] pp, then one per body
+    mat_pair* d_mp = nullptr;  // [nscene] particle pairs of each scene, then one per body
     unsigned int *pp_count = nullptr, *pp_id = nullptr;
     double* pp_tsd = nullptr;
     unsigned int *pl_count = nullptr, *pl_id = nullptr;
@@ -106,6 +110,16 @@ struct xdem_sim {
     };
     bool use_graph = false;
     StepGraph graphs[2];
+    // batched scenes (nscene == 1: one scene)
+    unsigned int nscene = 1;
+    std::vector<unsigned int> scene_first, scene_plane_first;
+    std::vector<device_contact_property> scene_cp;
+    unsigned int* d_scene_of = nullptr;           // [np]
+    unsigned int* d_scene_first = nullptr;        // [nscene + 1]
+    unsigned int* d_scene_plane_first = nullptr;  // [nscene + 1]
+    double* d_scene_energy = nullptr;             // [2 * nscene]
+    // capacities of the body tables
+    size_t plane_cap = 0, body_cap = 0, mp_cap = 0;
 };
 
 namespace {
@@ -206,10 +220,12 @@ int ensure_tables(xdem_sim* s)
     A(s->sorted_index, s->nentry);
     const unsigned int nb = blocks_for(s->nentry);
     const size_t nbody = std::max<size_t>(s->bodies.size(), 1);
-    A(s->bsums, (size_t)nb * 6 * nbody);
+    // batched handles keep no body wrenches: no per-block partials
+    A(s->bsums, (size_t)nb * 6 * (s->nscene > 1 ? 1 : nbody));
     A(s->wrench, 6 * nbody);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->wrench, 0, 6 * nbody * sizeof(double), s->st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->bsums, 0, (size_t)nb * 6 * nbody * sizeof(double), s->st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(s->bsums, 0, (size_t)nb * 6 * (s->nscene > 1 ? 1 : nbody) * sizeof(double), s->st);
     if (e != cudaSuccess) return XDEM_ERR_ALLOC;
     if (int r = fused_alloc(s->fs, n, s->nentry, s->precision_mixed(), s->st)) return r;
     s->skey = nullptr;
@@ -223,22 +239,35 @@ int upload_bodies(xdem_sim* s)
     if (!s->dirty_bodies) return XDEM_OK;
     cudaError_t e = cudaSuccess;
     const size_t nb = s->bodies.size();
+    const size_t S = s->nscene;
     if (s->planes.size()) {
-        if (!s->d_planes) e = dalloc(s->d_planes, 64);
+        if (s->planes.size() > s->plane_cap) {
+            e = dalloc(s->d_planes, s->planes.size());
+            s->plane_cap = e == cudaSuccess ? s->planes.size() : 0;
+        }
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(s->d_planes, s->planes.data(), s->planes.size() * sizeof(device_plane_info),
                                 cudaMemcpyHostToDevice, s->st);
     }
     std::vector<double> rec(std::max<size_t>(nb, 1) * 15, 0.0);
     for (size_t i = 0; i < nb; ++i) std::memcpy(&rec[i * 15], s->bodies[i].rec, sizeof(double) * 15);
+    if (e == cudaSuccess && rec.size() / 15 > s->body_cap) {
+        e = dalloc(s->d_body, rec.size());
+        s->body_cap = e == cudaSuccess ? rec.size() / 15 : 0;
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->d_body, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice, s->st);
-    // material constants: [0] particle-particle, [1 + b] body b
-    std::vector<mat_pair> mps(nb + 1);
-    mps[0] = make_mat_pair(s->pp_cp, s->prm.contact_model, false);
+    // material constants: [s] particle-particle of scene s, [nscene + b] body b
+    std::vector<mat_pair> mps(S + nb);
+    for (size_t k = 0; k < S; ++k)
+        mps[k] = make_mat_pair(S > 1 ? s->scene_cp[k] : s->pp_cp, s->prm.contact_model, false);
     for (size_t i = 0; i < nb; ++i)
-        mps[i + 1] = make_mat_pair(s->body_cp[i], s->prm.contact_model,
+        mps[S + i] = make_mat_pair(s->body_cp[i], s->prm.contact_model,
                                    s->clusters && s->bodies[i].kind == 0 /* cluster-plane swap */);
+    if (e == cudaSuccess && mps.size() > s->mp_cap) {
+        e = dalloc(s->d_mp, mps.size());
+        s->mp_cap = e == cudaSuccess ? mps.size() : 0;
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->d_mp, mps.data(), mps.size() * sizeof(mat_pair), cudaMemcpyHostToDevice, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -246,7 +275,7 @@ int upload_bodies(xdem_sim* s)
     s->dirty_bodies = false;
     const double org[3] = {s->prm.world_origin.x, s->prm.world_origin.y, s->prm.world_origin.z};
     return fused_set_bodies(s->fs, s->d_planes, (unsigned int)s->planes.size(), s->d_body, s->d_mp,
-                            s->planes.data(), mps.data(), (unsigned int)mps.size(), org, s->st);
+                            s->planes.data(), mps.data(), (unsigned int)mps.size(), (unsigned int)S, org, s->st);
 }
 
 // ---------------------------------------------------------------- launcher-order step
@@ -299,7 +328,7 @@ int step_launcher(xdem_sim* s, cudaEvent_t e0, cudaEvent_t e1)
         BodyPartials bp{};
         bp.block_sums = s->bsums + (size_t)b * nb * 6;
         const double* dbi = s->d_body + 15 * b;
-        const mat_pair* mp = s->d_mp + 1 + b;
+        const mat_pair* mp = s->d_mp + s->nscene + b;
         if (bd.kind == 0) {
             const device_plane_info* pl = s->d_planes + bd.index;
             if (s->clusters)
@@ -362,6 +391,10 @@ FusedArgs fused_args(xdem_sim* s)
     a.status = s->d_status;
     a.rolling = s->has_pp && s->pp_cp.rfric != 0.0;
     for (const device_contact_property& cp : s->body_cp) a.rolling = a.rolling || cp.rfric != 0.0;
+    for (const device_contact_property& cp : s->scene_cp) a.rolling = a.rolling || cp.rfric != 0.0;
+    a.nscene = s->nscene;
+    a.scene_of = s->d_scene_of;
+    a.scene_plane_first = s->d_scene_plane_first;
     return a;
 }
 
@@ -493,6 +526,8 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
     A(s->d_status, 1);
     A(s->d_mp, 65);
     A(s->d_body, 64 * 15);
+    s->mp_cap = 65;
+    s->body_cap = 64;
     if (s->clusters) A(s->cpos, ns * 4);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
@@ -523,11 +558,12 @@ XDEM_API int xdem_sim_destroy(xdem_sim* s)
     fused_free(s->fs);
     double* dp[] = {s->pos, s->cpos, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass,
                     s->inertia, s->tmax, s->rres, s->rloc, s->pp_tsd, s->pl_tsd, s->ms_tsd, s->d_body,
-                    s->d_vlist, s->d_dlocal, s->d_sphere, s->bsums, s->wrench};
+                    s->d_vlist, s->d_dlocal, s->d_sphere, s->bsums, s->wrench, s->d_scene_energy};
     for (double* q : dp)
         if (q) cudaFree(q);
     unsigned int* up[] = {s->k0, s->v0, s->k1, s->v1, s->hist, s->cstart, s->cend, s->sorted_index, s->pp_count,
-                          s->pp_id, s->pl_count, s->pl_id, s->ms_count, s->ms_id, s->d_status};
+                          s->pp_id, s->pl_count, s->pl_id, s->ms_count, s->ms_id, s->d_status,
+                          s->d_scene_of, s->d_scene_first, s->d_scene_plane_first};
     for (unsigned int* q : up)
         if (q) cudaFree(q);
     if (s->xci) cudaFree(s->xci);
@@ -614,11 +650,53 @@ XDEM_API int xdem_sim_set_pp_contact(xdem_sim* s, const device_contact_property*
     return XDEM_OK;
 }
 
+XDEM_API int xdem_sim_set_scenes(xdem_sim* s, unsigned int nscene, const unsigned int* first,
+                                 const device_contact_property* pp_cp, const unsigned int* plane_first)
+{
+    if (!s || !nscene || !first || !pp_cp || !plane_first) return XDEM_ERR_ARG;
+    if (s->clusters || s->cfg.launcher_path) return XDEM_ERR_ARG;
+    if (first[0] != 0 || first[nscene] != s->np || plane_first[0] != 0) return XDEM_ERR_ARG;
+    for (unsigned int k = 0; k < nscene; ++k)
+        if (first[k] > first[k + 1] || plane_first[k] > plane_first[k + 1]) return XDEM_ERR_ARG;
+    std::vector<unsigned int> of(s->np);
+    for (unsigned int k = 0; k < nscene; ++k)
+        for (unsigned int i = first[k]; i < first[k + 1]; ++i) of[i] = k;
+    cudaError_t e = dalloc(s->d_scene_of, s->np);
+    if (e == cudaSuccess) e = dalloc(s->d_scene_first, nscene + 1);
+    if (e == cudaSuccess) e = dalloc(s->d_scene_plane_first, nscene + 1);
+    if (e == cudaSuccess) e = dalloc(s->d_scene_energy, 2 * (size_t)nscene);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s->d_scene_of, of.data(), of.size() * sizeof(unsigned int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s->d_scene_first, first, (nscene + 1) * sizeof(unsigned int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s->d_scene_plane_first, plane_first, (nscene + 1) * sizeof(unsigned int),
+                       cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return XDEM_ERR_ALLOC;
+    s->nscene = nscene;
+    s->scene_first.assign(first, first + nscene + 1);
+    s->scene_plane_first.assign(plane_first, plane_first + nscene + 1);
+    s->scene_cp.assign(pp_cp, pp_cp + nscene);
+    s->pp_cp = pp_cp[0];
+    s->has_pp = true;
+    s->dirty_bodies = true;
+    s->dirty_alloc = true;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_scene_energy(xdem_sim* s, double* ke, unsigned int* ncontact)
+{
+    if (!s || s->nscene < 2 || !s->d_scene_first) return XDEM_ERR_ARG;
+    if (int r = ensure_tables(s)) return r;
+    return fused_scene_energy(s->vel, s->ep, s->ev, s->mass, s->inertia, s->d_scene_first, s->nscene, s->pp_count,
+                              s->pl_count, s->d_scene_energy, ke, ncontact, s->st);
+}
+
 XDEM_API int xdem_sim_add_plane(xdem_sim* s, const device_plane_info* plane, const double body[15],
                                 const device_contact_property* cp, int* body_index)
 {
     if (!s || !plane || !body || !cp) return XDEM_ERR_ARG;
-    if (s->bodies.size() >= 64 || s->planes.size() >= 64) return XDEM_ERR_ARG;
+    if (s->bodies.size() >= kMaxBodies) return XDEM_ERR_ARG;
     if (!s->meshes.empty()) return XDEM_ERR_ARG;  // planes first, in id order, then meshes
     SimBody b{};
     b.kind = 0;
@@ -640,7 +718,7 @@ XDEM_API int xdem_sim_add_mesh(xdem_sim* s, unsigned int ntri, const double* vli
                                const device_contact_property* cp, int* body_index)
 {
     if (!s || !ntri || !vlist_local || !body || !cp) return XDEM_ERR_ARG;
-    if (s->bodies.size() >= 64 || s->meshes.size() >= kMaxFusedMeshes) return XDEM_ERR_ARG;
+    if (s->bodies.size() >= kMaxBodies || s->meshes.size() >= kMaxFusedMeshes) return XDEM_ERR_ARG;
     const unsigned int first = s->ntri_total;
     const h3 bp{body[XDEM_PX], body[XDEM_PY], body[XDEM_PZ]};
     h3 R[3];
@@ -706,6 +784,7 @@ XDEM_API int xdem_sim_get_mesh(xdem_sim* s, int body_index, device_triangle_info
 XDEM_API int xdem_sim_set_body(xdem_sim* s, int body_index, const double body[15], const device_plane_info* plane)
 {
     if (!s || body_index < 0 || body_index >= (int)s->bodies.size() || !body) return XDEM_ERR_ARG;
+    if (int r = upload_bodies(s)) return r;  // tables sized for every body added so far
     SimBody& b = s->bodies[body_index];
     std::memcpy(b.rec, body, sizeof(b.rec));
     cudaError_t e = cudaMemcpyAsync(s->d_body + 15 * body_index, b.rec, sizeof(b.rec), cudaMemcpyHostToDevice, s->st);
@@ -736,6 +815,9 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->clusters && !s->xci) return XDEM_ERR_ARG;
+    // a batch needs its planes in place and no meshes (no body wrenches)
+    if (s->nscene > 1 && (s->scene_plane_first.back() != s->planes.size() || !s->meshes.empty()))
+        return XDEM_ERR_ARG;
     // the graph bakes in the tables' pointers, the body set and the values
     // computed when the step is primed: any of those changing drops it
     if (s->dirty_alloc || s->dirty_bodies || !s->fs.primed) drop_graph(s);
@@ -825,6 +907,7 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 XDEM_API int xdem_sim_body_wrench(xdem_sim* s, int body_index, double out6[6])
 {
     if (!s || !out6 || body_index < 0 || body_index >= (int)s->bodies.size()) return XDEM_ERR_ARG;
+    if (s->nscene > 1) return XDEM_ERR_ARG;  // batched handles keep no body wrenches
     cudaError_t e = cudaMemcpyAsync(out6, s->wrench + 6 * body_index, 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     return cerr(e);

@@ -131,6 +131,35 @@ def sphere_drop(n_per_layer_side=41, layers=6, r=1e-3, rho=2500.0, E=1e7, nu=0.3
                  name="sphere_drop", note=f"{N} spheres r={r}")
 
 
+def poly_drop(n, r_min=1e-3, r_max=3e-3, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3, dt=1e-5, box=0.1,
+              seed=7):
+    """Polydisperse drop in the first configuration's open box (0.1 x 0.1 m,
+    floor and four walls): n spheres with radii U[r_min, r_max] on a jittered
+    cubic lattice of pitch 2.4 r_max (jitter +-0.1 r_max) filling the box's
+    footprint layer by layer, walls as tall as the lattice; cell size 2 r_max.
+    The member scene of the batched parameter sweep."""
+    rng = np.random.default_rng(seed)
+    sp = 2.4 * r_max
+    side = max(1, int(np.floor((box - 2.0 * r_max) / sp)) + 1)
+    layers = int(np.ceil(n / (side * side)))
+    width = (side - 1) * sp
+    x0 = -0.5 * width
+    pts = jittered_lattice(side, layers, side, sp, (x0, 2.0 * r_max + 0.5 * sp, x0), 0.1 * r_max, rng)[:n]
+    radii = rng.uniform(r_min, r_max, size=n)
+    pos = np.zeros((n, 4))
+    pos[:, :3] = pts
+    pos[:, 3] = radii
+    m, J = sphere_mass_inertia(radii, rho)
+    vel, acc, ep, ev, ea = _init_state(n)
+    h = max(0.05, pts[:, 1].max() + 4 * r_max)
+    cp = default_material(E, nu, rest, fric)
+    planes = open_box_planes(-0.5 * box, 0.5 * box, 0.0, h, -0.5 * box, 0.5 * box)
+    return Scene(np_=n, ns=n, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=m,
+                 inertia=J.ravel(), dt=dt, cell_size=2.0 * r_max, pp_cp=cp, planes=planes,
+                 plane_cp=[cp] * len(planes), plane_body=[T.body_record() for _ in planes],
+                 name="poly_drop", note=f"{n} spheres r~U[{r_min},{r_max}] fric={fric:.3f} rest={rest:.3f}")
+
+
 def pow2_at_least(n):
     p = 1
     while p < n:
