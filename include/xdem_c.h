@@ -414,6 +414,36 @@ XDEM_API int xdem_sim_set_graph(xdem_sim* sim, int on);
 XDEM_API int xdem_sim_profile(xdem_sim* sim, unsigned int* launches,
                               double* contact_ms, unsigned int* contact_launches);
 
+/* ------------------------------------------------------------------------ */
+/* Adjoint of the FP64 trajectory (reverse mode, checkpointed)              */
+/* ------------------------------------------------------------------------ */
+/* Gradients of a loss on the final positions / velocities of a trajectory
+ * of the handle with respect to each contact property's friction,
+ * restitution and Young's moduli (device_contact_property fric, rest, Ei,
+ * Ej).  Supported: XDEM_FP64 handles of free spheres and planes, contact
+ * model 0 or 1, no cohesion, no rolling resistance, one scene, at most 16
+ * planes.  The forward stores the state every `checkpoint_every` steps; the
+ * backward re-runs each segment from its checkpoint and reverses it.
+ * Bodies must not be moved (xdem_sim_set_body) between forward and
+ * backward.  The reference has no adjoint: this is new surface. */
+typedef struct xdem_adj xdem_adj;
+XDEM_API int xdem_adj_create(xdem_sim* sim, unsigned int checkpoint_every, xdem_adj** out);
+XDEM_API int xdem_adj_destroy(xdem_adj* adj);
+/* Advances the handle nsteps from its current state, keeping checkpoints.
+ * Returns the handle's status bits of those steps (pair-list overflow or
+ * non-finite positions leave no usable adjoint). */
+XDEM_API int xdem_adj_forward(xdem_adj* adj, unsigned int nsteps);
+/* dl_dpos, dl_dvel: DEVICE arrays [np*3] of the loss gradient at the final
+ * state (NULL = 0).  grad: HOST array [4 * nprop], per contact property
+ * (0 = particle-particle, 1 + k = plane k) d/dfric, d/drest, d/dEi, d/dEj.
+ * dl_dpos0, dl_dvel0: optional DEVICE arrays [np*3] receiving the gradient
+ * with respect to the initial positions and velocities.  Leaves the handle
+ * at the end of the first segment's re-run. */
+XDEM_API int xdem_adj_backward(xdem_adj* adj, const double* dl_dpos, const double* dl_dvel, double* grad,
+                               double* dl_dpos0, double* dl_dvel0);
+/* Properties (1 + planes), steps of the last forward, device bytes held. */
+XDEM_API int xdem_adj_info(xdem_adj* adj, unsigned int* nprop, unsigned int* nsteps, unsigned long long* bytes);
+
 #ifdef __cplusplus
 }
 #endif

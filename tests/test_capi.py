@@ -54,3 +54,10 @@ def test_argument_checks_need_no_gpu(L):
     assert L.setDEMSymbolicParameter(None) == T.XDEM_ERR_ARG
     cfg = T.SimConfig()
     assert L.xdem_sim_create(C.byref(cfg), None) == T.XDEM_ERR_ARG
+    # adjoint entry points reject a missing handle before touching the device
+    h = C.c_void_p()
+    assert L.xdem_adj_create(None, 10, C.byref(h)) == T.XDEM_ERR_ARG
+    assert L.xdem_adj_forward(None, 1) == T.XDEM_ERR_ARG
+    assert L.xdem_adj_backward(None, None, None, None, None, None) == T.XDEM_ERR_ARG
+    assert L.xdem_adj_info(None, None, None, None) == T.XDEM_ERR_ARG
+    assert L.xdem_adj_destroy(None) == T.XDEM_ERR_ARG

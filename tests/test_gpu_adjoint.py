@@ -1,0 +1,210 @@
+"""Adjoint of the FP64 trajectory (xdem_adj_* through xdynamics_dll_gb300.adjoint)
+against central finite differences of the same GPU forward, against finite
+differences of the CPU oracle's trajectory (the FP64 reference gradient), and
+across checkpoint intervals.
+
+Finite differences use relative steps of 1e-6 on parameters that enter
+smoothly between contact-set changes; horizons are short enough that no
+contact opens, closes or changes regime (stick/slip) inside the step.
+"""
+import numpy as np
+import pytest
+import torch
+
+from xdynamics_dll_gb300 import scenes
+from xdynamics_dll_gb300 import types as T
+
+pytestmark = pytest.mark.gpu
+
+P0 = (0.3, 0.5, 1e7)  # friction, restitution, Young's modulus
+
+
+@pytest.fixture(scope="module")
+def mods():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from xdynamics_dll_gb300 import build
+    build.build()
+    from xdynamics_dll_gb300 import adjoint, sim
+    return adjoint, sim
+
+
+def packed(n=400, seed=3):
+    return scenes.random_packed(n, 1e-3, 1.5e-3, 0.05, seed, overlap=0.04, vel_scale=0.05, omega_scale=5.0)
+
+
+def weights(n, seed=11):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(n, 3)), rng.normal(size=(n, 3)) * 1e-3
+
+
+def lin_loss(st, w, u):
+    return float((w * st["pos"].reshape(-1, 4)[:, :3]).sum() + (u * st["vel"].reshape(-1, 3)).sum())
+
+
+def gpu_loss(mods, sc, nsteps, w, u, params):
+    adjoint, sim = mods
+    s = sim.Sim(adjoint.with_parameters(sc, *params), precision=T.XDEM_FP64)
+    s.step(nsteps)
+    assert s.status() == 0
+    out = lin_loss(s.state(), w, u)
+    s.close()
+    return out
+
+
+def adjoint_grads(mods, sc, nsteps, w, u, params=P0, K=10, initial=False):
+    adjoint, sim = mods
+    s = sim.Sim(adjoint.with_parameters(sc, *params), precision=T.XDEM_FP64)
+    a = adjoint.Adjoint(s, K)
+    a.forward(nsteps)
+    g, x0, v0 = a.backward(w, u, initial=initial)
+    a.close()
+    s.close()
+    return g, x0, v0
+
+
+def central(f, p, i, rel=1e-6):
+    h = rel * abs(p[i])
+    pp = list(p)
+    pm = list(p)
+    pp[i] += h
+    pm[i] -= h
+    return (f(pp) - f(pm)) / (2 * h)
+
+
+@pytest.mark.parametrize("nsteps", [1, 25])
+def test_parameter_gradients_match_central_differences(mods, nsteps):
+    sc = packed()
+    w, u = weights(sc.np_)
+    g, _, _ = adjoint_grads(mods, sc, nsteps, w, u)
+    ad = [g[:, 0].sum(), g[:, 1].sum(), (g[:, 2] + g[:, 3]).sum()]
+    f = lambda p: gpu_loss(mods, sc, nsteps, w, u, p)
+    for i, name in enumerate(("fric", "rest", "E")):
+        fd = central(f, P0, i)
+        assert abs(ad[i] - fd) <= 1e-5 * max(abs(fd), 1e-300), (nsteps, name, ad[i], fd)
+
+
+def test_per_property_gradient(mods):
+    """Friction of the particle pairs alone (planes unchanged)."""
+    adjoint, sim = mods
+    sc = packed(seed=5)
+    w, u = weights(sc.np_, seed=12)
+    nsteps = 10
+    g, _, _ = adjoint_grads(mods, sc, nsteps, w, u)
+
+    def f(mu):
+        s2 = adjoint.with_parameters(sc, *P0)
+        s2.pp_cp.fric = mu
+        s = sim.Sim(s2, precision=T.XDEM_FP64)
+        s.step(nsteps)
+        out = lin_loss(s.state(), w, u)
+        s.close()
+        return out
+
+    h = 1e-6 * P0[0]
+    fd = (f(P0[0] + h) - f(P0[0] - h)) / (2 * h)
+    assert abs(g[0, 0] - fd) <= 1e-5 * abs(fd), (g[0, 0], fd)
+    assert abs(g[1:, 0].sum()) > 0  # the planes carry their own share
+
+
+def test_initial_state_gradient(mods):
+    adjoint, sim = mods
+    sc = packed(seed=7)
+    w, u = weights(sc.np_, seed=13)
+    nsteps = 15
+    _, x0, v0 = adjoint_grads(mods, sc, nsteps, w, u, initial=True)
+    x0 = x0.cpu().numpy()
+    v0 = v0.cpu().numpy()
+    rng = np.random.default_rng(1)
+    for i in rng.choice(sc.np_, 4, replace=False):
+        for c in range(3):
+            def f(dx, which):
+                s2 = adjoint.with_parameters(sc, *P0)
+                if which == "pos":
+                    s2.pos = s2.pos.copy()
+                    s2.pos[4 * i + c] += dx
+                else:
+                    s2.vel = s2.vel.copy()
+                    s2.vel[3 * i + c] += dx
+                s = sim.Sim(s2, precision=T.XDEM_FP64)
+                s.step(nsteps)
+                out = lin_loss(s.state(), w, u)
+                s.close()
+                return out
+
+            hx = 1e-10
+            fd = (f(hx, "pos") - f(-hx, "pos")) / (2 * hx)
+            assert abs(x0[i, c] - fd) <= 1e-4 * max(abs(fd), 1e-3), (i, c, x0[i, c], fd)
+            hv = 1e-8
+            fd = (f(hv, "vel") - f(-hv, "vel")) / (2 * hv)
+            assert abs(v0[i, c] - fd) <= 1e-4 * max(abs(fd), 1e-6), (i, c, v0[i, c], fd)
+
+
+def test_checkpoint_interval_does_not_change_the_gradient(mods):
+    sc = packed(seed=9)
+    w, u = weights(sc.np_, seed=14)
+    ref = None
+    for K in (1, 4, 23, 100):
+        g, x0, _ = adjoint_grads(mods, sc, 23, w, u, K=K, initial=True)
+        cur = (g, x0.cpu().numpy())
+        if ref is None:
+            ref = cur
+        else:
+            assert np.array_equal(ref[0], cur[0]), K
+            assert np.array_equal(ref[1], cur[1]), K
+
+
+def test_gradient_matches_oracle_finite_differences(mods, oracle):
+    """The FP64 reference gradient: central differences of the CPU oracle's
+    own trajectory (the restated reference step)."""
+    import kseq
+    adjoint, _ = mods
+    sc = packed(n=300, seed=15)
+    w, u = weights(sc.np_, seed=16)
+    nsteps = 8
+    g, _, _ = adjoint_grads(mods, sc, nsteps, w, u)
+    ad = [g[:, 0].sum(), g[:, 1].sum(), (g[:, 2] + g[:, 3]).sum()]
+    be = kseq.OracleBackend(oracle)
+
+    def f(p):
+        s2 = adjoint.with_parameters(sc, *p)
+        s = kseq.state_arrays(s2)
+        for _ in range(nsteps):
+            _, st, _ = kseq.sphere_step(be, s2, s, compat=0)
+            assert st == 0
+        return float((w * s["pos"].reshape(-1, 4)[:, :3]).sum() + (u * s["vel"].reshape(-1, 3)).sum())
+
+    for i, name in enumerate(("fric", "rest", "E")):
+        fd = central(f, P0, i)
+        assert abs(ad[i] - fd) <= 1e-5 * abs(fd), (name, ad[i], fd)
+
+
+def test_column_collapse_calibration_gradient(mods):
+    """The calibration loss (MSE of the radial height profile against the
+    profile of hidden parameters 0.35 / 0.45) through the autograd.Function,
+    against central differences of the same loss."""
+    adjoint, _ = mods
+    sc = scenes.column_collapse(n_target=3000, R=0.03, H=0.05, v0=0.5, seed=77)
+    nsteps, K = 300, 100
+    center, r_max = (0.0, 0.0), 0.04
+    dev = torch.device("cuda")
+
+    def profile(p, grad=False):
+        t = [torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=grad) for v in p]
+        pos = adjoint.trajectory(t[0], t[1], t[2], sc, nsteps, K)
+        return adjoint.radial_height_profile(pos, center, r_max), t
+
+    target, _ = profile((0.35, 0.45, 1e7))
+    target = target.detach()
+    prof, t = profile(P0, grad=True)
+    loss = ((prof - target) ** 2).mean()
+    loss.backward()
+    ad = [float(x.grad) for x in t]
+
+    def f(p):
+        pr, _ = profile(p)
+        return float(((pr - target) ** 2).mean())
+
+    for i, name in enumerate(("fric", "rest", "E")):
+        fd = central(f, P0, i, rel=1e-5)
+        assert abs(ad[i] - fd) <= 1e-3 * max(abs(fd), 1e-300), (name, ad[i], fd)

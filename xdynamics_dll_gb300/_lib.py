@@ -70,6 +70,11 @@ _SIGS = {
     "xdem_sim_set_profiling": ([vp, i32], i32),
     "xdem_sim_set_graph": ([vp, i32], i32),
     "xdem_sim_profile": ([vp, vp, vp, vp], i32),
+    "xdem_adj_create": ([vp, u32, vp], i32),
+    "xdem_adj_destroy": ([vp], i32),
+    "xdem_adj_forward": ([vp, u32], i32),
+    "xdem_adj_backward": ([vp] * 6, i32),
+    "xdem_adj_info": ([vp, vp, vp, vp], i32),
 }
 
 

@@ -30,6 +30,7 @@ UNITS = {
     "xdem_fused_fp64.cu": ["-fmad=false"],
     "xdem_fused_mixed.cu": ["-fmad=true"],
     "xdem_noalloc.cu": [],
+    "xdem_adjoint.cu": ["-fmad=false"],
 }
 
 

@@ -369,3 +369,50 @@ def wheel_mesh(radius=0.15, width=0.1, n_around=100, n_width=4):
             a = (*ring[j], z); b = (*ring[j + 1], z)
             tris.append((o, b, a) if sgn < 0 else (o, a, b))
     return np.array(tris, dtype=np.float64).reshape(-1, 9)
+
+
+def column_collapse(n_target=65536, r=1.5e-3, R=0.1, H=0.3, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3,
+                    dt=1e-5, seed=5150, v0=0.0, floor_half=0.5, jitter=0.1):
+    """Column collapse of the differentiable-calibration configuration:
+    about n_target spheres of radius r on a seeded jittered cubic lattice
+    (jitter +-jitter r) filling a vertical cylinder of radius R and height H
+    that stands on a floor plane (a 2 floor_half square at y = 0, normal +y);
+    no cylinder wall, so the column collapses once released.  The lattice
+    spacing is the largest (never below 2.2 r) that puts at least n_target
+    sites inside the cylinder; v0 is an optional initial downward speed."""
+    rng = np.random.default_rng(seed)
+
+    def layout(sp):
+        nxz = int(np.floor(2.0 * R / sp)) + 1
+        ny = max(1, int(np.floor((H - 2.0 * r) / sp)) + 1)
+        x0 = -0.5 * (nxz - 1) * sp
+        c = x0 + sp * np.arange(nxz)
+        inside = int(((c[:, None] ** 2 + c[None, :] ** 2) <= (R - r) ** 2).sum())
+        return nxz, ny, x0, inside * ny
+
+    sp = max(2.2 * r, (np.pi * R * R * H / n_target) ** (1.0 / 3.0))
+    while sp > 2.2 * r and layout(sp)[3] < n_target:
+        sp = max(2.2 * r, sp * 0.995)
+    nxz, ny, x0, _ = layout(sp)
+    pts = jittered_lattice(nxz, ny, nxz, sp, (x0, r + 0.5 * sp, x0), jitter * r, rng)
+    keep = pts[:, 0] ** 2 + pts[:, 2] ** 2 <= (R - r) ** 2
+    pts = pts[keep]
+    N = pts.shape[0]
+    pos = np.zeros((N, 4))
+    pos[:, :3] = pts
+    pos[:, 3] = r
+    m, J = sphere_mass_inertia(np.full(N, r), rho)
+    vel, acc, ep, ev, ea = _init_state(N)
+    vel[1::3] = -abs(v0)
+    cp = default_material(E, nu, rest, fric)
+    f = floor_half
+    planes = [T.plane_from_points(0, (-f, 0.0, -f), (-f, 0.0, f), (f, 0.0, -f))]
+    cs = 2.0 * r
+    extent = max(2.0 * (R + 0.05), H + 0.02)
+    g = pow2_at_least(int(np.ceil(extent / cs)))
+    grid = (g, g, g)
+    origin = (-0.5 * g * cs, -2.0 * cs, -0.5 * g * cs)
+    return Scene(np_=N, ns=N, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=m,
+                 inertia=J.ravel(), dt=dt, cell_size=cs, grid=grid, origin=origin, pp_cp=cp, planes=planes,
+                 plane_cp=[cp], plane_body=[T.body_record()], name="column_collapse",
+                 note=f"{N} spheres r={r} in a cylinder R={R} H={H}")
