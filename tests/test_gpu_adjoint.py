@@ -3,9 +3,12 @@ against central finite differences of the same GPU forward, against finite
 differences of the CPU oracle's trajectory (the FP64 reference gradient), and
 across checkpoint intervals.
 
-Finite differences use relative steps of 1e-6 on parameters that enter
-smoothly between contact-set changes; horizons are short enough that no
-contact opens, closes or changes regime (stick/slip) inside the step.
+Finite differences are central and Richardson-extrapolated from relative
+parameter steps h = 1e-7 and h/2: the trajectory is strongly curved in the
+parameters (a plain central quotient is off by up to 2e-3 at h = 1e-6 and
+2e-5 at h = 1e-7 after 8 to 25 steps, falling as h^2), and the horizons are
+short enough that no contact opens, closes or changes regime (stick/slip)
+within the step.
 """
 import numpy as np
 import pytest
@@ -63,13 +66,18 @@ def adjoint_grads(mods, sc, nsteps, w, u, params=P0, K=10, initial=False):
     return g, x0, v0
 
 
-def central(f, p, i, rel=1e-6):
+def central(f, p, i, rel=1e-7, richardson=True):
+    def d(h):
+        pp = list(p)
+        pm = list(p)
+        pp[i] += h
+        pm[i] -= h
+        return (f(pp) - f(pm)) / (2 * h)
+
     h = rel * abs(p[i])
-    pp = list(p)
-    pm = list(p)
-    pp[i] += h
-    pm[i] -= h
-    return (f(pp) - f(pm)) / (2 * h)
+    if not richardson:
+        return d(h)
+    return (4.0 * d(0.5 * h) - d(h)) / 3.0
 
 
 @pytest.mark.parametrize("nsteps", [1, 25])
@@ -101,8 +109,7 @@ def test_per_property_gradient(mods):
         s.close()
         return out
 
-    h = 1e-6 * P0[0]
-    fd = (f(P0[0] + h) - f(P0[0] - h)) / (2 * h)
+    fd = central(lambda p: f(p[0]), P0, 0)
     assert abs(g[0, 0] - fd) <= 1e-5 * abs(fd), (g[0, 0], fd)
     assert abs(g[1:, 0].sum()) > 0  # the planes carry their own share
 
@@ -115,6 +122,9 @@ def test_initial_state_gradient(mods):
     _, x0, v0 = adjoint_grads(mods, sc, nsteps, w, u, initial=True)
     x0 = x0.cpu().numpy()
     v0 = v0.cpu().numpy()
+    # small entries are judged against the typical entry: the difference
+    # quotient of a sum over all spheres carries rounding of that size
+    sx, sv = 1e-2 * np.abs(x0).max(), 1e-2 * np.abs(v0).max()
     rng = np.random.default_rng(1)
     for i in rng.choice(sc.np_, 4, replace=False):
         for c in range(3):
@@ -134,10 +144,10 @@ def test_initial_state_gradient(mods):
 
             hx = 1e-10
             fd = (f(hx, "pos") - f(-hx, "pos")) / (2 * hx)
-            assert abs(x0[i, c] - fd) <= 1e-4 * max(abs(fd), 1e-3), (i, c, x0[i, c], fd)
+            assert abs(x0[i, c] - fd) <= 1e-4 * max(abs(fd), sx), (i, c, x0[i, c], fd)
             hv = 1e-8
             fd = (f(hv, "vel") - f(-hv, "vel")) / (2 * hv)
-            assert abs(v0[i, c] - fd) <= 1e-4 * max(abs(fd), 1e-6), (i, c, v0[i, c], fd)
+            assert abs(v0[i, c] - fd) <= 1e-4 * max(abs(fd), sv), (i, c, v0[i, c], fd)
 
 
 def test_checkpoint_interval_does_not_change_the_gradient(mods):
@@ -206,5 +216,5 @@ def test_column_collapse_calibration_gradient(mods):
         return float(((pr - target) ** 2).mean())
 
     for i, name in enumerate(("fric", "rest", "E")):
-        fd = central(f, P0, i, rel=1e-5)
+        fd = central(f, P0, i, rel=1e-5, richardson=False)
         assert abs(ad[i] - fd) <= 1e-3 * max(abs(fd), 1e-300), (name, ad[i], fd)
