@@ -218,3 +218,43 @@ def test_column_collapse_calibration_gradient(mods):
     for i, name in enumerate(("fric", "rest", "E")):
         fd = central(f, P0, i, rel=1e-5, richardson=False)
         assert abs(ad[i] - fd) <= 1e-3 * max(abs(fd), 1e-300), (name, ad[i], fd)
+
+
+def test_full_calibration_scene_gradient(mods):
+    """The full calibration scene (66,099 spheres of radius 1.5 mm in a
+    0.1 x 0.3 m column) over 2,600 steps with checkpoints every 100: the
+    adjoint against central differences of the same loss.  Over this horizon
+    the layers fall and the lowest ones bounce off the floor with vertical
+    motion only, so friction has exactly zero influence on both sides and the
+    loss is smooth in restitution and E.  Later (about 3,000 steps on) the
+    layers collide with tangential slip and the loss turns discontinuous in
+    the parameters: the reference's normal damping term beta (v . n) makes
+    the contact force jump when a contact opens, so a parameter change that
+    moves an opening across a step boundary moves the loss by a finite
+    amount, and difference quotients grow like 1/h."""
+    adjoint, _ = mods
+    sc = scenes.column_collapse()
+    nsteps, K = 2600, 100
+    center, r_max = (0.0, 0.0), 0.15
+    dev = torch.device("cuda")
+
+    def profile(p, grad=False):
+        t = [torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=grad) for v in p]
+        pos = adjoint.trajectory(t[0], t[1], t[2], sc, nsteps, K)
+        return adjoint.radial_height_profile(pos, center, r_max), t
+
+    target, _ = profile((0.35, 0.45, 1e7))
+    target = target.detach()
+    prof, t = profile(P0, grad=True)
+    loss = ((prof - target) ** 2).mean()
+    loss.backward()
+    ad = [float(x.grad) for x in t]
+    assert ad[0] == 0.0 and ad[1] != 0.0 and ad[2] != 0.0
+
+    def f(p):
+        pr, _ = profile(p)
+        return float(((pr - target) ** 2).mean())
+
+    for i in (1, 2):
+        fd = central(f, P0, i, rel=1e-6, richardson=False)
+        assert abs(ad[i] - fd) <= 1e-3 * abs(fd), (i, ad[i], fd)
