@@ -114,6 +114,7 @@ class Batch:
         L = self.sim.L
         _lib.check(L.xdem_sim_set_scenes(self.sim.h, n, self.first.ctypes.data_as(C.c_void_p), cps,
                                          self.plane_first.ctypes.data_as(C.c_void_p)), "xdem_sim_set_scenes")
+        self.sim.nscene = n
 
     def scene_alone(self, k):
         """Scene k on its own, on a grid whose cells line up with its cells
@@ -131,6 +132,12 @@ class Batch:
 
     def set_graph(self, on):
         self.sim.set_graph(on)
+
+    def autotune(self, trial_steps=10, cache=None):
+        """Block shapes for this batch from the autotuner (or from `cache`,
+        a JSON file of earlier choices); see xdynamics_dll_gb300.autotune."""
+        from .autotune import tune
+        return tune(self.sim, trial_steps=trial_steps, cache=cache)
 
     def energies(self):
         """Kinetic energy and stored contacts (particle and plane) of every scene."""

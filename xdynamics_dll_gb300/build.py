@@ -31,6 +31,7 @@ UNITS = {
     "xdem_fused_mixed.cu": ["-fmad=true"],
     "xdem_noalloc.cu": [],
     "xdem_adjoint.cu": ["-fmad=false"],
+    "xdem_tune.cu": [],
 }
 
 

@@ -67,7 +67,16 @@ struct MatF {
     int coh;
 };
 
+// Block shapes of the mixed contact stage, chosen by the autotuner
+// (xdem_sim_autotune): threads per block of the pair kernel and of the body
+// kernel (64, 128 or 256) and the pair kernel's candidate-stage depth (8 or
+// 16 entries a thread).  Results do not depend on them.
+struct MixedTune {
+    unsigned int nt_pairs = 128, stage = 16, nt_bodies = 128;
+};
+
 struct FusedState {
+    MixedTune tune;
     bool mixed = false;
     bool primed = false;       // next positions + keys hold the next step's input
     bool have_prev = false;    // skey_prev lists the occupied cells of the last step
@@ -177,6 +186,7 @@ int fused_energy(FusedState& fs, const double* vel, const double* ep, const doub
 // Contact kernels (one translation unit per arithmetic type).
 struct ContactLaunch {
     device_dem_parameters prm;
+    MixedTune tune;
     unsigned int np, nentry;
     int vel_compat;
     bool rolling;

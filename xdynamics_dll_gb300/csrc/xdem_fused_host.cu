@@ -565,7 +565,12 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.pl_count = a.pl_count; c.pl_id = a.pl_id; c.pl_tsd = a.pl_tsd;
     c.tri = a.tri; c.ms_count = a.ms_count; c.ms_id = a.ms_id; c.ms_tsd = a.ms_tsd;
     c.body = a.body; c.mp = a.mp;
-    c.nblocks = (n + kFusedThreads - 1) / kFusedThreads;
+    // body wrench partials: one row entry per block of the emitting kernel
+    // (the mixed pair and body kernels share their block size whenever the
+    // handle keeps wrenches)
+    c.tune = fs.tune;
+    const unsigned int nt_emit = fs.mixed ? fs.tune.nt_bodies : (unsigned int)kFusedThreads;
+    c.nblocks = (n + nt_emit - 1) / nt_emit;
     c.bsums = a.bsums;
     c.status = a.status;
     c.nscene = a.nscene ? a.nscene : 1;

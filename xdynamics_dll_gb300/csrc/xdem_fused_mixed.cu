@@ -206,13 +206,14 @@ struct Acc {
 //     carry their low parts), so the overlap -- which can be 1e-6 of the
 //     radius -- keeps ~1e-16 m resolution and the contact test classifies as
 //     the FP64 form does; then the contact force.
-// The stage holds kStage entries per thread in shared memory; when more pass
-// the screen, the walk is repeated for the rest, in the same order.  Entries
+// The stage holds STAGE entries per thread in shared memory (a tuning
+// parameter, as is the block size NT: shared arrays are laid out
+// [slot][thread] with stride NT); when more pass the screen, the walk is
+// repeated for the rest, in the same order.  Entries
 // whose packed unwrapped cell is not one of the stencil's are aliases of the
 // wrapping hash and are skipped.
-constexpr unsigned int kStage = 16;
-
 // Pass 2 for one staged candidate at sorted position j.
+template <unsigned int NT>
 __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oid, unsigned int j, unsigned int ux,
                                          unsigned int uy, unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
                                          unsigned int sid, unsigned int old_count, const unsigned int* old_id,
@@ -267,7 +268,7 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
     // old list, the matching history from global memory
     float sd0 = 0.f, sd1 = 0.f;
     for (unsigned int q = 0; q < old_count; ++q)
-        if (old_id[q * kFusedThreads] == k) {
+        if (old_id[q * NT] == k) {
             const double2 t = reinterpret_cast<const double2*>(c.pp_tsd_old)[sid + q];
             sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
             break;
@@ -304,6 +305,7 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
     }
 }
 
+template <unsigned int NT, unsigned int STAGE>
 __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int oid, unsigned int gx,
                                           unsigned int gy, unsigned int gz, float4 Ai, float4 Li, unsigned int Ti,
                                           float4 Bi, float4 Ci, unsigned int* stage, unsigned int* old_id,
@@ -319,7 +321,7 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
     unsigned int old_count = c.pp_count_old[oid];
     if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
     // the old partner ids travel to shared memory while the stencil is walked
-    for (unsigned int q = 0; q < old_count; ++q) cp_async4(old_id + q * kFusedThreads, c.pp_id_old + sid + q);
+    for (unsigned int q = 0; q < old_count; ++q) cp_async4(old_id + q * NT, c.pp_id_old + sid + q);
     cp_async_commit();
     V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
     unsigned int cnt = 0, done = 0;
@@ -381,11 +383,11 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                             if (!(dx * dx + dy * dy + dz * dz < rr * rr * screen)) continue;
                         }
                         if (seen++ < done) continue;
-                        if (nc == kStage) {
+                        if (nc == STAGE) {
                             more = true;
                             break;
                         }
-                        stage[nc++ * kFusedThreads] = j;
+                        stage[nc++ * NT] = j;
                     }
                 }
             }
@@ -399,7 +401,7 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
         cp_async_wait_all();
         // ---- pass 2: float-pair overlap and contact force, in walk order
         for (unsigned int q = 0; q < nc; ++q)
-            p2p_pair(c, oid, stage[q * kFusedThreads], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
+            p2p_pair<NT>(c, oid, stage[q * NT], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
                      coh, Ft, Fn, cnt, acc, bits);
     }
     c.pp_count_new[oid] = cnt;
@@ -829,12 +831,13 @@ __device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned in
 // the sphere's force, moment and rolling sums (original order) for kernel 2.
 // It holds no plane or integration state, so it runs at twice the occupancy
 // of a kernel doing all of it -- the stencil walk is latency-bound.
-template <bool MESH>
-__global__ void __launch_bounds__(kFusedThreads, 6) k_mixed_pairs(const __grid_constant__ ContactLaunch c)
+// NT threads per block with 768 / NT blocks per SM (80 registers a thread).
+template <bool MESH, unsigned int NT, unsigned int STAGE>
+__global__ void __launch_bounds__(NT, 768 / NT) k_mixed_pairs(const __grid_constant__ ContactLaunch c)
 {
-    __shared__ float smf[(kFusedThreads / 32) * 6 * 2];
-    __shared__ unsigned int stage[kStage * kFusedThreads];  // p2p candidates, [slot][thread]
-    __shared__ unsigned int old_id[MAX_P2P_COUNT * kFusedThreads];  // old pair list, [slot][thread]
+    __shared__ float smf[(NT / 32) * 6 * 2];
+    __shared__ unsigned int stage[STAGE * NT];                // p2p candidates, [slot][thread]
+    __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned int oid = 0xffffffffu;
     if (s < c.nentry) oid = c.sorted_index[s];
@@ -865,7 +868,8 @@ __global__ void __launch_bounds__(kFusedThreads, 6) k_mixed_pairs(const __grid_c
 
     // ------------------------------------------------ particle-particle (impl:613-733)
     if (live && c.has_pp)
-        p2p_mixed(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc, bits);
+        p2p_mixed<NT, STAGE>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
+                             bits);
 
     // ------------------------------------------------ triangle meshes (impl:1930-2109)
     if (MESH) {
@@ -889,9 +893,10 @@ __global__ void __launch_bounds__(kFusedThreads, 6) k_mixed_pairs(const __grid_c
 // every state array is read and written coalesced.  Plane contact (planes in
 // id order), rolling resistance, the velocity and position update and the
 // next step's records, on top of kernel 1's particle-particle sums.
-__global__ void __launch_bounds__(kFusedThreads, 4) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
+template <unsigned int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
 {
-    __shared__ float smf[(kFusedThreads / 32) * 6 * 2];
+    __shared__ float smf[(NT / 32) * 6 * 2];
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = oid < c.np;
     float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
@@ -986,22 +991,50 @@ __global__ void __launch_bounds__(kFusedThreads, 4) k_mixed_bodies(const __grid_
     mixed_tail(c, oid, ip, Ai, Li, Bi, Ff, Mf, bits);
 }
 
+template <bool MESH, unsigned int NT, unsigned int STAGE>
+cudaError_t launch_pairs(const ContactLaunch& c, cudaStream_t st)
+{
+    k_mixed_pairs<MESH, NT, STAGE><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
+    return cudaGetLastError();
+}
+template <bool MESH, unsigned int NT>
+cudaError_t launch_pairs_stage(const ContactLaunch& c, cudaStream_t st)
+{
+    return c.tune.stage == 8 ? launch_pairs<MESH, NT, 8>(c, st) : launch_pairs<MESH, NT, 16>(c, st);
+}
+template <bool MESH>
+cudaError_t launch_pairs_nt(const ContactLaunch& c, cudaStream_t st)
+{
+    switch (c.tune.nt_pairs) {
+    case 64: return launch_pairs_stage<MESH, 64>(c, st);
+    case 256: return launch_pairs_stage<MESH, 256>(c, st);
+    default: return launch_pairs_stage<MESH, 128>(c, st);
+    }
+}
+template <unsigned int NT>
+cudaError_t launch_bodies(const ContactLaunch& c, cudaStream_t st)
+{
+    k_mixed_bodies<NT><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
-// Both kernels use nblocks = ceil(nentry / 128) blocks, so each body's
-// wrench partials fill one [nblocks] row whichever kernel writes them.
+// The block shapes come from c.tune (the autotuner's choice; 128 / 16 / 128
+// by default).  Body wrench partials are written per block by the kernel
+// that owns the body (meshes: pairs, planes: bodies) into rows of c.nblocks
+// entries, so a handle that keeps wrenches runs both kernels with the same
+// block size (tune_valid) and c.nblocks = ceil(nentry / that size).
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
 {
     if (c.nentry == 0) return cudaSuccess;
-    const unsigned int nb = (c.nentry + kFusedThreads - 1) / kFusedThreads;
-    if (c.nmesh)
-        k_mixed_pairs<true><<<nb, kFusedThreads, 0, st>>>(c);
-    else
-        k_mixed_pairs<false><<<nb, kFusedThreads, 0, st>>>(c);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = c.nmesh ? launch_pairs_nt<true>(c, st) : launch_pairs_nt<false>(c, st);
     if (e != cudaSuccess) return e;
-    k_mixed_bodies<<<nb, kFusedThreads, 0, st>>>(c);
-    return cudaGetLastError();
+    switch (c.tune.nt_bodies) {
+    case 64: return launch_bodies<64>(c, st);
+    case 256: return launch_bodies<256>(c, st);
+    default: return launch_bodies<128>(c, st);
+    }
 }
 
 }  // namespace xdem

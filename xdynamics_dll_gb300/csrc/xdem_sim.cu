@@ -120,7 +120,8 @@ int ensure_tables(xdem_sim* s)
     A(s->k0, s->nentry); A(s->v0, s->nentry); A(s->k1, s->nentry); A(s->v1, s->nentry);
     A(s->hist, radix_hist_size(s->nentry));
     A(s->sorted_index, s->nentry);
-    const unsigned int nb = blocks_for(s->nentry);
+    // partial rows sized for the smallest block shape the tuner may pick
+    const unsigned int nb = blocks_for(s->nentry, 64);
     const size_t nbody = std::max<size_t>(s->bodies.size(), 1);
     // batched handles keep no body wrenches: no per-block partials
     A(s->bsums, (size_t)nb * 6 * (s->nscene > 1 ? 1 : nbody));

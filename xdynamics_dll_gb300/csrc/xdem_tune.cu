@@ -1,0 +1,160 @@
+// xdem_tune.cu -- block-shape autotuner of the mixed contact stage.
+//
+// xdem_sim_autotune times every candidate shape of the two mixed contact
+// kernels (threads per block of the pair and body kernels, depth of the pair
+// kernel's candidate stage) on the handle's own scene, with CUDA events
+// around the contact stage, and keeps the fastest.  Each candidate starts
+// from the same saved state, and the state is put back at the end, so
+// tuning does not advance the simulation.  The shapes do not change results:
+// every sphere's arithmetic is the same whatever block it runs in.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "xdem_sim_impl.h"
+
+namespace {
+
+// A device copy of everything a step reads and writes.
+struct Snapshot {
+    std::vector<std::pair<void*, size_t>> bufs;  // (copy, bytes)
+    std::vector<void**> live;                     // the handle fields copied, in order
+    cudaError_t take(xdem_sim* s)
+    {
+        const size_t n = s->np, ns = s->ns;
+        const size_t bytes[] = {n * 32, ns * 24, ns * 24, ns * 32, ns * 32, ns * 32,
+                                n * 4, n * MAX_P2P_COUNT * 4, n * MAX_P2P_COUNT * 16,
+                                n * 4, n * MAX_P2PL_COUNT * 4, n * MAX_P2PL_COUNT * 16,
+                                n * 4, n * MAX_P2MS_COUNT * 4, n * MAX_P2MS_COUNT * 16};
+        void** fields[] = {reinterpret_cast<void**>(&s->pos), reinterpret_cast<void**>(&s->vel),
+                           reinterpret_cast<void**>(&s->acc), reinterpret_cast<void**>(&s->ep),
+                           reinterpret_cast<void**>(&s->ev), reinterpret_cast<void**>(&s->ea),
+                           reinterpret_cast<void**>(&s->pp_count), reinterpret_cast<void**>(&s->pp_id),
+                           reinterpret_cast<void**>(&s->pp_tsd), reinterpret_cast<void**>(&s->pl_count),
+                           reinterpret_cast<void**>(&s->pl_id), reinterpret_cast<void**>(&s->pl_tsd),
+                           reinterpret_cast<void**>(&s->ms_count), reinterpret_cast<void**>(&s->ms_id),
+                           reinterpret_cast<void**>(&s->ms_tsd)};
+        for (size_t i = 0; i < sizeof(bytes) / sizeof(bytes[0]); ++i) {
+            if (!*fields[i]) continue;
+            void* c = nullptr;
+            cudaError_t e = cudaMalloc(&c, bytes[i]);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(c, *fields[i], bytes[i], cudaMemcpyDeviceToDevice, s->st);
+            if (e != cudaSuccess) {
+                if (c) cudaFree(c);
+                return e;
+            }
+            bufs.push_back({c, bytes[i]});
+            live.push_back(fields[i]);
+        }
+        return cudaStreamSynchronize(s->st);
+    }
+    // copies back into whatever buffers the handle's fields point to now
+    cudaError_t put(xdem_sim* s) const
+    {
+        cudaError_t e = cudaSuccess;
+        for (size_t i = 0; i < bufs.size() && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(*live[i], bufs[i].first, bufs[i].second, cudaMemcpyDeviceToDevice, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        fused_invalidate(s->fs);
+        return e;
+    }
+    ~Snapshot()
+    {
+        for (auto& b : bufs) cudaFree(b.first);
+    }
+};
+
+bool shape_ok(unsigned int nt) { return nt == 64 || nt == 128 || nt == 256; }
+
+// Body wrench partials need one block size for both kernels.
+bool keeps_wrenches(const xdem_sim* s) { return s->nscene == 1 && !s->bodies.empty(); }
+
+}  // namespace
+
+XDEM_API int xdem_sim_set_tune(xdem_sim* s, const xdem_tune* t)
+{
+    if (!s || !t) return XDEM_ERR_ARG;
+    if (!shape_ok(t->nt_pairs) || !shape_ok(t->nt_bodies) || (t->stage != 8 && t->stage != 16)) return XDEM_ERR_ARG;
+    if (keeps_wrenches(s) && t->nt_pairs != t->nt_bodies) return XDEM_ERR_ARG;
+    s->fs.tune.nt_pairs = t->nt_pairs;
+    s->fs.tune.stage = t->stage;
+    s->fs.tune.nt_bodies = t->nt_bodies;
+    fused_invalidate(s->fs);  // the captured step graphs bake in the shapes
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_get_tune(xdem_sim* s, xdem_tune* t)
+{
+    if (!s || !t) return XDEM_ERR_ARG;
+    t->nt_pairs = s->fs.tune.nt_pairs;
+    t->stage = s->fs.tune.stage;
+    t->nt_bodies = s->fs.tune.nt_bodies;
+    t->contact_ms = 0.0;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_autotune(xdem_sim* s, unsigned int trial_steps, xdem_tune* best, xdem_tune* all,
+                               unsigned int* nall)
+{
+    if (!s || !best || trial_steps == 0) return XDEM_ERR_ARG;
+    // only the mixed fused step has shapes to choose
+    if (!s->precision_mixed() || s->cfg.launcher_path || s->clusters) {
+        xdem_sim_get_tune(s, best);
+        if (nall) *nall = 0;
+        return XDEM_OK;
+    }
+    if (int r = xdem_sim_step(s, 0)) return r;  // tables exist before the snapshot
+    // status bits raised by the caller's own steps survive the trials
+    const int pending = xdem_sim_status(s);
+    if (pending & XDEM_ERR_CUDA) return XDEM_ERR_CUDA;
+    Snapshot snap;
+    if (cudaError_t e = snap.take(s)) {
+        fprintf(stderr, "xdem_sim_autotune: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+        return XDEM_ERR_ALLOC;
+    }
+    std::vector<xdem_tune> cand;
+    const unsigned int nts[3] = {64, 128, 256}, stages[2] = {8, 16};
+    for (unsigned int a : nts)
+        for (unsigned int st : stages)
+            for (unsigned int b : nts) {
+                if (keeps_wrenches(s) && a != b) continue;
+                cand.push_back(xdem_tune{a, st, b, 0.0});
+            }
+    const MixedTune keep = s->fs.tune;
+    const bool prof = s->profiling;
+    int r = XDEM_OK;
+    xdem_tune win = {keep.nt_pairs, keep.stage, keep.nt_bodies, 1e300};
+    for (size_t i = 0; i < cand.size() && r == XDEM_OK; ++i) {
+        if (snap.put(s) != cudaSuccess) { r = XDEM_ERR_CUDA; break; }
+        s->fs.tune = MixedTune{cand[i].nt_pairs, cand[i].stage, cand[i].nt_bodies};
+        s->profiling = false;
+        if ((r = xdem_sim_step(s, 2)) != XDEM_OK) break;  // warm-up (priming, caches)
+        s->profiling = true;
+        if ((r = xdem_sim_step(s, trial_steps)) != XDEM_OK) break;
+        const unsigned int nrec = s->prof_contact_launches;
+        cand[i].contact_ms = nrec ? s->prof_ms / nrec : 0.0;
+        if (nrec && cand[i].contact_ms < win.contact_ms) win = cand[i];
+    }
+    s->profiling = prof;
+    if (snap.put(s) != cudaSuccess && r == XDEM_OK) r = XDEM_ERR_CUDA;
+    xdem_sim_status(s);  // the trials' bits belong to no user step
+    if (pending) {
+        const unsigned int h = (unsigned int)pending;
+        if (cudaMemcpy(s->d_status, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess && r == XDEM_OK)
+            r = XDEM_ERR_CUDA;
+    }
+    if (r != XDEM_OK) {
+        s->fs.tune = keep;
+        return r;
+    }
+    s->fs.tune = MixedTune{win.nt_pairs, win.stage, win.nt_bodies};
+    *best = win;
+    if (all && nall) {
+        const unsigned int n = std::min<unsigned int>(*nall, (unsigned int)cand.size());
+        for (unsigned int i = 0; i < n; ++i) all[i] = cand[i];
+    }
+    if (nall) *nall = (unsigned int)cand.size();
+    return XDEM_OK;
+}

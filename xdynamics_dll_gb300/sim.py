@@ -141,6 +141,26 @@ class Sim:
         """Replay the step from a captured CUDA graph (identical results)."""
         _lib.check(self.L.xdem_sim_set_graph(self.h, int(on)), "xdem_sim_set_graph")
 
+    def set_tune(self, nt_pairs=128, stage=16, nt_bodies=128):
+        """Block shapes of the mixed contact stage (results do not depend on them)."""
+        t = T.Tune(nt_pairs, stage, nt_bodies, 0.0)
+        _lib.check(self.L.xdem_sim_set_tune(self.h, C.byref(t)), "xdem_sim_set_tune")
+
+    def get_tune(self):
+        t = T.Tune()
+        _lib.check(self.L.xdem_sim_get_tune(self.h, C.byref(t)), "xdem_sim_get_tune")
+        return t.as_dict()
+
+    def autotune(self, trial_steps=10):
+        """Times every candidate shape on this scene (state restored after),
+        keeps the fastest; returns (best, all candidates) as dicts."""
+        best = T.Tune()
+        cap = C.c_uint(64)
+        allv = (T.Tune * 64)()
+        _lib.check(self.L.xdem_sim_autotune(self.h, int(trial_steps), C.byref(best), allv, C.byref(cap)),
+                   "xdem_sim_autotune")
+        return best.as_dict(), [allv[i].as_dict() for i in range(cap.value)]
+
     def profile(self):
         nl = C.c_uint()
         ms = C.c_double()

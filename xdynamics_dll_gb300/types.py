@@ -90,6 +90,14 @@ class ClusterInformation(C.Structure):
     _fields_ = [("sid", C.c_uint), ("scid", C.c_uint), ("count", C.c_uint), ("neach", C.c_uint)]
 
 
+class Tune(C.Structure):
+    """xdem_tune (include/xdem_c.h): block shapes of the mixed contact stage."""
+    _fields_ = [("nt_pairs", C.c_uint), ("stage", C.c_uint), ("nt_bodies", C.c_uint), ("contact_ms", C.c_double)]
+
+    def as_dict(self):
+        return dict(nt_pairs=self.nt_pairs, stage=self.stage, nt_bodies=self.nt_bodies, contact_ms=self.contact_ms)
+
+
 class SimConfig(C.Structure):
     """xdem_sim_config (include/xdem_c.h)."""
     _fields_ = [
