@@ -271,6 +271,130 @@ def bench_e2e(sm, scene, torch, steps):
             "steps": steps}
 
 
+def bench_sweep(args, torch, local):
+    """The batched parameter sweep: 256 sphere drops with particle counts
+    U{2000..60000}, radii U[1, 3] mm, friction U[0.1, 0.6], restitution
+    U[0.2, 0.8] (seeded), advanced together by one handle in the mixed form:
+    one graph launch per step covers every scene.  Block shapes come from
+    the autotuner.  Also times the same scenes stepped one handle after
+    another (each with its own graph) over a few steps, and the batch in
+    FP64."""
+    from xdynamics_dll_gb300 import batch, types as T
+
+    def stage(msg):
+        sys.stderr.write(f"[sweep] {msg}\n")
+        sys.stderr.flush()
+
+    nsc = args.scenes
+    members = batch.sweep(nsc, seed=404)
+    t0 = time.perf_counter()
+    b = batch.Batch(members, precision=T.XDEM_MIXED)
+    setup_s = time.perf_counter() - t0
+    stage(f"batch of {nsc} scenes, {b.combined.np_} spheres, grid {b.combined.grid}: {setup_s:.1f} s")
+    tune, _ = b.autotune(trial_steps=10)
+    stage(f"autotune: {tune['nt_pairs']}/{tune['stage']}/{tune['nt_bodies']}")
+    stream = torch.cuda.Stream(device=local)
+    b.sim.L.xdem_sim_set_stream(b.sim.h, stream.cuda_stream)
+    b.set_graph(True)
+    warmup = max(3, args.warmup)
+    b.step(warmup)
+    sampler = ClockSampler(local)
+    with sampler:
+        secs = time_device(b.sim, torch, args.steps, stream)
+    launches, _, _ = b.sim.profile()
+    ke, nc = b.energies()
+    st = b.status()
+    n = b.combined.np_
+    b.close()
+    stage("mixed batch timed")
+    # FP64 batch, same scenes
+    b64 = batch.Batch(members, precision=T.XDEM_FP64)
+    s64 = torch.cuda.Stream(device=local)
+    b64.sim.L.xdem_sim_set_stream(b64.sim.h, s64.cuda_stream)
+    b64.set_graph(True)
+    b64.step(warmup)
+    k64 = max(1, args.steps // 5)
+    secs64 = time_device(b64.sim, torch, k64, s64)
+    b64.close()
+    stage("fp64 batch timed")
+    # the same scenes as separate handles, one after another
+    from xdynamics_dll_gb300 import sim as S
+    ksep = max(1, min(args.steps, 20))
+    sims = []
+    for m in members:
+        sm = S.Sim(m, precision=T.XDEM_MIXED)
+        sm.L.xdem_sim_set_stream(sm.h, stream.cuda_stream)
+        sm.set_graph(True)
+        sm.step(warmup)
+        sims.append(sm)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(ksep):
+        for sm in sims:
+            sm.step(1)
+    end.record(stream)
+    end.synchronize()
+    secs_sep = start.elapsed_time(end) / 1e3
+    for sm in sims:
+        sm.close()
+    stage("separate handles timed")
+    counts = [m.np_ for m in members]
+    out = {
+        "metric": "particle-steps/s, batched parameter sweep", "value": n * args.steps / secs, "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 contact / f64 state (mixed)",
+        "data": "synthetic",
+        "config": {"workload": f"batched sweep, {nsc} sphere-drop scenes, {n} spheres in all "
+                               f"(per scene {min(counts)}..{max(counts)}), r~U[1,3] mm, fric~U[0.1,0.6], "
+                               f"rest~U[0.2,0.8], dt=1e-5 s", "grid": list(b.combined.grid),
+                   "l2": "inputs larger than L2, no flush"},
+        "autotune": {k: tune[k] for k in ("nt_pairs", "stage", "nt_bodies", "contact_ms")},
+        "graph_launches_per_step": 1, "gpu_launches": launches,
+        "fp64": {"value": n * k64 / secs64, "ms_per_step": 1e3 * secs64 / k64},
+        "separate_handles": {"value": n * ksep / secs_sep, "ms_per_step": 1e3 * secs_sep / ksep, "steps": ksep,
+                             "handles": nsc},
+        "setup_s": setup_s, "contacts_per_sphere": float(nc.sum()) / n, "status": st,
+        "clocks": sampler.summary(),
+    }
+    print(json.dumps(out))
+
+
+def bench_calibration(args, torch, local):
+    """The differentiable calibration: column collapse of 66,099 spheres
+    (r 1.5 mm, 0.1 x 0.3 m column), 4,000 FP64 steps with checkpoints every
+    100, radial-height-profile loss; times the forward (with checkpoints)
+    and the backward (re-run plus reverse) of the adjoint."""
+    from xdynamics_dll_gb300 import adjoint, scenes
+    sc = scenes.column_collapse()
+    nsteps, K = args.steps, 100
+    dev = torch.device("cuda", local)
+    center, r_max = (0.0, 0.0), 0.15
+    with torch.no_grad():
+        tgt = adjoint.radial_height_profile(
+            adjoint.trajectory(*[torch.tensor(v, dtype=torch.float64, device=dev) for v in (0.35, 0.45, 1e7)],
+                               sc, nsteps, K), center, r_max)
+    p = [torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=True) for v in (0.3, 0.5, 1e7)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pos = adjoint.trajectory(*p, sc, nsteps, K)
+    loss = ((adjoint.radial_height_profile(pos, center, r_max) - tgt) ** 2).mean()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    loss.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    out = {
+        "metric": "particle-steps/s of forward + adjoint, differentiable calibration",
+        "value": sc.np_ * nsteps / (t2 - t0), "unit": UNIT, "n_gpus": 1, "steps": nsteps, "warmup": 0,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"column collapse, {sc.np_} spheres r=1.5 mm, checkpoint every {K} steps"},
+        "forward_s": t1 - t0, "backward_s": t2 - t1, "loss": loss.item(),
+        "grad": {"fric": float(p[0].grad), "rest": float(p[1].grad), "E": float(p[2].grad)},
+    }
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -279,6 +403,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--workload", default="dambreak", choices=["dambreak", "sweep", "calibration"],
+                    help="dambreak: the headline line; sweep: the batched 256-scene parameter sweep; "
+                         "calibration: forward + adjoint of the column collapse")
+    ap.add_argument("--scenes", type=int, default=256, help="scenes of the sweep workload")
     ap.add_argument("--settle", type=int, default=0,
                     help="untimed GPU settling steps behind a gate before timing (0: time the deterministic "
                          "initial packing, the same input the reference arm times)")
@@ -286,6 +414,11 @@ def main():
     ws, rank, local = dist_env()
     warmup = max(3, args.warmup)
 
+    if args.impl == "reference" and args.workload != "dambreak":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm covers the dam-break "
+                              "workload only (no batching and no adjoint in the reference)"}))
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -311,6 +444,14 @@ def main():
     torch.cuda.set_device(local)
     from xdynamics_dll_gb300 import build, types as T
     build.build()
+    if args.workload == "sweep":
+        if rank == 0:
+            bench_sweep(args, torch, local)
+        return
+    if args.workload == "calibration":
+        if rank == 0:
+            bench_calibration(args, torch, local)
+        return
     scene = make_scene(args.n)
     if args.settle:
         scene = settle(scene, args.settle, torch)

@@ -399,7 +399,9 @@ XDEM_API int xdem_sim_set_pairs(xdem_sim* sim, int kind,
 XDEM_API int xdem_sim_energy(xdem_sim* sim, double* ke, unsigned int* ncontact);
 /* Status bits accumulated since the last call. */
 XDEM_API int xdem_sim_status(xdem_sim* sim);
-/* Stream the handle's kernels run on (cudaStream_t). */
+/* Stream the handle's kernels run on (cudaStream_t).  The stream stays the
+ * caller's: keep it alive while the handle uses it; xdem_sim_destroy never
+ * destroys it.  NULL returns to the handle's own stream. */
 XDEM_API int xdem_sim_set_stream(xdem_sim* sim, void* stream);
 /* Kernel timing of the last xdem_sim_step call: number of launches and the
  * time of the particle-particle contact kernel, in milliseconds, from CUDA

@@ -141,3 +141,25 @@ def test_cluster_handle_matches_oracle(simmod, oracle):
             assert np.abs(st[k] - s[k]).max() <= 1e-11 * scale, (step, k)
         cnt, ids, _ = sm.pairs(0)
         assert kseq.pairs_equal(cnt, ids, s["pp_count"], s["pp_id"], 12) == sc.np_
+
+
+def test_caller_stream_survives_the_handle(simmod):
+    """A stream given with xdem_sim_set_stream stays the caller's: destroying
+    the handle must leave it usable for the next handle."""
+    import torch
+    from xdynamics_dll_gb300 import scenes
+    sc = scenes.sphere_drop(n_per_layer_side=12, layers=2)
+    stream = torch.cuda.Stream()
+    ref = None
+    for _ in range(2):
+        s = simmod.Sim(sc, precision=T.XDEM_MIXED)
+        s.L.xdem_sim_set_stream(s.h, stream.cuda_stream)
+        s.set_graph(True)
+        s.step(12)
+        st = s.state()
+        s.close()
+        if ref is None:
+            ref = st
+        else:
+            assert np.array_equal(ref["pos"], st["pos"])
+    stream.synchronize()

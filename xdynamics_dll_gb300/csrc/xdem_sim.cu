@@ -432,7 +432,8 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
     s->mp_cap = 65;
     s->body_cap = 64;
     if (s->clusters) A(s->cpos, ns * 4);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->own_st, cudaStreamNonBlocking);
+    s->st = s->own_st;
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     // zero everything that carries over between steps
@@ -479,7 +480,8 @@ XDEM_API int xdem_sim_destroy(xdem_sim* s)
         if (s->pe0[i]) cudaEventDestroy(s->pe0[i]);
         if (s->pe1[i]) cudaEventDestroy(s->pe1[i]);
     }
-    if (s->st) cudaStreamDestroy(s->st);
+    // a stream given by xdem_sim_set_stream belongs to the caller
+    if (s->own_st) cudaStreamDestroy(s->own_st);
     delete s;
     return XDEM_OK;
 }
@@ -488,7 +490,8 @@ XDEM_API int xdem_sim_set_stream(xdem_sim* s, void* stream)
 {
     if (!s) return XDEM_ERR_ARG;
     cudaStreamSynchronize(s->st);
-    s->st = reinterpret_cast<cudaStream_t>(stream);
+    // NULL returns to the handle's own stream
+    s->st = stream ? reinterpret_cast<cudaStream_t>(stream) : s->own_st;
     return XDEM_OK;
 }
 

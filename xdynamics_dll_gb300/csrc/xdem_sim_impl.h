@@ -31,7 +31,8 @@ struct SimMesh {
 struct xdem_sim {
     xdem_sim_config cfg{};
     device_dem_parameters prm{};
-    cudaStream_t st = 0;
+    cudaStream_t st = 0;       // the stream steps run on (the handle's own or the caller's)
+    cudaStream_t own_st = 0;   // created with the handle; the only stream destroy releases
     unsigned int np = 0, ns = 0, nco = 0, nrloc = 0;
     bool clusters = false;
     unsigned int status_host = 0;
