@@ -224,6 +224,8 @@ def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None):
     sm = new_sim(scene, precision)
     stream = torch.cuda.Stream(device=dev)
     sm.L.xdem_sim_set_stream(sm.h, stream.cuda_stream)
+    # block shapes from the autotuner (mixed form; the state is put back)
+    tune, _ = sm.autotune(trial_steps=10)
     sm.set_graph(True)
     sm.step(warmup)
     torch.cuda.synchronize()
@@ -240,7 +242,7 @@ def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None):
     sm.set_profiling(False)
     st = sm.status()
     return sm, stream, {"secs": secs, "launches": launches, "contact_ms": contact_ms / max(contact_n, 1),
-                        "contact_launches": contact_n, "ncontact": ncontact, "ke": ke, "status": st}
+                        "contact_launches": contact_n, "ncontact": ncontact, "ke": ke, "status": st, "tune": tune}
 
 
 def bench_e2e(sm, scene, torch, steps):
@@ -292,7 +294,7 @@ def bench_sweep(args, torch, local):
     setup_s = time.perf_counter() - t0
     stage(f"batch of {nsc} scenes, {b.combined.np_} spheres, grid {b.combined.grid}: {setup_s:.1f} s")
     tune, _ = b.autotune(trial_steps=10)
-    stage(f"autotune: {tune['nt_pairs']}/{tune['stage']}/{tune['nt_bodies']}")
+    stage("autotune: " + "/".join(str(tune[k]) for k in ("nt_pairs", "stage", "occ_pairs", "nt_bodies", "occ_bodies")))
     stream = torch.cuda.Stream(device=local)
     b.sim.L.xdem_sim_set_stream(b.sim.h, stream.cuda_stream)
     b.set_graph(True)
@@ -349,7 +351,7 @@ def bench_sweep(args, torch, local):
                                f"(per scene {min(counts)}..{max(counts)}), r~U[1,3] mm, fric~U[0.1,0.6], "
                                f"rest~U[0.2,0.8], dt=1e-5 s", "grid": list(b.combined.grid),
                    "l2": "inputs larger than L2, no flush"},
-        "autotune": {k: tune[k] for k in ("nt_pairs", "stage", "nt_bodies", "contact_ms")},
+        "autotune": {k: tune[k] for k in ("nt_pairs", "stage", "nt_bodies", "occ_pairs", "occ_bodies", "contact_ms")},
         "graph_launches_per_step": 1, "gpu_launches": launches,
         "fp64": {"value": n * k64 / secs64, "ms_per_step": 1e3 * secs64 / k64},
         "separate_handles": {"value": n * ksep / secs_sep, "ms_per_step": 1e3 * secs_sep / ksep, "steps": ksep,
@@ -499,6 +501,7 @@ def main():
         "e2e": e2e,
         "clocks": clocks,
         "gpu_launches": rmx["launches"],
+        "autotune": rmx["tune"],
         "status": {"fp64": r64["status"], "mixed": rmx["status"]},
     }
     if not args.no_cpu:

@@ -417,21 +417,25 @@ XDEM_API int xdem_sim_profile(xdem_sim* sim, unsigned int* launches,
                               double* contact_ms, unsigned int* contact_launches);
 
 /* Block shapes of the mixed contact stage (XDEM_MIXED handles): threads per
- * block of the pair kernel and of the body kernel (64, 128 or 256) and the
- * depth of the pair kernel's per-thread candidate stage (8 or 16).  A handle
+ * block of the pair kernel and of the body kernel (64, 128 or 256), the
+ * depth of the pair kernel's per-thread candidate stage (8 or 16), and the
+ * resident threads per SM each kernel is compiled for, i.e. its register
+ * budget (occ_pairs 768 or 1024; occ_bodies 512, 768 or 1024).  A handle
  * that keeps body wrenches (one scene with planes or meshes) needs
  * nt_pairs == nt_bodies.  Shapes never change results.  contact_ms: mean
  * event-timed contact stage of a step (autotune only).  No counterpart in
  * the reference, whose launchers fix 256 threads per block. */
 typedef struct xdem_tune {
-    unsigned int nt_pairs, stage, nt_bodies;
+    unsigned int nt_pairs, stage, nt_bodies, occ_pairs, occ_bodies;
     double contact_ms;
 } xdem_tune;
 XDEM_API int xdem_sim_set_tune(xdem_sim* sim, const xdem_tune* tune);
 XDEM_API int xdem_sim_get_tune(xdem_sim* sim, xdem_tune* tune);
-/* Times every candidate shape for trial_steps steps (after 2 warm-up steps)
+/* Times candidate shapes for trial_steps steps each (after 2 warm-up steps)
  * on the handle's scene, keeps the fastest in *best and on the handle, and
  * puts the state back as it was: tuning does not advance the simulation.
+ * A wrench-keeping handle tries every joint shape with equal block sizes
+ * (36); a batch tunes the pair kernel (12 shapes), then the body kernel (9).
  * all[0..*nall) receives every candidate with its time when given (*nall is
  * its capacity on entry, the number of candidates on return).  FP64 and
  * launcher-path handles have nothing to tune: *best is their fixed shape. */

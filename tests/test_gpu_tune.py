@@ -10,7 +10,8 @@ from xdynamics_dll_gb300 import types as T
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(64, 8, 64), (128, 16, 128), (256, 16, 64), (256, 8, 256), (64, 16, 256)]
+SHAPES = [(64, 8, 64, 768, 512), (128, 16, 128, 1024, 768), (256, 16, 64, 768, 1024), (256, 8, 256, 1024, 512),
+          (64, 16, 256, 768, 768)]
 
 
 @pytest.fixture(scope="module")
@@ -58,9 +59,9 @@ def test_wrench_keeping_handle_needs_equal_shapes(mods):
     with pytest.raises(_lib.XdemError):
         s.set_tune(64, 16, 128)
     ref = None
-    for nt in (64, 128, 256):
+    for nt, ob in ((64, 512), (128, 1024), (256, 768)):
         s2 = sim.Sim(sc, precision=T.XDEM_MIXED)
-        s2.set_tune(nt, 16, nt)
+        s2.set_tune(nt, 16, nt, 1024 if nt == 128 else 768, ob)
         s2.step(40)
         st, w = s2.state(), s2.wrench(0)
         if ref is None:
@@ -77,16 +78,15 @@ def test_autotune_leaves_the_simulation_where_it_was(mods, tmp_path):
     _, batch, _, _ = mods
     a = batch.Batch(members(batch))
     best, from_cache = a.autotune(trial_steps=5, cache=str(tmp_path / "tune.json"))
-    assert not from_cache and len(best["candidates"]) == 18
+    assert not from_cache and len(best["candidates"]) == 12 + 9
     assert best["contact_ms"] == min(c["contact_ms"] for c in best["candidates"])
     a.step(20)
     b = batch.Batch(members(batch))
-    b.sim.set_tune(best["nt_pairs"], best["stage"], best["nt_bodies"])
+    b.sim.set_tune(**{k: best[k] for k in T.Tune.SHAPE})
     b.step(20)
     states_equal(a.sim.state(), b.sim.state())
     # the same workload again: from the cache, nothing measured
     c = batch.Batch(members(batch))
     again, from_cache = c.autotune(trial_steps=5, cache=str(tmp_path / "tune.json"))
-    assert from_cache and {k: again[k] for k in ("nt_pairs", "stage", "nt_bodies")} == \
-        {k: best[k] for k in ("nt_pairs", "stage", "nt_bodies")}
+    assert from_cache and {k: again[k] for k in T.Tune.SHAPE} == {k: best[k] for k in T.Tune.SHAPE}
     assert c.sim.get_tune()["nt_pairs"] == best["nt_pairs"]

@@ -40,7 +40,7 @@ def tune(sim, trial_steps=10, cache=None):
             table = json.load(f)
     if key in table:
         t = table[key]
-        sim.set_tune(t["nt_pairs"], t["stage"], t["nt_bodies"])
+        sim.set_tune(**{k: t[k] for k in T.Tune.SHAPE})
         return dict(t), True
     best, cands = sim.autotune(trial_steps)
     if cache:

@@ -69,10 +69,12 @@ struct MatF {
 
 // Block shapes of the mixed contact stage, chosen by the autotuner
 // (xdem_sim_autotune): threads per block of the pair kernel and of the body
-// kernel (64, 128 or 256) and the pair kernel's candidate-stage depth (8 or
-// 16 entries a thread).  Results do not depend on them.
+// kernel (64, 128 or 256), the pair kernel's candidate-stage depth (8 or 16
+// entries a thread) and the resident threads per SM each kernel is compiled
+// for (pairs 768 or 1024, bodies 512, 768 or 1024: the register budget).
+// Results do not depend on them.
 struct MixedTune {
-    unsigned int nt_pairs = 128, stage = 16, nt_bodies = 128;
+    unsigned int nt_pairs = 128, stage = 16, nt_bodies = 128, occ_pairs = 768, occ_bodies = 512;
 };
 
 struct FusedState {

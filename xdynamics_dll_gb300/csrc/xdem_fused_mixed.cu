@@ -831,9 +831,10 @@ __device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned in
 // the sphere's force, moment and rolling sums (original order) for kernel 2.
 // It holds no plane or integration state, so it runs at twice the occupancy
 // of a kernel doing all of it -- the stencil walk is latency-bound.
-// NT threads per block with 768 / NT blocks per SM (80 registers a thread).
-template <bool MESH, unsigned int NT, unsigned int STAGE>
-__global__ void __launch_bounds__(NT, 768 / NT) k_mixed_pairs(const __grid_constant__ ContactLaunch c)
+// NT threads per block, OCC / NT blocks per SM (OCC 768: 80 registers a
+// thread, 1024: 64).
+template <bool MESH, unsigned int NT, unsigned int STAGE, unsigned int OCC>
+__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_constant__ ContactLaunch c)
 {
     __shared__ float smf[(NT / 32) * 6 * 2];
     __shared__ unsigned int stage[STAGE * NT];                // p2p candidates, [slot][thread]
@@ -893,8 +894,9 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_mixed_pairs(const __grid_const
 // every state array is read and written coalesced.  Plane contact (planes in
 // id order), rolling resistance, the velocity and position update and the
 // next step's records, on top of kernel 1's particle-particle sums.
-template <unsigned int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
+// OCC / NT blocks per SM (OCC 512: 128 registers a thread, 768: 80, 1024: 64).
+template <unsigned int NT, unsigned int OCC>
+__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
 {
     __shared__ float smf[(NT / 32) * 6 * 2];
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -991,16 +993,22 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_mixed_bodies(const __grid_cons
     mixed_tail(c, oid, ip, Ai, Li, Bi, Ff, Mf, bits);
 }
 
-template <bool MESH, unsigned int NT, unsigned int STAGE>
+template <bool MESH, unsigned int NT, unsigned int STAGE, unsigned int OCC>
 cudaError_t launch_pairs(const ContactLaunch& c, cudaStream_t st)
 {
-    k_mixed_pairs<MESH, NT, STAGE><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
+    k_mixed_pairs<MESH, NT, STAGE, OCC><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
     return cudaGetLastError();
+}
+template <bool MESH, unsigned int NT, unsigned int STAGE>
+cudaError_t launch_pairs_occ(const ContactLaunch& c, cudaStream_t st)
+{
+    return c.tune.occ_pairs == 1024 ? launch_pairs<MESH, NT, STAGE, 1024>(c, st)
+                                    : launch_pairs<MESH, NT, STAGE, 768>(c, st);
 }
 template <bool MESH, unsigned int NT>
 cudaError_t launch_pairs_stage(const ContactLaunch& c, cudaStream_t st)
 {
-    return c.tune.stage == 8 ? launch_pairs<MESH, NT, 8>(c, st) : launch_pairs<MESH, NT, 16>(c, st);
+    return c.tune.stage == 8 ? launch_pairs_occ<MESH, NT, 8>(c, st) : launch_pairs_occ<MESH, NT, 16>(c, st);
 }
 template <bool MESH>
 cudaError_t launch_pairs_nt(const ContactLaunch& c, cudaStream_t st)
@@ -1011,17 +1019,27 @@ cudaError_t launch_pairs_nt(const ContactLaunch& c, cudaStream_t st)
     default: return launch_pairs_stage<MESH, 128>(c, st);
     }
 }
-template <unsigned int NT>
+template <unsigned int NT, unsigned int OCC>
 cudaError_t launch_bodies(const ContactLaunch& c, cudaStream_t st)
 {
-    k_mixed_bodies<NT><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
+    k_mixed_bodies<NT, OCC><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
     return cudaGetLastError();
+}
+template <unsigned int NT>
+cudaError_t launch_bodies_occ(const ContactLaunch& c, cudaStream_t st)
+{
+    switch (c.tune.occ_bodies) {
+    case 768: return launch_bodies<NT, 768>(c, st);
+    case 1024: return launch_bodies<NT, 1024>(c, st);
+    default: return launch_bodies<NT, 512>(c, st);
+    }
 }
 
 }  // namespace
 
-// The block shapes come from c.tune (the autotuner's choice; 128 / 16 / 128
-// by default).  Body wrench partials are written per block by the kernel
+// The block shapes come from c.tune (the autotuner's choice; by default 128
+// threads, stage 16 and 768 threads per SM for the pairs, 128 threads and 512
+// per SM for the bodies).  Body wrench partials are written per block by the kernel
 // that owns the body (meshes: pairs, planes: bodies) into rows of c.nblocks
 // entries, so a handle that keeps wrenches runs both kernels with the same
 // block size (tune_valid) and c.nblocks = ceil(nentry / that size).
@@ -1031,9 +1049,9 @@ cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
     cudaError_t e = c.nmesh ? launch_pairs_nt<true>(c, st) : launch_pairs_nt<false>(c, st);
     if (e != cudaSuccess) return e;
     switch (c.tune.nt_bodies) {
-    case 64: return launch_bodies<64>(c, st);
-    case 256: return launch_bodies<256>(c, st);
-    default: return launch_bodies<128>(c, st);
+    case 64: return launch_bodies_occ<64>(c, st);
+    case 256: return launch_bodies_occ<256>(c, st);
+    default: return launch_bodies_occ<128>(c, st);
     }
 }
 

@@ -70,16 +70,25 @@ bool shape_ok(unsigned int nt) { return nt == 64 || nt == 128 || nt == 256; }
 // Body wrench partials need one block size for both kernels.
 bool keeps_wrenches(const xdem_sim* s) { return s->nscene == 1 && !s->bodies.empty(); }
 
+MixedTune from_abi(const xdem_tune& t)
+{
+    return MixedTune{t.nt_pairs, t.stage, t.nt_bodies, t.occ_pairs, t.occ_bodies};
+}
+xdem_tune to_abi(const MixedTune& m, double ms)
+{
+    return xdem_tune{m.nt_pairs, m.stage, m.nt_bodies, m.occ_pairs, m.occ_bodies, ms};
+}
+
 }  // namespace
 
 XDEM_API int xdem_sim_set_tune(xdem_sim* s, const xdem_tune* t)
 {
     if (!s || !t) return XDEM_ERR_ARG;
     if (!shape_ok(t->nt_pairs) || !shape_ok(t->nt_bodies) || (t->stage != 8 && t->stage != 16)) return XDEM_ERR_ARG;
+    if (t->occ_pairs != 768 && t->occ_pairs != 1024) return XDEM_ERR_ARG;
+    if (t->occ_bodies != 512 && t->occ_bodies != 768 && t->occ_bodies != 1024) return XDEM_ERR_ARG;
     if (keeps_wrenches(s) && t->nt_pairs != t->nt_bodies) return XDEM_ERR_ARG;
-    s->fs.tune.nt_pairs = t->nt_pairs;
-    s->fs.tune.stage = t->stage;
-    s->fs.tune.nt_bodies = t->nt_bodies;
+    s->fs.tune = from_abi(*t);
     fused_invalidate(s->fs);  // the captured step graphs bake in the shapes
     return XDEM_OK;
 }
@@ -87,10 +96,7 @@ XDEM_API int xdem_sim_set_tune(xdem_sim* s, const xdem_tune* t)
 XDEM_API int xdem_sim_get_tune(xdem_sim* s, xdem_tune* t)
 {
     if (!s || !t) return XDEM_ERR_ARG;
-    t->nt_pairs = s->fs.tune.nt_pairs;
-    t->stage = s->fs.tune.stage;
-    t->nt_bodies = s->fs.tune.nt_bodies;
-    t->contact_ms = 0.0;
+    *t = to_abi(s->fs.tune, 0.0);
     return XDEM_OK;
 }
 
@@ -114,28 +120,48 @@ XDEM_API int xdem_sim_autotune(xdem_sim* s, unsigned int trial_steps, xdem_tune*
         cudaGetLastError();
         return XDEM_ERR_ALLOC;
     }
-    std::vector<xdem_tune> cand;
-    const unsigned int nts[3] = {64, 128, 256}, stages[2] = {8, 16};
-    for (unsigned int a : nts)
-        for (unsigned int st : stages)
-            for (unsigned int b : nts) {
-                if (keeps_wrenches(s) && a != b) continue;
-                cand.push_back(xdem_tune{a, st, b, 0.0});
-            }
     const MixedTune keep = s->fs.tune;
     const bool prof = s->profiling;
-    int r = XDEM_OK;
-    xdem_tune win = {keep.nt_pairs, keep.stage, keep.nt_bodies, 1e300};
-    for (size_t i = 0; i < cand.size() && r == XDEM_OK; ++i) {
-        if (snap.put(s) != cudaSuccess) { r = XDEM_ERR_CUDA; break; }
-        s->fs.tune = MixedTune{cand[i].nt_pairs, cand[i].stage, cand[i].nt_bodies};
+    std::vector<xdem_tune> tried;
+    // one trial: from the snapshot, 2 warm-up steps, trial_steps timed
+    auto trial = [&](const MixedTune& t, double& ms) -> int {
+        if (snap.put(s) != cudaSuccess) return XDEM_ERR_CUDA;
+        s->fs.tune = t;
         s->profiling = false;
-        if ((r = xdem_sim_step(s, 2)) != XDEM_OK) break;  // warm-up (priming, caches)
+        if (int r = xdem_sim_step(s, 2)) return r;
         s->profiling = true;
-        if ((r = xdem_sim_step(s, trial_steps)) != XDEM_OK) break;
+        if (int r = xdem_sim_step(s, trial_steps)) return r;
         const unsigned int nrec = s->prof_contact_launches;
-        cand[i].contact_ms = nrec ? s->prof_ms / nrec : 0.0;
-        if (nrec && cand[i].contact_ms < win.contact_ms) win = cand[i];
+        ms = nrec ? s->prof_ms / nrec : 1e300;
+        tried.push_back(to_abi(t, ms));
+        return XDEM_OK;
+    };
+    const unsigned int nts[3] = {64, 128, 256}, stages[2] = {8, 16}, occp[2] = {768, 1024};
+    const unsigned int occb[3] = {512, 768, 1024};
+    int r = XDEM_OK;
+    MixedTune win = keep;
+    double win_ms = 1e300;
+    auto consider = [&](const MixedTune& t) {
+        if (r != XDEM_OK) return;
+        double ms = 0.0;
+        r = trial(t, ms);
+        if (r == XDEM_OK && ms < win_ms) {
+            win_ms = ms;
+            win = t;
+        }
+    };
+    if (keeps_wrenches(s)) {
+        for (unsigned int nt : nts)
+            for (unsigned int st : stages)
+                for (unsigned int op : occp)
+                    for (unsigned int ob : occb) consider(MixedTune{nt, st, nt, op, ob});
+    } else {
+        for (unsigned int nt : nts)
+            for (unsigned int st : stages)
+                for (unsigned int op : occp) consider(MixedTune{nt, st, keep.nt_bodies, op, keep.occ_bodies});
+        const MixedTune pw = win;
+        for (unsigned int nt : nts)
+            for (unsigned int ob : occb) consider(MixedTune{pw.nt_pairs, pw.stage, nt, pw.occ_pairs, ob});
     }
     s->profiling = prof;
     if (snap.put(s) != cudaSuccess && r == XDEM_OK) r = XDEM_ERR_CUDA;
@@ -149,12 +175,12 @@ XDEM_API int xdem_sim_autotune(xdem_sim* s, unsigned int trial_steps, xdem_tune*
         s->fs.tune = keep;
         return r;
     }
-    s->fs.tune = MixedTune{win.nt_pairs, win.stage, win.nt_bodies};
-    *best = win;
+    s->fs.tune = win;
+    *best = to_abi(win, win_ms);
     if (all && nall) {
-        const unsigned int n = std::min<unsigned int>(*nall, (unsigned int)cand.size());
-        for (unsigned int i = 0; i < n; ++i) all[i] = cand[i];
+        const unsigned int n = std::min<unsigned int>(*nall, (unsigned int)tried.size());
+        for (unsigned int i = 0; i < n; ++i) all[i] = tried[i];
     }
-    if (nall) *nall = (unsigned int)cand.size();
+    if (nall) *nall = (unsigned int)tried.size();
     return XDEM_OK;
 }

@@ -92,10 +92,14 @@ class ClusterInformation(C.Structure):
 
 class Tune(C.Structure):
     """xdem_tune (include/xdem_c.h): block shapes of the mixed contact stage."""
-    _fields_ = [("nt_pairs", C.c_uint), ("stage", C.c_uint), ("nt_bodies", C.c_uint), ("contact_ms", C.c_double)]
+    _fields_ = [("nt_pairs", C.c_uint), ("stage", C.c_uint), ("nt_bodies", C.c_uint), ("occ_pairs", C.c_uint),
+                ("occ_bodies", C.c_uint), ("contact_ms", C.c_double)]
+    SHAPE = ("nt_pairs", "stage", "nt_bodies", "occ_pairs", "occ_bodies")
 
     def as_dict(self):
-        return dict(nt_pairs=self.nt_pairs, stage=self.stage, nt_bodies=self.nt_bodies, contact_ms=self.contact_ms)
+        d = {k: getattr(self, k) for k in self.SHAPE}
+        d["contact_ms"] = self.contact_ms
+        return d
 
 
 class SimConfig(C.Structure):
