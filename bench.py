@@ -294,7 +294,8 @@ def bench_sweep(args, torch, local):
     setup_s = time.perf_counter() - t0
     stage(f"batch of {nsc} scenes, {b.combined.np_} spheres, grid {b.combined.grid}: {setup_s:.1f} s")
     tune, _ = b.autotune(trial_steps=10)
-    stage("autotune: " + "/".join(str(tune[k]) for k in ("nt_pairs", "stage", "occ_pairs", "nt_bodies", "occ_bodies")))
+    stage("autotune: " + "/".join(str(tune[k]) for k in ("nt_pairs", "stage", "occ_pairs", "nt_bodies", "occ_bodies",
+                                                         "skin_div")))
     stream = torch.cuda.Stream(device=local)
     b.sim.L.xdem_sim_set_stream(b.sim.h, stream.cuda_stream)
     b.set_graph(True)
@@ -351,7 +352,8 @@ def bench_sweep(args, torch, local):
                                f"(per scene {min(counts)}..{max(counts)}), r~U[1,3] mm, fric~U[0.1,0.6], "
                                f"rest~U[0.2,0.8], dt=1e-5 s", "grid": list(b.combined.grid),
                    "l2": "inputs larger than L2, no flush"},
-        "autotune": {k: tune[k] for k in ("nt_pairs", "stage", "nt_bodies", "occ_pairs", "occ_bodies", "contact_ms")},
+        "autotune": {k: tune[k] for k in ("nt_pairs", "stage", "nt_bodies", "occ_pairs", "occ_bodies", "skin_div",
+                                          "contact_ms")},
         "graph_launches_per_step": 1, "gpu_launches": launches,
         "fp64": {"value": n * k64 / secs64, "ms_per_step": 1e3 * secs64 / k64},
         "separate_handles": {"value": n * ksep / secs_sep, "ms_per_step": 1e3 * secs_sep / ksep, "steps": ksep,

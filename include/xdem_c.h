@@ -427,6 +427,9 @@ XDEM_API int xdem_sim_profile(xdem_sim* sim, unsigned int* launches,
  * the reference, whose launchers fix 256 threads per block. */
 typedef struct xdem_tune {
     unsigned int nt_pairs, stage, nt_bodies, occ_pairs, occ_bodies;
+    unsigned int skin_div;  /* pair search: 0 walks the 27-cell stencil every step; 8, 16 or 32 keep a
+                               candidate list per sphere with a skin of cell_size / skin_div, rebuilt on
+                               the device when a sphere has moved more than half the skin */
     double contact_ms;
 } xdem_tune;
 XDEM_API int xdem_sim_set_tune(xdem_sim* sim, const xdem_tune* tune);
@@ -436,6 +439,7 @@ XDEM_API int xdem_sim_get_tune(xdem_sim* sim, xdem_tune* tune);
  * puts the state back as it was: tuning does not advance the simulation.
  * A wrench-keeping handle tries every joint shape with equal block sizes
  * (36); a batch tunes the pair kernel (12 shapes), then the body kernel (9).
+ * Either then tries the four pair searches (skin_div 0, 8, 16, 32).
  * all[0..*nall) receives every candidate with its time when given (*nall is
  * its capacity on entry, the number of candidates on return).  FP64 and
  * launcher-path handles have nothing to tune: *best is their fixed shape. */

@@ -62,7 +62,7 @@ def test_argument_checks_need_no_gpu(L):
     assert L.xdem_adj_info(None, None, None, None) == T.XDEM_ERR_ARG
     assert L.xdem_adj_destroy(None) == T.XDEM_ERR_ARG
     # tuning entry points check their arguments first
-    t = T.Tune(128, 16, 128, 768, 512, 0.0)
+    t = T.Tune(128, 16, 128, 768, 512, 0, 0.0)
     assert L.xdem_sim_set_tune(None, C.byref(t)) == T.XDEM_ERR_ARG
     assert L.xdem_sim_get_tune(None, C.byref(t)) == T.XDEM_ERR_ARG
     assert L.xdem_sim_autotune(None, 5, C.byref(t), None, None) == T.XDEM_ERR_ARG

@@ -1,7 +1,8 @@
 """Block-shape autotuning of the mixed contact stage (xdem_sim_set_tune /
-xdem_sim_autotune): every shape gives the same state bit for bit, tuning
-leaves the simulation where it was, wrench-keeping handles refuse unequal
-shapes, and the cache answers a repeated workload without measuring."""
+xdem_sim_autotune): every shape and pair search (stencil walk or candidate
+lists) gives the same state bit for bit, tuning leaves the simulation where
+it was, wrench-keeping handles refuse unequal shapes, and the cache answers
+a repeated workload without measuring."""
 import numpy as np
 import pytest
 import torch
@@ -10,8 +11,8 @@ from xdynamics_dll_gb300 import types as T
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(64, 8, 64, 768, 512), (128, 16, 128, 1024, 768), (256, 16, 64, 768, 1024), (256, 8, 256, 1024, 512),
-          (64, 16, 256, 768, 768)]
+SHAPES = [(64, 8, 64, 768, 512, 0), (128, 16, 128, 1024, 768, 16), (256, 16, 64, 768, 1024, 8),
+          (256, 8, 256, 1024, 512, 32), (64, 16, 256, 768, 768, 16)]
 
 
 @pytest.fixture(scope="module")
@@ -61,7 +62,7 @@ def test_wrench_keeping_handle_needs_equal_shapes(mods):
     ref = None
     for nt, ob in ((64, 512), (128, 1024), (256, 768)):
         s2 = sim.Sim(sc, precision=T.XDEM_MIXED)
-        s2.set_tune(nt, 16, nt, 1024 if nt == 128 else 768, ob)
+        s2.set_tune(nt, 16, nt, 1024 if nt == 128 else 768, ob, 16 if nt == 64 else 0)
         s2.step(40)
         st, w = s2.state(), s2.wrench(0)
         if ref is None:
@@ -78,7 +79,7 @@ def test_autotune_leaves_the_simulation_where_it_was(mods, tmp_path):
     _, batch, _, _ = mods
     a = batch.Batch(members(batch))
     best, from_cache = a.autotune(trial_steps=5, cache=str(tmp_path / "tune.json"))
-    assert not from_cache and len(best["candidates"]) == 12 + 9
+    assert not from_cache and len(best["candidates"]) == 12 + 9 + 3
     assert best["contact_ms"] == min(c["contact_ms"] for c in best["candidates"])
     a.step(20)
     b = batch.Batch(members(batch))
@@ -90,3 +91,67 @@ def test_autotune_leaves_the_simulation_where_it_was(mods, tmp_path):
     again, from_cache = c.autotune(trial_steps=5, cache=str(tmp_path / "tune.json"))
     assert from_cache and {k: again[k] for k in T.Tune.SHAPE} == {k: best[k] for k in T.Tune.SHAPE}
     assert c.sim.get_tune()["nt_pairs"] == best["nt_pairs"]
+
+
+@pytest.mark.parametrize("skin_div", [8, 32])
+def test_candidate_lists_match_the_stencil_walk(mods, skin_div):
+    """A moving, colliding bed over 400 steps: the lists are rebuilt many
+    times (a thin skin more often) and every step matches the walk."""
+    _, _, scenes, sim = mods
+    sc = scenes.random_packed(3000, 1e-3, 2e-3, 0.05, 17, overlap=0.03, vel_scale=0.3, omega_scale=20.0)
+    out = []
+    for sd in (0, skin_div):
+        s = sim.Sim(sc, precision=T.XDEM_MIXED)
+        s.set_tune(128, 16, 128, 768, 512, sd)
+        st = []
+        for _ in range(4):
+            s.step(100)
+            st.append((s.state(), s.pairs(0)))
+        assert s.status() == 0
+        out.append(st)
+        s.close()
+    for (a, pa), (b, pb) in zip(*out):
+        states_equal(a, b)
+        for x, y in zip(pa, pb):
+            assert np.array_equal(x, y)
+
+
+def test_overflowing_candidate_list_walks(mods):
+    """A 3 mm sphere ringed by 40 small ones within the skin holds more
+    candidates than a list keeps: it walks the stencil, the rest use lists,
+    and the state matches the walk everywhere."""
+    _, _, scenes, sim = mods
+    rng = np.random.default_rng(5)
+    n_in, n_out = 10, 30
+    pts = [np.zeros(3)]
+    rad = [3e-3]
+    k = np.arange(n_in + n_out) + 0.5
+    th = np.arccos(1 - 2 * k / (n_in + n_out))
+    ph = np.pi * (1 + 5 ** 0.5) * k
+    dirs = np.stack([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)], 1)
+    for i, d in enumerate(dirs):
+        pts.append(d * (3.45e-3 if i % 4 == 0 and i // 4 < n_in else 3.7e-3))
+        rad.append(0.5e-3)
+    n = len(pts)
+    sc = scenes.random_packed(n, 1e-3, 1e-3, 0.05, 3, nplanes=0)
+    pos = np.zeros((n, 4))
+    pos[:, :3] = np.array(pts) + 0.1
+    pos[:, 3] = rad
+    sc.pos = pos.ravel()
+    m, J = scenes.sphere_mass_inertia(np.array(rad), 2500.0)
+    sc.mass, sc.inertia = m, J.ravel()
+    sc.vel = rng.normal(0, 0.02, n * 3)
+    sc.gravity = (0.0, 0.0, 0.0)
+    sc.cell_size = 6e-3
+    out = []
+    for sd in (0, 8):
+        s = sim.Sim(sc, precision=T.XDEM_MIXED)
+        s.set_tune(128, 16, 128, 768, 512, sd)
+        s.step(20)
+        assert s.status() == 0
+        out.append((s.state(), s.pairs(0)))
+        s.close()
+    states_equal(out[0][0], out[1][0])
+    assert out[0][1][0][0] >= 5  # the big sphere keeps its contacts
+    for x, y in zip(out[0][1], out[1][1]):
+        assert np.array_equal(x, y)

@@ -73,9 +73,15 @@ struct MatF {
 // entries a thread) and the resident threads per SM each kernel is compiled
 // for (pairs 768 or 1024, bodies 512, 768 or 1024: the register budget).
 // Results do not depend on them.
+// skin_div selects the pair search: 0 walks the 27-cell stencil every step;
+// d > 0 keeps a candidate list per sphere with a skin of (cell size) / d,
+// rebuilt by a stencil walk only when some sphere has moved more than half
+// the skin since the last build.
 struct MixedTune {
-    unsigned int nt_pairs = 128, stage = 16, nt_bodies = 128, occ_pairs = 768, occ_bodies = 512;
+    unsigned int nt_pairs = 128, stage = 16, nt_bodies = 128, occ_pairs = 768, occ_bodies = 512, skin_div = 0;
 };
+// Candidates a sphere's list holds; a sphere with more walks the stencil.
+constexpr unsigned int kListCap = 24;
 
 struct FusedState {
     MixedTune tune;
@@ -104,6 +110,13 @@ struct FusedState {
     float* fA = nullptr;        // [np*4] particle-particle force, rolling resistance (original order)
     float* fB = nullptr;        // [np*4] particle-particle moment
     float* fC = nullptr;        // [np*4] rolling: sum of contact moments
+    // candidate lists (skin_div > 0): ids in any order, count (> kListCap:
+    // overflowed, walk), FP32 centre at the build, rebuild flags [in, out]
+    unsigned int* vl_ids = nullptr;  // [np * kListCap]
+    unsigned int* vl_cnt = nullptr;  // [np]
+    float* vl_xb = nullptr;          // [np*4]
+    unsigned int* vl_flag = nullptr; // [2]
+    bool any_coh = false;            // cohesion in a particle-pair material (no lists)
     MatF* d_mpf = nullptr;      // FP32 material table (scenes' particle pairs, then bodies)
     size_t mpf_cap = 0;
     unsigned int* pp_count2 = nullptr;
@@ -210,6 +223,14 @@ struct ContactLaunch {
     float* rB;
     float* rC;
     unsigned int* rT;
+    // candidate lists (use_list): see FusedState
+    bool use_list;
+    unsigned int* vl_ids;
+    unsigned int* vl_cnt;
+    float* vl_xb;
+    const unsigned int* vl_in;  // nonzero: this step rebuilds (walk)
+    unsigned int* vl_out;       // set when a sphere moved beyond half the skin
+    float skin_f, half_skin2_f;
     const PlaneF* planef;
     const PlaneDF* planedf;
     double inv_cs;   // 1 / cell size

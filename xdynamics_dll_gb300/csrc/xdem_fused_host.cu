@@ -309,6 +309,10 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.rB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rC, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.rT, np);
+        if (e == cudaSuccess) e = dalloc(fs.vl_ids, (size_t)np * kListCap);
+        if (e == cudaSuccess) e = dalloc(fs.vl_cnt, np);
+        if (e == cudaSuccess) e = dalloc(fs.vl_xb, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.vl_flag, 2);
     } else {
         if (e == cudaSuccess) e = dalloc(fs.snap_pos, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.snap_vel, (size_t)nentry * 4);
@@ -331,7 +335,7 @@ void fused_free(FusedState& fs)
 {
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
                   fs.mC, fs.mIT, fs.rA, fs.rL, fs.rB, fs.rC, fs.rT, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
-                  fs.pp_tsd2,
+                  fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag,
                   fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf};
     for (void* q : ps)
         if (q) cudaFree(q);
@@ -409,6 +413,8 @@ int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned i
         fs.mpf_cap = nmp;
     }
     std::vector<MatF> mf(nmp);
+    fs.any_coh = false;
+    for (unsigned int i = 0; i < nscene && i < nmp; ++i) fs.any_coh = fs.any_coh || host_mp[i].coh != 0.0;
     for (unsigned int i = 0; i < nmp; ++i) {
         const mat_pair& m = host_mp[i];
         mf[i] = MatF{(float)m.Eeq, (float)m.Seq8, (float)m.beta, (float)m.vs1, (float)m.sratio, (float)m.fric,
@@ -495,6 +501,11 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         // and the origin separately, so the origin's size counts too
         const double o_len = std::sqrt(org[0] * org[0] + org[1] * org[1] + org[2] * org[2]);
         fs.frame_margin = (float)(16.0 * (R + o_len) * std::ldexp(1.0, -24) + 1e-9);
+        // the first step after priming builds the candidate lists
+        if (fs.vl_flag) {
+            ok(cudaMemsetAsync(fs.vl_flag, 1, sizeof(unsigned int), st));
+            ok(cudaMemsetAsync(fs.vl_flag + 1, 0, sizeof(unsigned int), st));
+        }
         fs.primed = true;
     }
     // Between steps *a.pos / *a.ep hold the committed state (x_n) and the
@@ -538,6 +549,11 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.mA = fs.mA; c.mL = fs.mL; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
     c.rA = fs.rA; c.rL = fs.rL; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
     c.fA = fs.fA; c.fB = fs.fB; c.fC = fs.fC;
+    c.use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && a.nmesh == 0 && !fs.any_coh && fs.vl_flag;
+    c.vl_ids = fs.vl_ids; c.vl_cnt = fs.vl_cnt; c.vl_xb = fs.vl_xb;
+    c.vl_in = fs.vl_flag; c.vl_out = fs.vl_flag ? fs.vl_flag + 1 : nullptr;
+    c.skin_f = fs.tune.skin_div ? (float)(a.prm.cell_size / fs.tune.skin_div) : 0.f;
+    c.half_skin2_f = 0.25f * c.skin_f * c.skin_f;
     c.mpf = fs.d_mpf;
     c.planef = fs.d_planef;
     c.planedf = fs.d_planedf;
@@ -578,7 +594,9 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.scene_plane_first = c.nscene > 1 ? a.scene_plane_first : nullptr;
     if (e0) cudaEventRecord(e0, st);
     ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
-    if (fs.mixed) nl++;  // the mixed contact stage is two kernels (pairs, bodies)
+    // the mixed contact stage is two kernels (pairs, bodies), with candidate
+    // lists four (stencil walk, list pairs, bodies, flag roll)
+    if (fs.mixed) nl += c.use_list ? 3 : 1;
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody && c.nscene == 1) {  // batched handles keep no body wrenches
         k_body_sums<<<a.nbody * 6, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench);

@@ -212,24 +212,18 @@ struct Acc {
 // repeated for the rest, in the same order.  Entries
 // whose packed unwrapped cell is not one of the stencil's are aliases of the
 // wrapping hash and are skipped.
-// Pass 2 for one staged candidate at sorted position j.
+// Pass 2 for one candidate: sphere k with packed cell Tk and records Aj, Lj,
+// Bj, Cj.
 template <unsigned int NT>
-__device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oid, unsigned int j, unsigned int ux,
-                                         unsigned int uy, unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
-                                         unsigned int sid, unsigned int old_count, const unsigned int* old_id,
-                                         unsigned int scene, bool coh, V3<float>& Ft, V3<float>& Fn,
-                                         unsigned int& cnt, Acc& acc, unsigned int& bits)
+__device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned int k, unsigned int Tk, float4 Aj,
+                                             float4 Lj, float4 Bj, float4 Cj, unsigned int ux, unsigned int uy,
+                                             unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
+                                             unsigned int sid, unsigned int old_count, const unsigned int* old_id,
+                                             unsigned int scene, bool coh, V3<float>& Ft, V3<float>& Fn,
+                                             unsigned int& cnt, Acc& acc, unsigned int& bits)
 {
     const float cs = c.cs_f, cs_lo = c.cs_lo;
-    // every record of the candidate in one round trip (the screen is tight,
-    // so velocity and spin are nearly always needed)
-    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
-    if (c.scene_of && c.scene_of[it.x] != scene) return;  // another scene of the batch
-    const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
-    const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
-    const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
-    const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
-    const unsigned int k = it.x;
+    const uint2 it = make_uint2(k, Tk);
     // stencil steps (+1) from the packed cells, and the shifts as float pairs
     const unsigned int xs = (it.y - ux + 1u) & 2047u;
     const unsigned int ys = ((it.y >> 11) - uy + 1u) & 2047u;
@@ -305,13 +299,38 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
     }
 }
 
+// Pass 2 for one staged candidate at sorted position j (every record of the
+// candidate in one round trip: the screen is tight, so velocity and spin are
+// nearly always needed).
+template <unsigned int NT>
+__device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oid, unsigned int j, unsigned int ux,
+                                         unsigned int uy, unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
+                                         unsigned int sid, unsigned int old_count, const unsigned int* old_id,
+                                         unsigned int scene, bool coh, V3<float>& Ft, V3<float>& Fn,
+                                         unsigned int& cnt, Acc& acc, unsigned int& bits)
+{
+    const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
+    if (c.scene_of && c.scene_of[it.x] != scene) return;  // another scene of the batch
+    const float4 Aj = reinterpret_cast<const float4*>(c.mA)[j];
+    const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
+    const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
+    const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
+    p2p_pair_rec<NT>(c, it.x, it.y, Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene, coh, Ft,
+                     Fn, cnt, acc, bits);
+}
+
+// Pass 1 + 2 over the 27-cell stencil.  With `build` the screen widens by
+// the skin and every candidate it passes (at most kListCap; the count keeps
+// going past it to flag an overflow) goes to the sphere's candidate list.
 template <unsigned int NT, unsigned int STAGE>
 __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int oid, unsigned int gx,
                                           unsigned int gy, unsigned int gz, float4 Ai, float4 Li, unsigned int Ti,
                                           float4 Bi, float4 Ci, unsigned int* stage, unsigned int* old_id,
-                                          Acc& acc, unsigned int& bits)
+                                          Acc& acc, unsigned int& bits, bool build = false)
 {
     const device_dem_parameters& p = c.prm;
+    unsigned int nlist = 0;
+    unsigned int* vl = build ? c.vl_ids + (size_t)oid * kListCap : nullptr;
     const unsigned int scene = scene_index(c, oid);
     const bool coh = c.mpf[scene].coh != 0;
     const float cs = c.cs_f;
@@ -380,7 +399,8 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                             const float dx = Aj.x + ((xs == 0u ? -cs : (xs == 2u ? cs : 0.f)) - Ai.x);
                             const float dy = Aj.y + sy, dz = Aj.z + sz;
                             const float rr = Ai.w + Aj.w;
-                            if (!(dx * dx + dy * dy + dz * dz < rr * rr * screen)) continue;
+                            const float lim = build ? (rr + c.skin_f) * (rr + c.skin_f) : rr * rr * screen;
+                            if (!(dx * dx + dy * dy + dz * dz < lim)) continue;
                         }
                         if (seen++ < done) continue;
                         if (nc == STAGE) {
@@ -388,6 +408,10 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                             break;
                         }
                         stage[nc++ * NT] = j;
+                        if (build) {
+                            if (nlist < kListCap) vl[nlist] = it.x;
+                            nlist++;
+                        }
                     }
                 }
             }
@@ -403,6 +427,69 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
         for (unsigned int q = 0; q < nc; ++q)
             p2p_pair<NT>(c, oid, stage[q * NT], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
                      coh, Ft, Fn, cnt, acc, bits);
+    }
+    c.pp_count_new[oid] = cnt;
+    if (build) {
+        c.vl_cnt[oid] = nlist;
+        reinterpret_cast<float4*>(c.vl_xb)[oid] =
+            make_float4((float)ux * cs + Ai.x, (float)uy * cs + Ai.y, (float)uz * cs + Ai.z, 0.f);
+    }
+}
+
+// The same contacts from sphere oid's candidate list instead of the stencil
+// walk.  The walk meets neighbours cell by cell (z, then y, then x offset of
+// the neighbour's cell from oid's, each -1..1) and, within a cell, in sorted
+// order, which is ascending id (the sort is stable and its input is in id
+// order).  Sorting the candidates by (cell offset, id) from this step's
+// cells therefore visits the contacts in the walk's order: pair lists, the
+// Ft a zero-slip contact keeps and every sum come out the same.  The list
+// holds every sphere within r_i + r_j + skin at its build, so while no
+// sphere has moved half the skin it holds every contact.
+template <unsigned int NT>
+__device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oid, float4 Ai, float4 Li,
+                                         unsigned int Ti, float4 Bi, float4 Ci, unsigned int* old_id, Acc& acc,
+                                         unsigned int& bits)
+{
+    const unsigned int scene = scene_index(c, oid);
+    const bool coh = false;  // lists are only kept without cohesion
+    const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
+    const unsigned int sid = oid * MAX_P2P_COUNT;
+    unsigned int old_count = c.pp_count_old[oid];
+    if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
+    for (unsigned int q = 0; q < old_count; ++q) cp_async4(old_id + q * NT, c.pp_id_old + sid + q);
+    cp_async_commit();
+    const unsigned int n = c.vl_cnt[oid];
+    const unsigned int* ids = c.vl_ids + (size_t)oid * kListCap;
+    // (cell offset key, id) of the candidates inside this step's stencil
+    unsigned long long key[kListCap];
+    unsigned int nk = 0;
+    for (unsigned int q = 0; q < n; ++q) {
+        const unsigned int k = ids[q];
+        if (c.scene_of && c.scene_of[k] != scene) continue;  // another scene of the batch
+        const unsigned int Tk = c.rT[k];
+        const unsigned int xs = (Tk - ux + 1u) & 2047u;
+        const unsigned int ys = ((Tk >> 11) - uy + 1u) & 2047u;
+        const unsigned int zs = ((Tk >> 22) - uz + 1u) & 1023u;
+        if (xs > 2u || ys > 2u || zs > 2u) continue;
+        const unsigned long long kk = ((unsigned long long)((zs * 3u + ys) * 3u + xs) << 32) | k;
+        unsigned int p = nk++;
+        while (p > 0 && key[p - 1] > kk) {
+            key[p] = key[p - 1];
+            --p;
+        }
+        key[p] = kk;
+    }
+    cp_async_wait_all();
+    V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
+    unsigned int cnt = 0;
+    for (unsigned int q = 0; q < nk; ++q) {
+        const unsigned int k = (unsigned int)key[q];
+        const float4 Aj = reinterpret_cast<const float4*>(c.rA)[k];
+        const float4 Lj = reinterpret_cast<const float4*>(c.rL)[k];
+        const float4 Bj = reinterpret_cast<const float4*>(c.rB)[k];
+        const float4 Cj = reinterpret_cast<const float4*>(c.rC)[k];
+        p2p_pair_rec<NT>(c, k, c.rT[k], Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene, coh,
+                         Ft, Fn, cnt, acc, bits);
     }
     c.pp_count_new[oid] = cnt;
 }
@@ -789,6 +876,15 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
     reinterpret_cast<float4*>(c.rB)[oid] = make_float4(vn.x, vn.y, vn.z, Bi.w);
     reinterpret_cast<float4*>(c.rC)[oid] = make_float4(w.x, w.y, w.z, 0.f);
     c.rT[oid] = pack_cell(cell[0], cell[1], cell[2]);
+    if (c.use_list) {
+        // distance from the centre at the last list build, in the lists'
+        // frame (packed cell times cell size plus the offset)
+        const float4 xb = reinterpret_cast<const float4*>(c.vl_xb)[oid];
+        const float dx = (float)(cell[0] & 2047) * c.cs_f + A[0].hi - xb.x;
+        const float dy = (float)(cell[1] & 2047) * c.cs_f + A[1].hi - xb.y;
+        const float dz = (float)(cell[2] & 1023) * c.cs_f + A[2].hi - xb.z;
+        if (!(dx * dx + dy * dy + dz * dz < c.half_skin2_f)) atomicOr(c.vl_out, 1u);
+    }
     if (bits) atomicOr(c.status, bits);
 }
 
@@ -839,6 +935,10 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     __shared__ float smf[(NT / 32) * 6 * 2];
     __shared__ unsigned int stage[STAGE * NT];                // p2p candidates, [slot][thread]
     __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
+    // with candidate lists the walk runs only on rebuild steps (a uniform
+    // branch); k_mixed_pairs_list does the other steps
+    const bool build = c.use_list;
+    if (build && !*c.vl_in) return;
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned int oid = 0xffffffffu;
     if (s < c.nentry) oid = c.sorted_index[s];
@@ -870,7 +970,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     // ------------------------------------------------ particle-particle (impl:613-733)
     if (live && c.has_pp)
         p2p_mixed<NT, STAGE>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
-                             bits);
+                             bits, build);
 
     // ------------------------------------------------ triangle meshes (impl:1930-2109)
     if (MESH) {
@@ -888,6 +988,50 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     reinterpret_cast<float4*>(c.fB)[oid] = make_float4(acc.m[0].value(), acc.m[1].value(), acc.m[2].value(), 0.f);
     if (c.rolling) reinterpret_cast<float4*>(c.fC)[oid] = make_float4(acc.tm.x, acc.tm.y, acc.tm.z, 0.f);
     if (bits) atomicOr(c.status, bits);
+}
+
+// Kernel 1 on the steps between list rebuilds: one thread per sphere in
+// original order, particle-particle contact from the sphere's candidate list
+// (a sphere whose list overflowed walks the stencil).  Writes the same sums
+// as k_mixed_pairs for kernel 2.
+template <unsigned int NT, unsigned int OCC>
+__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
+{
+    __shared__ unsigned int stage[16 * NT];                   // walk fallback candidates, [slot][thread]
+    __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
+    if (*c.vl_in) return;  // a rebuild step: k_mixed_pairs walks
+    const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (oid >= c.np) return;
+    const float4 Ai = reinterpret_cast<const float4*>(c.rA)[oid];
+    const float4 Li = reinterpret_cast<const float4*>(c.rL)[oid];
+    const float4 Bi = reinterpret_cast<const float4*>(c.rB)[oid];
+    const float4 Ci = reinterpret_cast<const float4*>(c.rC)[oid];
+    const unsigned int Ti = c.rT[oid];
+    Acc acc;
+    acc.tm = v3<float>(0.f, 0.f, 0.f);
+    acc.rs = 0.f;
+    unsigned int bits = 0;
+    if (c.vl_cnt[oid] <= kListCap) {
+        p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, acc, bits);
+    } else {
+        const device_dem_parameters& p = c.prm;
+        const unsigned int gx = (Ti & 2047u) & (p.grid_size.x - 1), gy = ((Ti >> 11) & 2047u) & (p.grid_size.y - 1);
+        const unsigned int gz = (Ti >> 22) & (p.grid_size.z - 1);
+        p2p_mixed<NT, 16>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
+                          bits);
+    }
+    reinterpret_cast<float4*>(c.fA)[oid] = make_float4(acc.f[0].value(), acc.f[1].value(), acc.f[2].value(), acc.rs);
+    reinterpret_cast<float4*>(c.fB)[oid] = make_float4(acc.m[0].value(), acc.m[1].value(), acc.m[2].value(), 0.f);
+    if (c.rolling) reinterpret_cast<float4*>(c.fC)[oid] = make_float4(acc.tm.x, acc.tm.y, acc.tm.z, 0.f);
+    if (bits) atomicOr(c.status, bits);
+}
+
+// After kernel 2: this step's "moved too far" flag becomes the next step's
+// rebuild flag.
+__global__ void k_vl_roll(unsigned int* flag)
+{
+    flag[0] = flag[1];
+    flag[1] = 0u;
 }
 
 // Kernel 2 of the mixed step: one thread per sphere in original order, so
@@ -1020,6 +1164,21 @@ cudaError_t launch_pairs_nt(const ContactLaunch& c, cudaStream_t st)
     }
 }
 template <unsigned int NT, unsigned int OCC>
+cudaError_t launch_list(const ContactLaunch& c, cudaStream_t st)
+{
+    k_mixed_pairs_list<NT, OCC><<<(c.np + NT - 1) / NT, NT, 0, st>>>(c);
+    return cudaGetLastError();
+}
+inline cudaError_t launch_list_nt(const ContactLaunch& c, cudaStream_t st)
+{
+    const bool hi = c.tune.occ_pairs == 1024;
+    switch (c.tune.nt_pairs) {
+    case 64: return hi ? launch_list<64, 1024>(c, st) : launch_list<64, 768>(c, st);
+    case 256: return hi ? launch_list<256, 1024>(c, st) : launch_list<256, 768>(c, st);
+    default: return hi ? launch_list<128, 1024>(c, st) : launch_list<128, 768>(c, st);
+    }
+}
+template <unsigned int NT, unsigned int OCC>
 cudaError_t launch_bodies(const ContactLaunch& c, cudaStream_t st)
 {
     k_mixed_bodies<NT, OCC><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
@@ -1048,11 +1207,18 @@ cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
     if (c.nentry == 0) return cudaSuccess;
     cudaError_t e = c.nmesh ? launch_pairs_nt<true>(c, st) : launch_pairs_nt<false>(c, st);
     if (e != cudaSuccess) return e;
-    switch (c.tune.nt_bodies) {
-    case 64: return launch_bodies_occ<64>(c, st);
-    case 256: return launch_bodies_occ<256>(c, st);
-    default: return launch_bodies_occ<128>(c, st);
+    if (c.use_list) {
+        e = launch_list_nt(c, st);
+        if (e != cudaSuccess) return e;
     }
+    switch (c.tune.nt_bodies) {
+    case 64: e = launch_bodies_occ<64>(c, st); break;
+    case 256: e = launch_bodies_occ<256>(c, st); break;
+    default: e = launch_bodies_occ<128>(c, st); break;
+    }
+    if (e != cudaSuccess || !c.use_list) return e;
+    k_vl_roll<<<1, 1, 0, st>>>(c.vl_out - 1);
+    return cudaGetLastError();
 }
 
 }  // namespace xdem

@@ -72,11 +72,11 @@ bool keeps_wrenches(const xdem_sim* s) { return s->nscene == 1 && !s->bodies.emp
 
 MixedTune from_abi(const xdem_tune& t)
 {
-    return MixedTune{t.nt_pairs, t.stage, t.nt_bodies, t.occ_pairs, t.occ_bodies};
+    return MixedTune{t.nt_pairs, t.stage, t.nt_bodies, t.occ_pairs, t.occ_bodies, t.skin_div};
 }
 xdem_tune to_abi(const MixedTune& m, double ms)
 {
-    return xdem_tune{m.nt_pairs, m.stage, m.nt_bodies, m.occ_pairs, m.occ_bodies, ms};
+    return xdem_tune{m.nt_pairs, m.stage, m.nt_bodies, m.occ_pairs, m.occ_bodies, m.skin_div, ms};
 }
 
 }  // namespace
@@ -87,6 +87,7 @@ XDEM_API int xdem_sim_set_tune(xdem_sim* s, const xdem_tune* t)
     if (!shape_ok(t->nt_pairs) || !shape_ok(t->nt_bodies) || (t->stage != 8 && t->stage != 16)) return XDEM_ERR_ARG;
     if (t->occ_pairs != 768 && t->occ_pairs != 1024) return XDEM_ERR_ARG;
     if (t->occ_bodies != 512 && t->occ_bodies != 768 && t->occ_bodies != 1024) return XDEM_ERR_ARG;
+    if (t->skin_div != 0 && t->skin_div != 8 && t->skin_div != 16 && t->skin_div != 32) return XDEM_ERR_ARG;
     if (keeps_wrenches(s) && t->nt_pairs != t->nt_bodies) return XDEM_ERR_ARG;
     s->fs.tune = from_abi(*t);
     fused_invalidate(s->fs);  // the captured step graphs bake in the shapes
@@ -154,14 +155,24 @@ XDEM_API int xdem_sim_autotune(xdem_sim* s, unsigned int trial_steps, xdem_tune*
         for (unsigned int nt : nts)
             for (unsigned int st : stages)
                 for (unsigned int op : occp)
-                    for (unsigned int ob : occb) consider(MixedTune{nt, st, nt, op, ob});
+                    for (unsigned int ob : occb) consider(MixedTune{nt, st, nt, op, ob, keep.skin_div});
     } else {
         for (unsigned int nt : nts)
             for (unsigned int st : stages)
-                for (unsigned int op : occp) consider(MixedTune{nt, st, keep.nt_bodies, op, keep.occ_bodies});
+                for (unsigned int op : occp)
+                    consider(MixedTune{nt, st, keep.nt_bodies, op, keep.occ_bodies, keep.skin_div});
         const MixedTune pw = win;
         for (unsigned int nt : nts)
-            for (unsigned int ob : occb) consider(MixedTune{pw.nt_pairs, pw.stage, nt, pw.occ_pairs, ob});
+            for (unsigned int ob : occb) consider(MixedTune{pw.nt_pairs, pw.stage, nt, pw.occ_pairs, ob, pw.skin_div});
+    }
+    // pair search: stencil walk every step, or candidate lists of three skins
+    const MixedTune bw = win;
+    const unsigned int skins[4] = {0, 8, 16, 32};
+    for (unsigned int sk : skins) {
+        if (sk == bw.skin_div) continue;
+        MixedTune t = bw;
+        t.skin_div = sk;
+        consider(t);
     }
     s->profiling = prof;
     if (snap.put(s) != cudaSuccess && r == XDEM_OK) r = XDEM_ERR_CUDA;

@@ -141,9 +141,10 @@ class Sim:
         """Replay the step from a captured CUDA graph (identical results)."""
         _lib.check(self.L.xdem_sim_set_graph(self.h, int(on)), "xdem_sim_set_graph")
 
-    def set_tune(self, nt_pairs=128, stage=16, nt_bodies=128, occ_pairs=768, occ_bodies=512):
-        """Block shapes of the mixed contact stage (results do not depend on them)."""
-        t = T.Tune(nt_pairs, stage, nt_bodies, occ_pairs, occ_bodies, 0.0)
+    def set_tune(self, nt_pairs=128, stage=16, nt_bodies=128, occ_pairs=768, occ_bodies=512, skin_div=0):
+        """Block shapes and pair search of the mixed contact stage (results do
+        not depend on them)."""
+        t = T.Tune(nt_pairs, stage, nt_bodies, occ_pairs, occ_bodies, skin_div, 0.0)
         _lib.check(self.L.xdem_sim_set_tune(self.h, C.byref(t)), "xdem_sim_set_tune")
 
     def get_tune(self):

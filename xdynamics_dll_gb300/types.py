@@ -93,8 +93,8 @@ class ClusterInformation(C.Structure):
 class Tune(C.Structure):
     """xdem_tune (include/xdem_c.h): block shapes of the mixed contact stage."""
     _fields_ = [("nt_pairs", C.c_uint), ("stage", C.c_uint), ("nt_bodies", C.c_uint), ("occ_pairs", C.c_uint),
-                ("occ_bodies", C.c_uint), ("contact_ms", C.c_double)]
-    SHAPE = ("nt_pairs", "stage", "nt_bodies", "occ_pairs", "occ_bodies")
+                ("occ_bodies", C.c_uint), ("skin_div", C.c_uint), ("contact_ms", C.c_double)]
+    SHAPE = ("nt_pairs", "stage", "nt_bodies", "occ_pairs", "occ_bodies", "skin_div")
 
     def as_dict(self):
         d = {k: getattr(self, k) for k in self.SHAPE}
