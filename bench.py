@@ -217,23 +217,30 @@ def time_device(sim, torch, steps, stream):
     return start.elapsed_time(end) / 1e3
 
 
-def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None):
+def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None, shapes=None):
     """Times `steps` steps replayed from the handle's CUDA graph (the way a
     user runs it), then times the contact stage alone with CUDA events over
     up to 64 further, eagerly launched steps."""
     sm = new_sim(scene, precision)
     stream = torch.cuda.Stream(device=dev)
     sm.L.xdem_sim_set_stream(sm.h, stream.cuda_stream)
-    # block shapes from the autotuner (mixed form; the state is put back)
-    tune, _ = sm.autotune(trial_steps=10)
+    # block shapes from the autotuner (mixed form; the state is put back),
+    # or given (a profiler run repeats a tuned run's shapes)
+    if shapes:
+        sm.set_tune(**shapes)
+        tune = sm.get_tune()
+    else:
+        tune, _ = sm.autotune(trial_steps=10)
     sm.set_graph(True)
     sm.step(warmup)
     torch.cuda.synchronize()
+    rb0 = sm.list_rebuilds()
     if sampler:
         with sampler:
             secs = time_device(sm, torch, steps, stream)
     else:
         secs = time_device(sm, torch, steps, stream)
+    rebuilds = sm.list_rebuilds() - rb0
     launches, _, _ = sm.profile()
     ke, ncontact = sm.energy()
     sm.set_profiling(True)
@@ -242,7 +249,8 @@ def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None):
     sm.set_profiling(False)
     st = sm.status()
     return sm, stream, {"secs": secs, "launches": launches, "contact_ms": contact_ms / max(contact_n, 1),
-                        "contact_launches": contact_n, "ncontact": ncontact, "ke": ke, "status": st, "tune": tune}
+                        "contact_launches": contact_n, "ncontact": ncontact, "ke": ke, "status": st, "tune": tune,
+                        "list_rebuilds": rebuilds}
 
 
 def bench_e2e(sm, scene, torch, steps):
@@ -411,6 +419,9 @@ def main():
                     help="dambreak: the headline line; sweep: the batched 256-scene parameter sweep; "
                          "calibration: forward + adjoint of the column collapse")
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the sweep workload")
+    ap.add_argument("--shapes", default=None,
+                    help='mixed-stage shapes as JSON (e.g. the "autotune" field of an earlier line) instead of '
+                         'autotuning')
     ap.add_argument("--settle", type=int, default=0,
                     help="untimed GPU settling steps behind a gate before timing (0: time the deterministic "
                          "initial packing, the same input the reference arm times)")
@@ -464,7 +475,10 @@ def main():
     sm64, _, r64 = bench_precision(scene, T.XDEM_FP64, args.steps, warmup, torch, local)
     sm64.close()
     sampler = ClockSampler(local)
-    smx, stream, rmx = bench_precision(scene, T.XDEM_MIXED, args.steps, warmup, torch, local, sampler)
+    shapes = None
+    if args.shapes:
+        shapes = {k: int(v) for k, v in json.loads(args.shapes).items() if k in T.Tune.SHAPE}
+    smx, stream, rmx = bench_precision(scene, T.XDEM_MIXED, args.steps, warmup, torch, local, sampler, shapes)
     clocks = sampler.summary()
     e2e = bench_e2e(smx, scene, torch, min(args.steps, 200))
     smx.close()
@@ -504,6 +518,7 @@ def main():
         "clocks": clocks,
         "gpu_launches": rmx["launches"],
         "autotune": rmx["tune"],
+        "list_rebuilds": rmx["list_rebuilds"],
         "status": {"fp64": r64["status"], "mixed": rmx["status"]},
     }
     if not args.no_cpu:

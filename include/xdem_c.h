@@ -445,6 +445,9 @@ XDEM_API int xdem_sim_get_tune(xdem_sim* sim, xdem_tune* tune);
  * launcher-path handles have nothing to tune: *best is their fixed shape. */
 XDEM_API int xdem_sim_autotune(xdem_sim* sim, unsigned int trial_steps, xdem_tune* best, xdem_tune* all,
                                unsigned int* nall);
+/* Candidate-list rebuilds triggered by motion since the handle's tables were
+ * made (the build on the first step after a state change is not counted). */
+XDEM_API int xdem_sim_list_rebuilds(xdem_sim* sim, unsigned int* rebuilds);
 
 /* ------------------------------------------------------------------------ */
 /* Adjoint of the FP64 trajectory (reverse mode, checkpointed)              */

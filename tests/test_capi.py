@@ -66,3 +66,4 @@ def test_argument_checks_need_no_gpu(L):
     assert L.xdem_sim_set_tune(None, C.byref(t)) == T.XDEM_ERR_ARG
     assert L.xdem_sim_get_tune(None, C.byref(t)) == T.XDEM_ERR_ARG
     assert L.xdem_sim_autotune(None, 5, C.byref(t), None, None) == T.XDEM_ERR_ARG
+    assert L.xdem_sim_list_rebuilds(None, None) == T.XDEM_ERR_ARG

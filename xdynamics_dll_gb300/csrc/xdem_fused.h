@@ -82,6 +82,12 @@ struct MixedTune {
 };
 // Candidates a sphere's list holds; a sphere with more walks the stencil.
 constexpr unsigned int kListCap = 24;
+// Blocks per body of the wrench reduction.
+constexpr unsigned int kWrenchChunks = 32;
+// Words of the candidate-list flags: rebuild this step, a sphere moved more
+// than half the skin (this step), rebuilds counted, a list overflowed at the
+// last build, the cell sort is needed this step (rebuild or overflow).
+enum { kVlRebuild = 0, kVlMoved = 1, kVlCount = 2, kVlOverflow = 3, kVlSort = 4, kVlWords = 5 };
 
 struct FusedState {
     MixedTune tune;
@@ -115,8 +121,12 @@ struct FusedState {
     unsigned int* vl_ids = nullptr;  // [np * kListCap]
     unsigned int* vl_cnt = nullptr;  // [np]
     float* vl_xb = nullptr;          // [np*4]
-    unsigned int* vl_flag = nullptr; // [2]
+    unsigned int* vl_flag = nullptr; // [kVlWords], indices kVl* below
     bool any_coh = false;            // cohesion in a particle-pair material (no lists)
+    // body wrench reduction: per-chunk sums and per-body finish counters
+    double* wsum = nullptr;          // [wsum_cap * kWrenchChunks * 6]
+    unsigned int* wcnt = nullptr;    // [wsum_cap]
+    unsigned int wsum_cap = 0;
     MatF* d_mpf = nullptr;      // FP32 material table (scenes' particle pairs, then bodies)
     size_t mpf_cap = 0;
     unsigned int* pp_count2 = nullptr;
@@ -228,8 +238,7 @@ struct ContactLaunch {
     unsigned int* vl_ids;
     unsigned int* vl_cnt;
     float* vl_xb;
-    const unsigned int* vl_in;  // nonzero: this step rebuilds (walk)
-    unsigned int* vl_out;       // set when a sphere moved beyond half the skin
+    unsigned int* vl_flag;      // [kVlWords]: see FusedState
     float skin_f, half_skin2_f;
     const PlaneF* planef;
     const PlaneDF* planedf;

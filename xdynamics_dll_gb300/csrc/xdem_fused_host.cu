@@ -155,12 +155,14 @@ __global__ void k_reorder_fp64(const unsigned int* sk, const unsigned int* sv, u
 }
 
 // Mixed form: cell ranges and the FP32 records permuted into sorted order.
-__global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, unsigned int n, unsigned int np,
+__global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk, const unsigned int* sv,
+                                unsigned int n, unsigned int np,
                                 unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index,
                                 unsigned int* skey, const float4* rA, const float4* rL, const float4* rB,
                                 const float4* rC, const unsigned int* rT, float4* mA, float4* mL, float4* mB,
                                 float4* mC, uint2* mIT)
 {
+    if (gate && !*gate) return;
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const unsigned int k = sk[s];
@@ -180,22 +182,50 @@ __global__ void k_reorder_mixed(const unsigned int* sk, const unsigned int* sv, 
     }
 }
 
-// One block of 256 threads per (body, component): sum of the contact
-// kernel's per-block partials.
-__global__ void k_body_sums(const double* bsums, unsigned int nblocks, double* wrench)
+// Sum of the contact kernel's per-block wrench partials, kWrenchChunks
+// blocks of 256 threads per body: each block sums one contiguous chunk of
+// partial rows (6 doubles a row, read whole, so a warp reads contiguous
+// memory), the last block of a body to finish adds the chunk sums in chunk
+// order.  The order of every addition is fixed: the result does not depend
+// on which block finishes last.
+__global__ void k_body_sums(const double* bsums, unsigned int nblocks, double* wrench, double* chunk,
+                            unsigned int* done)
 {
-    __shared__ double sm[8];
-    const unsigned int b = blockIdx.x / 6, c = blockIdx.x % 6;
-    double s = 0.0;
-    for (unsigned int i = threadIdx.x; i < nblocks; i += blockDim.x) s += bsums[((size_t)b * nblocks + i) * 6 + c];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < 8; ++w) t += sm[w];
-        wrench[b * 6 + c] = t;
+    __shared__ double sm[8 * 6];
+    __shared__ bool last;
+    const unsigned int b = blockIdx.x / kWrenchChunks, q = blockIdx.x % kWrenchChunks;
+    const unsigned int per = (nblocks + kWrenchChunks - 1) / kWrenchChunks;
+    const unsigned int i0 = q * per, i1 = min(nblocks, i0 + per);
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (unsigned int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const double* r = bsums + ((size_t)b * nblocks + i) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s[c] += r[c];
     }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_down_sync(0xffffffffu, s[c], o);
+        if ((threadIdx.x & 31) == 0) sm[(threadIdx.x >> 5) * 6 + c] = s[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += sm[w * 6 + threadIdx.x];
+        chunk[((size_t)b * kWrenchChunks + q) * 6 + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done + b, 1u) == kWrenchChunks - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (unsigned int k = 0; k < kWrenchChunks; ++k)
+            t += __ldcg(chunk + ((size_t)b * kWrenchChunks + k) * 6 + threadIdx.x);
+        wrench[b * 6 + threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) done[b] = 0u;  // ready for the next step
 }
 
 __global__ void k_energy(const double* vel, const double* ep, const double* ev, const double* mass,
@@ -312,7 +342,8 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.vl_ids, (size_t)np * kListCap);
         if (e == cudaSuccess) e = dalloc(fs.vl_cnt, np);
         if (e == cudaSuccess) e = dalloc(fs.vl_xb, (size_t)np * 4);
-        if (e == cudaSuccess) e = dalloc(fs.vl_flag, 2);
+        if (e == cudaSuccess) e = dalloc(fs.vl_flag, kVlWords);
+        if (e == cudaSuccess) e = cudaMemsetAsync(fs.vl_flag, 0, kVlWords * sizeof(unsigned int), st);
     } else {
         if (e == cudaSuccess) e = dalloc(fs.snap_pos, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.snap_vel, (size_t)nentry * 4);
@@ -336,7 +367,7 @@ void fused_free(FusedState& fs)
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
                   fs.mC, fs.mIT, fs.rA, fs.rL, fs.rB, fs.rC, fs.rT, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
                   fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag,
-                  fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf};
+                  fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf, fs.wsum, fs.wcnt};
     for (void* q : ps)
         if (q) cudaFree(q);
     fs = FusedState{};
@@ -408,6 +439,13 @@ int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned i
     fs.mp = mp;
     for (int i = 0; i < 3; ++i) fs.origin[i] = origin[i];
     if (nmp < nscene + nplane) return XDEM_ERR_ARG;
+    const unsigned int nbody = nmp - nscene;
+    if (nbody > fs.wsum_cap) {
+        if (dalloc(fs.wsum, (size_t)nbody * kWrenchChunks * 6) != cudaSuccess || dalloc(fs.wcnt, nbody) != cudaSuccess)
+            return XDEM_ERR_ALLOC;
+        if (cudaMemsetAsync(fs.wcnt, 0, nbody * sizeof(unsigned int), st) != cudaSuccess) return XDEM_ERR_CUDA;
+        fs.wsum_cap = nbody;
+    }
     if (nmp > fs.mpf_cap) {
         if (dalloc(fs.d_mpf, nmp) != cudaSuccess) return XDEM_ERR_ALLOC;
         fs.mpf_cap = nmp;
@@ -503,8 +541,10 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         fs.frame_margin = (float)(16.0 * (R + o_len) * std::ldexp(1.0, -24) + 1e-9);
         // the first step after priming builds the candidate lists
         if (fs.vl_flag) {
-            ok(cudaMemsetAsync(fs.vl_flag, 1, sizeof(unsigned int), st));
-            ok(cudaMemsetAsync(fs.vl_flag + 1, 0, sizeof(unsigned int), st));
+            ok(cudaMemsetAsync(fs.vl_flag + kVlRebuild, 1, sizeof(unsigned int), st));
+            ok(cudaMemsetAsync(fs.vl_flag + kVlMoved, 0, sizeof(unsigned int), st));
+            ok(cudaMemsetAsync(fs.vl_flag + kVlOverflow, 0, sizeof(unsigned int), st));
+            ok(cudaMemsetAsync(fs.vl_flag + kVlSort, 1, sizeof(unsigned int), st));
         }
         fs.primed = true;
     }
@@ -518,13 +558,19 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     for (unsigned int m = 0; m < a.nmesh; ++m)
         ok(launch_hash(a.prm, a.k0, a.v0, a.tri_sphere + 4 * (size_t)a.mesh_first[m], np + a.mesh_first[m],
                        a.mesh_ntri[m], a.status, st));
-    if (fs.have_prev) ok(launch_clear_cells(fs.skey_prev, n, a.cstart, a.cend, st));
+    // With candidate lists the cell sort is only read by the stencil walk of
+    // a rebuild step (or of a sphere whose list overflowed at the last
+    // build): the device skips the clear, sort and reorder otherwise.
+    const bool use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && a.nmesh == 0 && !fs.any_coh && fs.vl_flag;
+    const unsigned int* sort_gate = use_list ? fs.vl_flag + kVlSort : nullptr;
+    if (fs.have_prev) ok(launch_clear_cells(fs.skey_prev, n, a.cstart, a.cend, st, sort_gate));
     unsigned int *sk = nullptr, *sv = nullptr;
-    ok(radix_sort_pairs(a.k0, a.v0, a.k1, a.v1, a.hist, n, a.sort_bits, &sk, &sv, st));
+    ok(radix_sort_pairs(a.k0, a.v0, a.k1, a.v1, a.hist, n, a.sort_bits, &sk, &sv, st, sort_gate));
     nl += 3 * ((a.sort_bits + 7) / 8) - 1;
     if (fs.mixed) {
         k_reorder_mixed<<<blocks_for(n), kThreads, 0, st>>>(
-            sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev, reinterpret_cast<const float4*>(fs.rA),
+            sort_gate, sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev,
+            reinterpret_cast<const float4*>(fs.rA),
             reinterpret_cast<const float4*>(fs.rL), reinterpret_cast<const float4*>(fs.rB),
             reinterpret_cast<const float4*>(fs.rC), fs.rT, reinterpret_cast<float4*>(fs.mA),
             reinterpret_cast<float4*>(fs.mL), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
@@ -549,9 +595,9 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.mA = fs.mA; c.mL = fs.mL; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
     c.rA = fs.rA; c.rL = fs.rL; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
     c.fA = fs.fA; c.fB = fs.fB; c.fC = fs.fC;
-    c.use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && a.nmesh == 0 && !fs.any_coh && fs.vl_flag;
+    c.use_list = use_list;
     c.vl_ids = fs.vl_ids; c.vl_cnt = fs.vl_cnt; c.vl_xb = fs.vl_xb;
-    c.vl_in = fs.vl_flag; c.vl_out = fs.vl_flag ? fs.vl_flag + 1 : nullptr;
+    c.vl_flag = fs.vl_flag;
     c.skin_f = fs.tune.skin_div ? (float)(a.prm.cell_size / fs.tune.skin_div) : 0.f;
     c.half_skin2_f = 0.25f * c.skin_f * c.skin_f;
     c.mpf = fs.d_mpf;
@@ -595,11 +641,12 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     if (e0) cudaEventRecord(e0, st);
     ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
     // the mixed contact stage is two kernels (pairs, bodies), with candidate
-    // lists four (stencil walk, list pairs, bodies, flag roll)
-    if (fs.mixed) nl += c.use_list ? 3 : 1;
+    // lists three (list pairs, bodies, flag roll)
+    if (fs.mixed) nl += c.use_list ? 2 : 1;
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody && c.nscene == 1) {  // batched handles keep no body wrenches
-        k_body_sums<<<a.nbody * 6, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench);
+        if (a.nbody > fs.wsum_cap) return XDEM_ERR_ARG;  // fused_set_bodies sizes the chunk sums
+        k_body_sums<<<a.nbody * kWrenchChunks, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench, fs.wsum, fs.wcnt);
         ok(cudaGetLastError());
     }
     if (e != cudaSuccess) return XDEM_ERR_CUDA;

@@ -430,6 +430,7 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
     }
     c.pp_count_new[oid] = cnt;
     if (build) {
+        if (nlist > kListCap) atomicOr(c.vl_flag + kVlOverflow, 1u);
         c.vl_cnt[oid] = nlist;
         reinterpret_cast<float4*>(c.vl_xb)[oid] =
             make_float4((float)ux * cs + Ai.x, (float)uy * cs + Ai.y, (float)uz * cs + Ai.z, 0.f);
@@ -883,7 +884,7 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
         const float dx = (float)(cell[0] & 2047) * c.cs_f + A[0].hi - xb.x;
         const float dy = (float)(cell[1] & 2047) * c.cs_f + A[1].hi - xb.y;
         const float dz = (float)(cell[2] & 1023) * c.cs_f + A[2].hi - xb.z;
-        if (!(dx * dx + dy * dy + dz * dz < c.half_skin2_f)) atomicOr(c.vl_out, 1u);
+        if (!(dx * dx + dy * dy + dz * dz < c.half_skin2_f)) atomicOr(c.vl_flag + kVlMoved, 1u);
     }
     if (bits) atomicOr(c.status, bits);
 }
@@ -935,10 +936,6 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     __shared__ float smf[(NT / 32) * 6 * 2];
     __shared__ unsigned int stage[STAGE * NT];                // p2p candidates, [slot][thread]
     __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
-    // with candidate lists the walk runs only on rebuild steps (a uniform
-    // branch); k_mixed_pairs_list does the other steps
-    const bool build = c.use_list;
-    if (build && !*c.vl_in) return;
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned int oid = 0xffffffffu;
     if (s < c.nentry) oid = c.sorted_index[s];
@@ -970,7 +967,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     // ------------------------------------------------ particle-particle (impl:613-733)
     if (live && c.has_pp)
         p2p_mixed<NT, STAGE>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
-                             bits, build);
+                             bits);
 
     // ------------------------------------------------ triangle meshes (impl:1930-2109)
     if (MESH) {
@@ -990,16 +987,17 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     if (bits) atomicOr(c.status, bits);
 }
 
-// Kernel 1 on the steps between list rebuilds: one thread per sphere in
-// original order, particle-particle contact from the sphere's candidate list
-// (a sphere whose list overflowed walks the stencil).  Writes the same sums
-// as k_mixed_pairs for kernel 2.
+// Kernel 1 with candidate lists: one thread per sphere in original order.
+// On a rebuild step every sphere walks the stencil and records its list;
+// otherwise its contacts come from the list (a sphere whose list overflowed
+// walks; the cell sort is kept up to date for it).  Writes the same sums as
+// k_mixed_pairs for kernel 2.
 template <unsigned int NT, unsigned int OCC>
 __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
 {
     __shared__ unsigned int stage[16 * NT];                   // walk fallback candidates, [slot][thread]
     __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
-    if (*c.vl_in) return;  // a rebuild step: k_mixed_pairs walks
+    const bool rebuild = c.vl_flag[kVlRebuild] != 0u;
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
     if (oid >= c.np) return;
     const float4 Ai = reinterpret_cast<const float4*>(c.rA)[oid];
@@ -1011,14 +1009,14 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_
     acc.tm = v3<float>(0.f, 0.f, 0.f);
     acc.rs = 0.f;
     unsigned int bits = 0;
-    if (c.vl_cnt[oid] <= kListCap) {
+    if (!rebuild && c.vl_cnt[oid] <= kListCap) {
         p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, acc, bits);
     } else {
         const device_dem_parameters& p = c.prm;
         const unsigned int gx = (Ti & 2047u) & (p.grid_size.x - 1), gy = ((Ti >> 11) & 2047u) & (p.grid_size.y - 1);
         const unsigned int gz = (Ti >> 22) & (p.grid_size.z - 1);
         p2p_mixed<NT, 16>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
-                          bits);
+                          bits, rebuild);
     }
     reinterpret_cast<float4*>(c.fA)[oid] = make_float4(acc.f[0].value(), acc.f[1].value(), acc.f[2].value(), acc.rs);
     reinterpret_cast<float4*>(c.fB)[oid] = make_float4(acc.m[0].value(), acc.m[1].value(), acc.m[2].value(), 0.f);
@@ -1027,11 +1025,19 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_
 }
 
 // After kernel 2: this step's "moved too far" flag becomes the next step's
-// rebuild flag.
+// rebuild flag (a rebuild also clears the overflow mark its build will
+// set again if needed), and the next step's sort is needed on a rebuild or
+// while a list overflowed.
 __global__ void k_vl_roll(unsigned int* flag)
 {
-    flag[0] = flag[1];
-    flag[1] = 0u;
+    const unsigned int moved = flag[kVlMoved];
+    flag[kVlRebuild] = moved;
+    if (moved) {
+        flag[kVlCount] += 1u;
+        flag[kVlOverflow] = 0u;
+    }
+    flag[kVlSort] = moved | flag[kVlOverflow];
+    flag[kVlMoved] = 0u;
 }
 
 // Kernel 2 of the mixed step: one thread per sphere in original order, so
@@ -1205,19 +1211,16 @@ cudaError_t launch_bodies_occ(const ContactLaunch& c, cudaStream_t st)
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
 {
     if (c.nentry == 0) return cudaSuccess;
-    cudaError_t e = c.nmesh ? launch_pairs_nt<true>(c, st) : launch_pairs_nt<false>(c, st);
+    cudaError_t e = c.use_list ? launch_list_nt(c, st)
+                               : (c.nmesh ? launch_pairs_nt<true>(c, st) : launch_pairs_nt<false>(c, st));
     if (e != cudaSuccess) return e;
-    if (c.use_list) {
-        e = launch_list_nt(c, st);
-        if (e != cudaSuccess) return e;
-    }
     switch (c.tune.nt_bodies) {
     case 64: e = launch_bodies_occ<64>(c, st); break;
     case 256: e = launch_bodies_occ<256>(c, st); break;
     default: e = launch_bodies_occ<128>(c, st); break;
     }
     if (e != cudaSuccess || !c.use_list) return e;
-    k_vl_roll<<<1, 1, 0, st>>>(c.vl_out - 1);
+    k_vl_roll<<<1, 1, 0, st>>>(c.vl_flag);
     return cudaGetLastError();
 }
 

@@ -122,8 +122,10 @@ __global__ void k_cell_bounds(const unsigned int* key, const unsigned int* val, 
     sorted_index[i] = val[i];
 }
 
-__global__ void k_clear_cells(const unsigned int* key, unsigned int n, unsigned int* cstart, unsigned int* cend)
+__global__ void k_clear_cells(const unsigned int* key, unsigned int n, unsigned int* cstart, unsigned int* cend,
+                              const unsigned int* gate)
 {
+    if (gate && !*gate) return;
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const unsigned int h = key[i];
@@ -759,9 +761,9 @@ cudaError_t launch_cell_bounds(const unsigned int* skey, const unsigned int* sva
 }
 
 cudaError_t launch_clear_cells(const unsigned int* keys, unsigned int n, unsigned int* cstart, unsigned int* cend,
-                               cudaStream_t st)
+                               cudaStream_t st, const unsigned int* gate)
 {
-    XDEM_LAUNCH(k_clear_cells, n, keys, n, cstart, cend);
+    XDEM_LAUNCH(k_clear_cells, n, keys, n, cstart, cend, gate);
 }
 
 cudaError_t launch_fill_u32(unsigned int* a, unsigned int v, size_t n, cudaStream_t st)

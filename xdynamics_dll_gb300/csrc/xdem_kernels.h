@@ -34,9 +34,10 @@ cudaError_t launch_hash(const device_dem_parameters& p, unsigned int* hash, unsi
 // sorted_index = index.
 cudaError_t launch_cell_bounds(const unsigned int* skey, const unsigned int* sval, unsigned int* cstart,
                                unsigned int* cend, unsigned int* sorted_index, unsigned int n, cudaStream_t st);
-// Marks the cells listed in `keys` empty again (0xffffffff / 0).
+// Marks the cells listed in `keys` empty again (0xffffffff / 0).  With a
+// gate, only when *gate is nonzero (decided on the device).
 cudaError_t launch_clear_cells(const unsigned int* keys, unsigned int n, unsigned int* cstart, unsigned int* cend,
-                               cudaStream_t st);
+                               cudaStream_t st, const unsigned int* gate = nullptr);
 cudaError_t launch_fill_u32(unsigned int* a, unsigned int v, size_t n, cudaStream_t st);
 
 cudaError_t launch_p2p(const device_dem_parameters& p, const double* pos, const double* ep, const double* vel,
@@ -111,10 +112,12 @@ int launcher_set_status(int s);
 // ---------------------------------------------------------------- radix sort
 // Stable LSD sort of (keys, vals) by the low `bits` bits of the keys.  Uses
 // ping-pong buffers k1/v1 (n each) and `hist` (radix_hist_size(n) uints).
-// The sorted result ends in the buffers returned through out_k/out_v.
+// The sorted result ends in the buffers returned through out_k/out_v.  With
+// a gate the kernels do nothing unless *gate is nonzero (a device-side skip
+// that keeps the launch sequence fixed, for CUDA graphs).
 size_t radix_hist_size(unsigned int n);
 cudaError_t radix_sort_pairs(unsigned int* k0, unsigned int* v0, unsigned int* k1, unsigned int* v1,
                              unsigned int* hist, unsigned int n, int bits, unsigned int** out_k,
-                             unsigned int** out_v, cudaStream_t st);
+                             unsigned int** out_v, cudaStream_t st, const unsigned int* gate = nullptr);
 
 }  // namespace xdem

@@ -23,8 +23,10 @@ constexpr int kTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
 
 __global__ void __launch_bounds__(kSortThreads)
-k_radix_upsweep(const unsigned int* keys, unsigned int n, int shift, unsigned int* hist, unsigned int ntiles)
+k_radix_upsweep(const unsigned int* keys, unsigned int n, int shift, unsigned int* hist, unsigned int ntiles,
+                const unsigned int* gate)
 {
+    if (gate && !*gate) return;
     __shared__ unsigned int h[kRadix];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -65,8 +67,9 @@ __device__ __forceinline__ unsigned int block_exclusive_scan(unsigned int v, uns
 // One block per digit: exclusive scan of that digit's per-tile counts (one
 // row of the digit-major table), row total into totals[digit].
 __global__ void __launch_bounds__(kSortThreads) k_radix_scan(unsigned int* hist, unsigned int ntiles,
-                                                             unsigned int* totals)
+                                                             unsigned int* totals, const unsigned int* gate)
 {
+    if (gate && !*gate) return;
     __shared__ unsigned int sm[kSortThreads / 32];
     unsigned int* row = hist + (size_t)blockIdx.x * ntiles;
     unsigned int carry = 0;
@@ -83,8 +86,10 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scan(unsigned int* hist,
 
 __global__ void __launch_bounds__(kSortThreads)
 k_radix_scatter(const unsigned int* kin, const unsigned int* vin, unsigned int* kout, unsigned int* vout,
-                unsigned int n, int shift, const unsigned int* hist, unsigned int ntiles, const unsigned int* totals)
+                unsigned int n, int shift, const unsigned int* hist, unsigned int ntiles, const unsigned int* totals,
+                const unsigned int* gate)
 {
+    if (gate && !*gate) return;
     constexpr int kWarps = kSortThreads / 32;
     __shared__ unsigned int base[kRadix];
     __shared__ unsigned int run[kRadix];
@@ -140,7 +145,7 @@ size_t radix_hist_size(unsigned int n)
 
 cudaError_t radix_sort_pairs(unsigned int* k0, unsigned int* v0, unsigned int* k1, unsigned int* v1,
                              unsigned int* hist, unsigned int n, int bits, unsigned int** out_k,
-                             unsigned int** out_v, cudaStream_t st)
+                             unsigned int** out_v, cudaStream_t st, const unsigned int* gate)
 {
     *out_k = k0;
     *out_v = v0;
@@ -149,9 +154,9 @@ cudaError_t radix_sort_pairs(unsigned int* k0, unsigned int* v0, unsigned int* k
     unsigned int* totals = hist + (size_t)ntiles * kRadix;
     unsigned int *ki = k0, *vi = v0, *ko = k1, *vo = v1;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_radix_upsweep<<<ntiles, kSortThreads, 0, st>>>(ki, n, shift, hist, ntiles);
-        k_radix_scan<<<kRadix, kSortThreads, 0, st>>>(hist, ntiles, totals);
-        k_radix_scatter<<<ntiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, hist, ntiles, totals);
+        k_radix_upsweep<<<ntiles, kSortThreads, 0, st>>>(ki, n, shift, hist, ntiles, gate);
+        k_radix_scan<<<kRadix, kSortThreads, 0, st>>>(hist, ntiles, totals, gate);
+        k_radix_scatter<<<ntiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, hist, ntiles, totals, gate);
         unsigned int* t = ki; ki = ko; ko = t;
         t = vi; vi = vo; vo = t;
     }

@@ -195,3 +195,13 @@ XDEM_API int xdem_sim_autotune(xdem_sim* s, unsigned int trial_steps, xdem_tune*
     if (nall) *nall = (unsigned int)tried.size();
     return XDEM_OK;
 }
+
+XDEM_API int xdem_sim_list_rebuilds(xdem_sim* s, unsigned int* rebuilds)
+{
+    if (!s || !rebuilds) return XDEM_ERR_ARG;
+    *rebuilds = 0;
+    if (!s->fs.vl_flag) return XDEM_OK;
+    cudaError_t e = cudaMemcpyAsync(rebuilds, s->fs.vl_flag + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
+}

@@ -162,6 +162,12 @@ class Sim:
                    "xdem_sim_autotune")
         return best.as_dict(), [allv[i].as_dict() for i in range(cap.value)]
 
+    def list_rebuilds(self):
+        """Candidate-list rebuilds motion has triggered so far (mixed form)."""
+        n = C.c_uint()
+        _lib.check(self.L.xdem_sim_list_rebuilds(self.h, C.byref(n)), "xdem_sim_list_rebuilds")
+        return n.value
+
     def profile(self):
         nl = C.c_uint()
         ms = C.c_double()
