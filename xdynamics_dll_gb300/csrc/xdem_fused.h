@@ -80,6 +80,10 @@ struct MatF {
 struct MixedTune {
     unsigned int nt_pairs = 128, stage = 16, nt_bodies = 128, occ_pairs = 768, occ_bodies = 512, skin_div = 0;
 };
+// Record k of sphere i: rec[4 i + k] (kRecA, kRecL, kRecB, kRecC).
+enum { kRecA = 0, kRecL = 1, kRecB = 2, kRecC = 3 };
+__device__ __forceinline__ unsigned int rec_cell(float4 C) { return __float_as_uint(C.w); }
+
 // Candidates a sphere's list holds; a sphere with more walks the stencil.
 constexpr unsigned int kListCap = 24;
 // Blocks per body of the wrench reduction.
@@ -108,11 +112,11 @@ struct FusedState {
     float* mB = nullptr;        // [nentry*4] vx, vy, vz, mass
     float* mC = nullptr;        // [nentry*4] wx, wy, wz, 0
     unsigned int* mIT = nullptr; // [nentry*2] (original id, packed unwrapped cell)
-    float* rA = nullptr;        // [np*4] next-step records written by the contact kernel
-    float* rL = nullptr;
-    float* rB = nullptr;
-    float* rC = nullptr;
-    unsigned int* rT = nullptr; // [np]
+    // next-step records written by the contact kernel, one 64-byte record
+    // per sphere in original order: A (cell offsets, radius), L (their low
+    // parts), B (velocity, mass), C (spin, packed cell bits in w) -- a
+    // neighbour's record is two sectors
+    float4* rec = nullptr;      // [np*4]
     float* fA = nullptr;        // [np*4] particle-particle force, rolling resistance (original order)
     float* fB = nullptr;        // [np*4] particle-particle moment
     float* fC = nullptr;        // [np*4] rolling: sum of contact moments
@@ -225,14 +229,10 @@ struct ContactLaunch {
     const float* mB;
     const float* mC;
     const unsigned int* mIT;
-    float* rA;
-    float* rL;
+    float4* rec;  // [np*4] records (see FusedState)
     float* fA;
     float* fB;
     float* fC;
-    float* rB;
-    float* rC;
-    unsigned int* rT;
     // candidate lists (use_list): see FusedState
     bool use_list;
     unsigned int* vl_ids;

@@ -53,7 +53,7 @@ __device__ __forceinline__ int3v mixed_record(const device_dem_parameters& p, do
 __global__ void k_prologue(device_dem_parameters p, const double* pos, const double* ep, const double* vel,
                            const double* ev, const double* acc, const double* ea, const double* mass,
                            double* pos_next, double* ep_next, unsigned int* key, unsigned int* val, unsigned int n,
-                           unsigned int* status, float* rA, float* rL, float* rB, float* rC, unsigned int* rT)
+                           unsigned int* status, float4* rec)
 {
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -69,16 +69,16 @@ __global__ void k_prologue(device_dem_parameters p, const double* pos, const dou
     st4(pos_next, i, mk4(x.x, x.y, x.z, q.w));
     if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(status, (unsigned int)XDEM_ERR_NONFINITE);
     int3v g;
-    if (rA) {
+    if (rec) {
         // mixed form: the key's cell is the cell the FP32 record is relative to
         float4 A, L, B, C;
         unsigned int T;
         g = mixed_record(p, 1.0 / p.cell_size, x, q.w, v, mass[i], ang_vel(en, ld4(ev, i)), A, L, B, C, T);
-        reinterpret_cast<float4*>(rA)[i] = A;
-        reinterpret_cast<float4*>(rL)[i] = L;
-        reinterpret_cast<float4*>(rB)[i] = B;
-        reinterpret_cast<float4*>(rC)[i] = C;
-        rT[i] = T;
+        C.w = __uint_as_float(T);
+        rec[4 * (size_t)i + kRecA] = A;
+        rec[4 * (size_t)i + kRecL] = L;
+        rec[4 * (size_t)i + kRecB] = B;
+        rec[4 * (size_t)i + kRecC] = C;
     } else {
         g = grid_pos(p, x);
     }
@@ -158,8 +158,7 @@ __global__ void k_reorder_fp64(const unsigned int* sk, const unsigned int* sv, u
 __global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk, const unsigned int* sv,
                                 unsigned int n, unsigned int np,
                                 unsigned int* cstart, unsigned int* cend, unsigned int* sorted_index,
-                                unsigned int* skey, const float4* rA, const float4* rL, const float4* rB,
-                                const float4* rC, const unsigned int* rT, float4* mA, float4* mL, float4* mB,
+                                unsigned int* skey, const float4* rec, float4* mA, float4* mL, float4* mB,
                                 float4* mC, uint2* mIT)
 {
     if (gate && !*gate) return;
@@ -171,11 +170,13 @@ __global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk
     sorted_index[s] = oid;
     skey[s] = k;
     if (oid < np) {
-        mA[s] = rA[oid];
-        mL[s] = rL[oid];
-        mB[s] = rB[oid];
-        mC[s] = rC[oid];
-        mIT[s] = make_uint2(oid, rT[oid]);
+        const float4* r = rec + 4 * (size_t)oid;
+        mA[s] = r[kRecA];
+        mL[s] = r[kRecL];
+        mB[s] = r[kRecB];
+        const float4 C = r[kRecC];
+        mC[s] = C;
+        mIT[s] = make_uint2(oid, rec_cell(C));
     } else {
         mA[s] = make_float4(0.f, 0.f, 0.f, -1.f);
         mIT[s] = make_uint2(oid, 0xffffffffu);
@@ -331,14 +332,11 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.mB, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mC, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mIT, (size_t)nentry * 2);
-        if (e == cudaSuccess) e = dalloc(fs.rA, (size_t)np * 4);
-        if (e == cudaSuccess) e = dalloc(fs.rL, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.rec, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.fA, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.fB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.fC, (size_t)np * 4);
-        if (e == cudaSuccess) e = dalloc(fs.rB, (size_t)np * 4);
-        if (e == cudaSuccess) e = dalloc(fs.rC, (size_t)np * 4);
-        if (e == cudaSuccess) e = dalloc(fs.rT, np);
+
         if (e == cudaSuccess) e = dalloc(fs.vl_ids, (size_t)np * kListCap);
         if (e == cudaSuccess) e = dalloc(fs.vl_cnt, np);
         if (e == cudaSuccess) e = dalloc(fs.vl_xb, (size_t)np * 4);
@@ -365,7 +363,7 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 void fused_free(FusedState& fs)
 {
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
-                  fs.mC, fs.mIT, fs.rA, fs.rL, fs.rB, fs.rC, fs.rT, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
+                  fs.mC, fs.mIT, fs.rec, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
                   fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag,
                   fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf, fs.wsum, fs.wcnt};
     for (void* q : ps)
@@ -509,8 +507,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         ok(cudaMemsetAsync(a.cend, 0, a.ncell * sizeof(unsigned int), st));
         fs.have_prev = false;
         k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, a.mass,
-                                                        fs.pos_alt, fs.ep_alt, a.k0, a.v0, np, a.status, fs.rA,
-                                                        fs.rL, fs.rB, fs.rC, fs.rT);
+                                                        fs.pos_alt, fs.ep_alt, a.k0, a.v0, np, a.status, fs.rec);
         ok(cudaGetLastError());
         const unsigned int nbb = std::min(kBboxBlocks, std::max(1u, blocks_for(np, 256)));
         k_bbox<<<nbb, 256, 0, st>>>(*a.pos, np, fs.d_bbox);
@@ -570,9 +567,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     if (fs.mixed) {
         k_reorder_mixed<<<blocks_for(n), kThreads, 0, st>>>(
             sort_gate, sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev,
-            reinterpret_cast<const float4*>(fs.rA),
-            reinterpret_cast<const float4*>(fs.rL), reinterpret_cast<const float4*>(fs.rB),
-            reinterpret_cast<const float4*>(fs.rC), fs.rT, reinterpret_cast<float4*>(fs.mA),
+            fs.rec, reinterpret_cast<float4*>(fs.mA),
             reinterpret_cast<float4*>(fs.mL), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
             reinterpret_cast<uint2*>(fs.mIT));
     } else {
@@ -593,7 +588,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.snap_pos = fs.snap_pos; c.snap_vel = fs.snap_vel; c.snap_om = fs.snap_om; c.snap_f = fs.snap_f;
     c.margin = fs.frame_margin;
     c.mA = fs.mA; c.mL = fs.mL; c.mB = fs.mB; c.mC = fs.mC; c.mIT = fs.mIT;
-    c.rA = fs.rA; c.rL = fs.rL; c.rB = fs.rB; c.rC = fs.rC; c.rT = fs.rT;
+    c.rec = fs.rec;
     c.fA = fs.fA; c.fB = fs.fB; c.fC = fs.fC;
     c.use_list = use_list;
     c.vl_ids = fs.vl_ids; c.vl_cnt = fs.vl_cnt; c.vl_xb = fs.vl_xb;

@@ -467,7 +467,7 @@ __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oi
     for (unsigned int q = 0; q < n; ++q) {
         const unsigned int k = ids[q];
         if (c.scene_of && c.scene_of[k] != scene) continue;  // another scene of the batch
-        const unsigned int Tk = c.rT[k];
+        const unsigned int Tk = rec_cell(c.rec[4 * (size_t)k + kRecC]);
         const unsigned int xs = (Tk - ux + 1u) & 2047u;
         const unsigned int ys = ((Tk >> 11) - uy + 1u) & 2047u;
         const unsigned int zs = ((Tk >> 22) - uz + 1u) & 1023u;
@@ -485,12 +485,10 @@ __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oi
     unsigned int cnt = 0;
     for (unsigned int q = 0; q < nk; ++q) {
         const unsigned int k = (unsigned int)key[q];
-        const float4 Aj = reinterpret_cast<const float4*>(c.rA)[k];
-        const float4 Lj = reinterpret_cast<const float4*>(c.rL)[k];
-        const float4 Bj = reinterpret_cast<const float4*>(c.rB)[k];
-        const float4 Cj = reinterpret_cast<const float4*>(c.rC)[k];
-        p2p_pair_rec<NT>(c, k, c.rT[k], Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene, coh,
-                         Ft, Fn, cnt, acc, bits);
+        const float4* r = c.rec + 4 * (size_t)k;
+        const float4 Aj = r[kRecA], Lj = r[kRecL], Bj = r[kRecB], Cj = r[kRecC];
+        p2p_pair_rec<NT>(c, k, rec_cell(Cj), Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
+                         coh, Ft, Fn, cnt, acc, bits);
     }
     c.pp_count_new[oid] = cnt;
 }
@@ -872,11 +870,11 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
     c.k_out[oid] = grid_hash(p, cell[0], cell[1], cell[2]);
     c.v_out[oid] = oid;
     const float3 w = ang_vel_f(en, evn);
-    reinterpret_cast<float4*>(c.rA)[oid] = make_float4(A[0].hi, A[1].hi, A[2].hi, Ai.w);
-    reinterpret_cast<float4*>(c.rL)[oid] = make_float4(A[0].lo, A[1].lo, A[2].lo, Li.w);
-    reinterpret_cast<float4*>(c.rB)[oid] = make_float4(vn.x, vn.y, vn.z, Bi.w);
-    reinterpret_cast<float4*>(c.rC)[oid] = make_float4(w.x, w.y, w.z, 0.f);
-    c.rT[oid] = pack_cell(cell[0], cell[1], cell[2]);
+    float4* r = c.rec + 4 * (size_t)oid;
+    r[kRecA] = make_float4(A[0].hi, A[1].hi, A[2].hi, Ai.w);
+    r[kRecL] = make_float4(A[0].lo, A[1].lo, A[2].lo, Li.w);
+    r[kRecB] = make_float4(vn.x, vn.y, vn.z, Bi.w);
+    r[kRecC] = make_float4(w.x, w.y, w.z, __uint_as_float(pack_cell(cell[0], cell[1], cell[2])));
     if (c.use_list) {
         // distance from the centre at the last list build, in the lists'
         // frame (packed cell times cell size plus the offset)
@@ -1000,11 +998,9 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_
     const bool rebuild = c.vl_flag[kVlRebuild] != 0u;
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
     if (oid >= c.np) return;
-    const float4 Ai = reinterpret_cast<const float4*>(c.rA)[oid];
-    const float4 Li = reinterpret_cast<const float4*>(c.rL)[oid];
-    const float4 Bi = reinterpret_cast<const float4*>(c.rB)[oid];
-    const float4 Ci = reinterpret_cast<const float4*>(c.rC)[oid];
-    const unsigned int Ti = c.rT[oid];
+    const float4* r = c.rec + 4 * (size_t)oid;
+    const float4 Ai = r[kRecA], Li = r[kRecL], Bi = r[kRecB], Ci = r[kRecC];
+    const unsigned int Ti = rec_cell(Ci);
     Acc acc;
     acc.tm = v3<float>(0.f, 0.f, 0.f);
     acc.rs = 0.f;
@@ -1057,10 +1053,11 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     acc.tm = v3<float>(0.f, 0.f, 0.f);
     acc.rs = 0.f;
     if (live) {
-        Ai = reinterpret_cast<const float4*>(c.rA)[oid];
-        Li = reinterpret_cast<const float4*>(c.rL)[oid];
-        Bi = reinterpret_cast<const float4*>(c.rB)[oid];
-        Ci = reinterpret_cast<const float4*>(c.rC)[oid];
+        const float4* r = c.rec + 4 * (size_t)oid;
+        Ai = r[kRecA];
+        Li = r[kRecL];
+        Bi = r[kRecB];
+        Ci = r[kRecC];
         ip = ld4(c.pos_cur, oid);
         const float4 fa = reinterpret_cast<const float4*>(c.fA)[oid];
         const float4 fb = reinterpret_cast<const float4*>(c.fB)[oid];
