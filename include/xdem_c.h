@@ -397,6 +397,17 @@ XDEM_API int xdem_sim_set_pairs(xdem_sim* sim, int kind,
                                 const unsigned int* ids, const double* tsd);
 /* Kinetic energy (translational + rotational) and stored contact count. */
 XDEM_API int xdem_sim_energy(xdem_sim* sim, double* ke, unsigned int* ncontact);
+/* Part files (xResultManager::export_step_data_to_file,
+ * source/xdynamics_manager/xResultManager.cpp:828-903, version 2): time,
+ * counts, mass, state (and cluster centres), then the particle-pair, plane
+ * and triangle pair lists with their tangential history, for the contact
+ * kinds the handle has.  No multibody block: the handle's bodies are posed by
+ * the caller.  load_part checks the counts and the file size against the
+ * handle and restores the state and every pair list, history included (the
+ * reference's resume leaves the lists empty, xContactManager.cpp:316-322);
+ * the inertia stays the handle's. */
+XDEM_API int xdem_sim_save_part(xdem_sim* sim, const char* path, double time);
+XDEM_API int xdem_sim_load_part(xdem_sim* sim, const char* path, double* time);
 /* Status bits accumulated since the last call. */
 XDEM_API int xdem_sim_status(xdem_sim* sim);
 /* Stream the handle's kernels run on (cudaStream_t).  The stream stays the

@@ -74,6 +74,8 @@ _SIGS = {
     "xdem_sim_get_tune": ([vp, vp], i32),
     "xdem_sim_autotune": ([vp, u32, vp, vp, vp], i32),
     "xdem_sim_list_rebuilds": ([vp, vp], i32),
+    "xdem_sim_save_part": ([vp, C.c_char_p, f64], i32),
+    "xdem_sim_load_part": ([vp, C.c_char_p, vp], i32),
     "xdem_adj_create": ([vp, u32, vp], i32),
     "xdem_adj_destroy": ([vp], i32),
     "xdem_adj_forward": ([vp, u32], i32),

@@ -32,6 +32,7 @@ UNITS = {
     "xdem_noalloc.cu": [],
     "xdem_adjoint.cu": ["-fmad=false"],
     "xdem_tune.cu": [],
+    "xdem_io.cu": [],
 }
 
 

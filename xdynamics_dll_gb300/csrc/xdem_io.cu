@@ -1,0 +1,142 @@
+// xdem_io.cu -- part files of a scene handle: the state and the pair lists
+// with their tangential history, in the layout xResultManager::
+// export_step_data_to_file writes (source/xdynamics_manager/
+// xResultManager.cpp:828-903, version 2):
+//
+//   double   time
+//   uint32   np, ns                         (spheres, clusters; ns == np: free spheres)
+//   double   mass[ns]
+//   double   pos[np*4], vel[ns*3], acc[ns*3], ep[ns*4], ev[ns*4], ea[ns*4]
+//   double   cpos[ns*4]                     (clusters only)
+//   uint32   p2p count[np], id[np*12]; double p2p tsd[np*24]    (particle pairs)
+//   uint32   p2pl count[np], id[np*3]; double p2pl tsd[np*6]    (planes)
+//   uint32   p2tri count[np], id[np*5]; double p2tri tsd[np*10] (meshes)
+//
+// little-endian, no padding.  The reference writes the pair blocks of the
+// contact kinds the model has, and a multibody block between the state and
+// the pairs when the model has one; a handle has no multibody system (its
+// bodies are posed by the caller), so it writes and reads none.  Loading a
+// part file restores the pair lists and their history, which the
+// reference's resume leaves empty (xContactManager.cpp:316-322).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "xdem_sim_impl.h"
+
+namespace {
+
+struct File {
+    FILE* f = nullptr;
+    explicit File(const char* path, const char* mode) : f(std::fopen(path, mode)) {}
+    ~File()
+    {
+        if (f) std::fclose(f);
+    }
+};
+
+template <class T>
+bool put(FILE* f, const std::vector<T>& v)
+{
+    return v.empty() || std::fwrite(v.data(), sizeof(T), v.size(), f) == v.size();
+}
+template <class T>
+bool get(FILE* f, std::vector<T>& v)
+{
+    return v.empty() || std::fread(v.data(), sizeof(T), v.size(), f) == v.size();
+}
+
+// The pair blocks a handle's part file holds.
+void blocks(const xdem_sim* s, bool& pp, bool& pl, bool& ms)
+{
+    pp = s->has_pp;
+    pl = !s->planes.empty();
+    ms = !s->meshes.empty();
+}
+
+}  // namespace
+
+XDEM_API int xdem_sim_save_part(xdem_sim* s, const char* path, double time)
+{
+    if (!s || !path) return XDEM_ERR_ARG;
+    if (int r = xdem_sim_step(s, 0)) return r;  // tables exist (a fresh handle saves empty lists)
+    const size_t np = s->np, ns = s->ns;
+    std::vector<double> pos(np * 4), vel(ns * 3), acc(ns * 3), ep(ns * 4), ev(ns * 4), ea(ns * 4), mass(ns),
+        cpos(s->clusters ? ns * 4 : 0);
+    if (int r = xdem_sim_get_state(s, pos.data(), vel.data(), acc.data(), ep.data(), ev.data(), ea.data(),
+                                   s->clusters ? cpos.data() : nullptr))
+        return r;
+    if (cudaMemcpy(mass.data(), s->mass, ns * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return XDEM_ERR_CUDA;
+    bool bpp, bpl, bms;
+    blocks(s, bpp, bpl, bms);
+    File out(path, "wb");
+    if (!out.f) return XDEM_ERR_ARG;
+    const unsigned int n32[2] = {(unsigned int)np, (unsigned int)ns};
+    bool ok = std::fwrite(&time, sizeof(double), 1, out.f) == 1 && std::fwrite(n32, sizeof(n32), 1, out.f) == 1;
+    ok = ok && put(out.f, mass) && put(out.f, pos) && put(out.f, vel) && put(out.f, acc) && put(out.f, ep) &&
+         put(out.f, ev) && put(out.f, ea) && put(out.f, cpos);
+    const bool want[3] = {bpp, bpl, bms};
+    const unsigned int cap[3] = {MAX_P2P_COUNT, MAX_P2PL_COUNT, MAX_P2MS_COUNT};
+    for (int kind = 0; kind < 3 && ok; ++kind) {
+        if (!want[kind]) continue;
+        std::vector<unsigned int> cnt(np), ids(np * cap[kind]);
+        std::vector<double> tsd(np * cap[kind] * 2);
+        if (int r = xdem_sim_get_pairs(s, kind, cnt.data(), ids.data(), tsd.data())) return r;
+        ok = put(out.f, cnt) && put(out.f, ids) && put(out.f, tsd);
+    }
+    return ok ? XDEM_OK : XDEM_ERR_ARG;
+}
+
+XDEM_API int xdem_sim_load_part(xdem_sim* s, const char* path, double* time)
+{
+    if (!s || !path) return XDEM_ERR_ARG;
+    File in(path, "rb");
+    if (!in.f) return XDEM_ERR_ARG;
+    double t = 0.0;
+    unsigned int n32[2] = {0, 0};
+    if (std::fread(&t, sizeof(double), 1, in.f) != 1 || std::fread(n32, sizeof(n32), 1, in.f) != 1)
+        return XDEM_ERR_ARG;
+    const size_t np = s->np, ns = s->ns;
+    if (n32[0] != np || n32[1] != ns) return XDEM_ERR_ARG;  // another model
+    std::vector<double> pos(np * 4), vel(ns * 3), acc(ns * 3), ep(ns * 4), ev(ns * 4), ea(ns * 4), mass(ns),
+        cpos(s->clusters ? ns * 4 : 0);
+    bool ok = get(in.f, mass) && get(in.f, pos) && get(in.f, vel) && get(in.f, acc) && get(in.f, ep) &&
+              get(in.f, ev) && get(in.f, ea) && get(in.f, cpos);
+    if (!ok) return XDEM_ERR_ARG;
+    bool bpp, bpl, bms;
+    blocks(s, bpp, bpl, bms);
+    const bool want[3] = {bpp, bpl, bms};
+    const unsigned int cap[3] = {MAX_P2P_COUNT, MAX_P2PL_COUNT, MAX_P2MS_COUNT};
+    std::vector<unsigned int> cnt[3], ids[3];
+    std::vector<double> tsd[3];
+    for (int kind = 0; kind < 3; ++kind) {
+        if (!want[kind]) continue;
+        cnt[kind].resize(np);
+        ids[kind].resize(np * cap[kind]);
+        tsd[kind].resize(np * cap[kind] * 2);
+        if (!(get(in.f, cnt[kind]) && get(in.f, ids[kind]) && get(in.f, tsd[kind]))) return XDEM_ERR_ARG;
+    }
+    char extra;
+    if (std::fread(&extra, 1, 1, in.f) != 0) return XDEM_ERR_ARG;  // blocks this handle has no contacts for
+    // the inertia is not in the file: the handle keeps its own
+    std::vector<double> iner(ns * 3);
+    if (cudaMemcpy(iner.data(), s->inertia, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return XDEM_ERR_CUDA;
+    if (int r = xdem_sim_set_state(s, pos.data(), vel.data(), acc.data(), ep.data(), ev.data(), ea.data(),
+                                   mass.data(), iner.data()))
+        return r;
+    if (s->clusters) {
+        if (cudaMemcpy(s->cpos, cpos.data(), cpos.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+            return XDEM_ERR_CUDA;
+    }
+    if (int r = xdem_sim_step(s, 0)) return r;  // pair tables exist before they are filled
+    for (int kind = 0; kind < 3; ++kind) {
+        if (!want[kind]) continue;
+        if (int r = xdem_sim_set_pairs(s, kind, cnt[kind].data(), ids[kind].data(), tsd[kind].data())) return r;
+    }
+    if (time) *time = t;
+    return XDEM_OK;
+}

@@ -131,6 +131,17 @@ class Sim:
         _lib.check(self.L.xdem_sim_energy(self.h, C.byref(ke), C.byref(nc)), "xdem_sim_energy")
         return ke.value, nc.value
 
+    def save_part(self, path, time=0.0):
+        """Part file of the current state and pair lists (xdynamics layout)."""
+        _lib.check(self.L.xdem_sim_save_part(self.h, str(path).encode(), float(time)), "xdem_sim_save_part")
+
+    def load_part(self, path):
+        """Restores state and pair lists (with history) from a part file;
+        returns its time."""
+        t = C.c_double()
+        _lib.check(self.L.xdem_sim_load_part(self.h, str(path).encode(), C.byref(t)), "xdem_sim_load_part")
+        return t.value
+
     def status(self):
         return self.L.xdem_sim_status(self.h)
 
