@@ -309,7 +309,8 @@ typedef struct xdem_sim xdem_sim;
 typedef struct xdem_sim_config {
     unsigned int np;          /* spheres (cluster members included)          */
     unsigned int ns;          /* clusters; 0 = free spheres (ns = np)        */
-    int precision;            /* XDEM_FP64 or XDEM_MIXED                     */
+    int precision;            /* XDEM_FP64 or XDEM_MIXED (free spheres only:
+                                 cluster handles are FP64)                   */
     int contact_model;        /* 0 DHS, 1 Hertz-Mindlin                      */
     int velocity_compat;      /* see xdem_set_velocity_compat                */
     double dt;

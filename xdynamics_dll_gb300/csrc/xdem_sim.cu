@@ -388,6 +388,9 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
 {
     if (!cfg || !out || cfg->np == 0 || !(cfg->cell_size > 0) || !(cfg->dt > 0)) return XDEM_ERR_ARG;
     if (cfg->precision != XDEM_FP64 && cfg->precision != XDEM_MIXED) return XDEM_ERR_ARG;
+    // clusters run on the launcher kernels, which are FP64 only: a mixed
+    // request is refused rather than run in another precision
+    if (cfg->precision == XDEM_MIXED && cfg->ns != 0 && cfg->ns != cfg->np) return XDEM_ERR_ARG;
     for (int i = 0; i < 3; ++i) {
         const unsigned int g = cfg->grid_size[i];
         if (!g || (g & (g - 1))) return XDEM_ERR_ARG;
