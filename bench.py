@@ -374,6 +374,164 @@ def bench_sweep(args, torch, local):
     print(json.dumps(out))
 
 
+def run_cpu_baseline_clusters(scene, budget_s=20.0, max_steps=20):
+    """The CPU oracle's cluster step (member pairs, cluster planes, cluster
+    mesh, cluster velocity update; OpenMP over particles) on the full scene
+    for as many steps as fit in `budget_s` seconds after one warm-up step."""
+    import kseq
+    import pyoracle
+    o = pyoracle.Oracle()
+    be = kseq.OracleBackend(o)
+    meshes = kseq.mesh_arrays(scene, o)
+    s = kseq.state_arrays(scene)
+    kseq.cluster_step(be, scene, s, meshes)
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        kseq.cluster_step(be, scene, s, meshes)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": scene.np_ * steps / dt, "unit": UNIT, "cores": o.threads(), "kind": "port",
+            "sample": f"{steps} steps of the full {scene.np_}-sphere cluster scene after 1 warm-up step "
+                      f"({dt:.1f} s, oracle/xdem_oracle.c, OpenMP)"}
+
+
+def bench_wheel(args, torch, local):
+    """The wheel testbed: 2,000,000 rigid clumps of three 2 mm spheres in a
+    trough (walls extended above it), a 20,480-triangle tyre driven at
+    2 rad/s resting on the bed, dt 1e-5 s.  `value` is the mixed cluster step
+    (FP32 contact geometry and forces, FP64 cluster state) with the wheel
+    held (its surface is invariant under its spin); the FP64 cluster step
+    (the reference-structured launcher kernels) runs on the same scene for
+    fewer steps.  e2e: every step re-poses the wheel (its record and the
+    triangles) and the planes from host records and reads every body's
+    wrench back, the host moving the wheel from its wrench."""
+    import ctypes as C
+    from xdynamics_dll_gb300 import scenes, sim as S, types as T
+
+    def stage(msg):
+        sys.stderr.write(f"[wheel] {msg}\n")
+        sys.stderr.flush()
+
+    sc = scenes.wheel_testbed(ncluster=args.clusters)
+    n, ns = sc.np_, sc.ns
+    stage(f"{sc.note}; grid {sc.grid}, cell {sc.cell_size * 1e3:.2f} mm")
+    warmup = max(3, args.warmup)
+    sm = S.Sim(sc, precision=T.XDEM_MIXED)
+    stream = torch.cuda.Stream(device=local)
+    sm.L.xdem_sim_set_stream(sm.h, stream.cuda_stream)
+    if args.shapes:
+        sm.set_tune(**{k: int(v) for k, v in json.loads(args.shapes).items() if k in T.Tune.SHAPE})
+        tune = sm.get_tune()
+    else:
+        tune, tried = sm.autotune(trial_steps=3)
+        for t in tried:
+            stage("  tried " + "/".join(str(t[k]) for k in T.Tune.SHAPE) + f": {t['contact_ms']:.3f} ms")
+    stage("autotune: " + "/".join(str(tune[k]) for k in T.Tune.SHAPE))
+    sm.set_graph(True)
+    sm.step(warmup)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    with sampler:
+        secs = time_device(sm, torch, args.steps, stream)
+    launches, _, _ = sm.profile()
+    ke, ncontact = sm.energy()
+    mesh_contacts = int(sm.pairs(2)[0].sum())
+    sm.set_profiling(True)
+    sm.step(min(args.steps, 16))
+    _, contact_ms, contact_n = sm.profile()
+    sm.set_profiling(False)
+    contact_ms /= max(contact_n, 1)
+    st_mx = sm.status()
+    stage(f"mixed timed: {1e3 * secs / args.steps:.3f} ms/step")
+    # e2e: the multibody exchange of every step -- host pose records in,
+    # wrenches out.  The host side moves the wheel: spin at omega about -z
+    # (prescribed drive) and vertical motion from the wrench and its weight
+    # (semi-implicit Euler), the pose of the next step re-placing its
+    # triangles; the planes stay where they are
+    k_e2e = max(1, min(args.steps, 100))
+    nb = len(sm.bodies)
+    recs = [np.asarray(b, dtype=np.float64) for b in sc.plane_body] + [np.asarray(sc.meshes[0]["body"])]
+    rec = torch.zeros((nb, 15), dtype=torch.float64).pin_memory()
+    for b in range(nb):
+        rec[b] = torch.from_numpy(recs[b])
+    wr = torch.zeros((nb, 6), dtype=torch.float64).pin_memory()
+    omega = -2.0 * float(recs[-1][14])
+    m_w = float(recs[-1][0])
+    y_w, vy_w = float(recs[-1][2]), 0.0
+    fy_sum = 0.0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(k_e2e):
+        th = -omega * sc.dt * (i + 1)  # rolling toward +x: rotation about -z
+        rec[nb - 1, 7] = float(np.cos(0.5 * th))
+        rec[nb - 1, 10] = float(np.sin(0.5 * th))
+        rec[nb - 1, 2] = y_w
+        rec[nb - 1, 5] = vy_w
+        for b in range(nb):
+            pl = C.byref(sc.planes[b]) if b < len(sc.planes) else None
+            sm.L.xdem_sim_set_body(sm.h, sm.bodies[b], C.c_void_p(rec[b].data_ptr()), pl)
+        sm.step(1)
+        for b in range(nb):
+            sm.L.xdem_sim_body_wrench(sm.h, sm.bodies[b], C.c_void_p(wr[b].data_ptr()))
+        fy = float(wr[nb - 1, 1])
+        fy_sum += fy
+        vy_w += sc.dt * (fy / m_w + sc.gravity[1])
+        y_w += sc.dt * vy_w
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    wheel_wrench = wr[nb - 1].tolist()
+    wheel = {"wrench_last": wheel_wrench, "mean_contact_force_y": fy_sum / k_e2e,
+             "sink_m": float(recs[-1][2]) - y_w, "mass_kg": m_w}
+    sm.close()
+    stage("e2e timed")
+    # FP64 cluster step on the same scene
+    s64 = S.Sim(sc, precision=T.XDEM_FP64)
+    st64 = torch.cuda.Stream(device=local)
+    s64.L.xdem_sim_set_stream(s64.h, st64.cuda_stream)
+    s64.step(warmup)
+    k64 = max(1, args.steps // 10)
+    secs64 = time_device(s64, torch, k64, st64)
+    status64 = s64.status()
+    s64.close()
+    stage(f"fp64 timed: {1e3 * secs64 / k64:.3f} ms/step")
+    cbar = ncontact / n
+    peak, peak_kind = load_peaks()
+    # algorithmic bytes of the mixed contact stage: each cluster's state read
+    # and written once (cpos in place of pos: 384 B), and per member its
+    # position read and written (64), the next hash and index (8), the force
+    # gather (24), the pair count (8) and 40 B per stored contact
+    b_stage = 384.0 * ns + (64.0 + 8.0 + 24.0 + 8.0 + B_PER_CONTACT * cbar) * n
+    achieved = b_stage / (contact_ms * 1e-3) / 1e9
+    out = {
+        "metric": "member particle-steps/s, wheel testbed of rigid clumps", "value": n * args.steps / secs,
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 contact / f64 state (mixed)", "data": "synthetic",
+        "config": {"workload": f"wheel testbed, {ns} clumps x 3 spheres r=2 mm ({n} spheres), tyre "
+                               f"{sc.meshes[0]['vlist_local'].shape[0]} triangles driven at 2 rad/s, 5 planes, "
+                               f"dt=1e-5 s", "grid": list(sc.grid), "cell_size": sc.cell_size,
+                   "l2": "inputs larger than L2, no flush"},
+        "clusters_per_s": ns * args.steps / secs,
+        "fp64": {"value": n * k64 / secs64, "ms_per_step": 1e3 * secs64 / k64, "steps": k64,
+                 "mixed_over_fp64": (n * args.steps / secs) / (n * k64 / secs64)},
+        "contacts_per_sphere": cbar,
+        "roofline": {"bound": "hbm", "kernel": "k_mixed_pairs<MESH> + k_mixed_cluster_bodies (mixed contact stage)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": b_stage,
+                     "contact_kernel_ms": contact_ms},
+        "e2e": {"value": n * k_e2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nb * 15 * 8 +
+                len(sc.planes) * C.sizeof(T.PlaneInfo), "d2h_bytes_per_step": nb * 48, "steps": k_e2e},
+        "clocks": sampler.summary(), "gpu_launches": launches, "autotune": tune,
+        "wheel": wheel, "mesh_contacts": mesh_contacts, "status": {"mixed": st_mx, "fp64": status64},
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = run_cpu_baseline_clusters(sc)
+    print(json.dumps(out))
+
+
 def bench_calibration(args, torch, local):
     """The differentiable calibration: column collapse of 66,099 spheres
     (r 1.5 mm, 0.1 x 0.3 m column), 4,000 FP64 steps with checkpoints every
@@ -417,9 +575,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--workload", default="dambreak", choices=["dambreak", "sweep", "calibration"],
+    ap.add_argument("--workload", default="dambreak", choices=["dambreak", "sweep", "calibration", "wheel"],
                     help="dambreak: the headline line; sweep: the batched 256-scene parameter sweep; "
-                         "calibration: forward + adjoint of the column collapse")
+                         "calibration: forward + adjoint of the column collapse; wheel: the wheel testbed "
+                         "of rigid clumps (mixed cluster step)")
+    ap.add_argument("--clusters", type=int, default=2_000_000, help="clumps of the wheel workload")
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the sweep workload")
     ap.add_argument("--advance", type=int, default=0,
                     help="untimed steps before the warm-up (0: time from t = 0 of the dam break, the "
@@ -437,7 +597,8 @@ def main():
     if args.impl == "reference" and args.workload != "dambreak":
         if rank == 0:
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm covers the dam-break "
-                              "workload only (no batching and no adjoint in the reference)"}))
+                              "workload only; the other workloads carry their own CPU baseline or have none "
+                              "in the reference (batching, adjoint)"}))
         return
     if args.impl == "reference":
         if rank != 0:
@@ -471,6 +632,10 @@ def main():
     if args.workload == "calibration":
         if rank == 0:
             bench_calibration(args, torch, local)
+        return
+    if args.workload == "wheel":
+        if rank == 0:
+            bench_wheel(args, torch, local)
         return
     scene = make_scene(args.n)
     if args.settle:

@@ -309,8 +309,11 @@ typedef struct xdem_sim xdem_sim;
 typedef struct xdem_sim_config {
     unsigned int np;          /* spheres (cluster members included)          */
     unsigned int ns;          /* clusters; 0 = free spheres (ns = np)        */
-    int precision;            /* XDEM_FP64 or XDEM_MIXED (free spheres only:
-                                 cluster handles are FP64)                   */
+    int precision;            /* XDEM_FP64 or XDEM_MIXED.  Mixed cluster
+                                 handles need one member count for every
+                                 cluster type and no rolling resistance or
+                                 cohesion; xdem_sim_step returns
+                                 XDEM_ERR_ARG otherwise                      */
     int contact_model;        /* 0 DHS, 1 Hertz-Mindlin                      */
     int velocity_compat;      /* see xdem_set_velocity_compat                */
     double dt;

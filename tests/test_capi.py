@@ -67,9 +67,9 @@ def test_argument_checks_need_no_gpu(L):
     assert L.xdem_sim_get_tune(None, C.byref(t)) == T.XDEM_ERR_ARG
     assert L.xdem_sim_autotune(None, 5, C.byref(t), None, None) == T.XDEM_ERR_ARG
     assert L.xdem_sim_list_rebuilds(None, None) == T.XDEM_ERR_ARG
-    # clusters are FP64 only: a mixed cluster handle is refused up front
+    # an unknown precision is refused before anything is allocated
     cfg = T.SimConfig()
-    cfg.np, cfg.ns, cfg.precision, cfg.dt, cfg.cell_size = 30, 10, T.XDEM_MIXED, 1e-5, 0.01
+    cfg.np, cfg.ns, cfg.precision, cfg.dt, cfg.cell_size = 30, 10, 7, 1e-5, 0.01
     for i in range(3):
         cfg.grid_size[i] = 16
     h = C.c_void_p()

@@ -116,6 +116,49 @@ def test_candidate_lists_match_the_stencil_walk(mods, skin_div):
             assert np.array_equal(x, y)
 
 
+def test_candidate_lists_with_a_moving_mesh(mods):
+    """A mesh body pushed through a moving bed, re-posed every five steps:
+    the lists hold the particle pairs, the spheres near the mesh search its
+    triangles, each re-pose makes the next step sort the cells again, and
+    the list form matches the walk bit for bit."""
+    _, _, scenes, sim = mods
+    sc = scenes.random_packed(3000, 0.8e-3, 1.2e-3, None, seed=21, vel_scale=0.3)
+    p = sc.pos.reshape(-1, 4)
+    c = p[:, :3].mean(0)
+    # no sphere starts inside the mesh (it would touch more triangles than a
+    # sphere's five mesh slots)
+    keep = np.linalg.norm(p[:, :3] - c, axis=1) > 2.5e-3 + p[:, 3] + 2e-4
+    sc.np_ = sc.ns = int(keep.sum())
+    sc.pos = p[keep].ravel()
+    for k, w in (("vel", 3), ("acc", 3), ("ep", 4), ("ev", 4), ("ea", 4), ("inertia", 3)):
+        setattr(sc, k, getattr(sc, k).reshape(-1, w)[keep].ravel())
+    sc.mass = sc.mass[keep]
+    mesh = scenes.uv_sphere_mesh(2.5e-3, 6, 10)
+    body = T.body_record(mass=0.05, pos=c, vel=(0.5, 0.0, 0.0), ed=(0.0, 0.0, 0.2, 0.0))
+    sc.meshes = [dict(vlist_local=mesh, body=body, cp=sc.pp_cp)]
+    out = []
+    for sd in (0, 16):
+        s = sim.Sim(sc, precision=T.XDEM_MIXED)
+        s.set_tune(128, 16, 128, 768, 512, sd)
+        rec = body.copy()
+        touched = 0
+        for _ in range(40):
+            rec[1] += 0.5 * 5 * sc.dt
+            s.set_body(s.bodies[-1], rec)
+            s.step(5)
+            touched += int(s.pairs(2)[0].sum())
+        assert s.status() == 0
+        assert touched > 0
+        if sd:
+            assert s.list_rebuilds() >= 1
+        out.append((s.state(), s.pairs(0), s.pairs(2)))
+        s.close()
+    (a, pa, ma), (b, pb, mb) = out
+    states_equal(a, b)
+    for x, y in zip(pa + ma, pb + mb):
+        assert np.array_equal(x, y)
+
+
 def test_overflowing_candidate_list_walks(mods):
     """A 3 mm sphere ringed by 40 small ones within the skin holds more
     candidates than a list keeps: it walks the stencil, the rest use lists,

@@ -37,6 +37,26 @@ namespace xdem {
 
 struct mat_pair;
 constexpr unsigned int kMaxFusedMeshes = 8;
+// Cluster types (xClusterInformation entries) the mixed cluster step holds.
+constexpr unsigned int kMaxClusterTypes = 8;
+
+// Clusters of the mixed step: ns rigid clusters of neach member spheres
+// each, the members of cluster c at c*neach .. c*neach + neach - 1 (one
+// member count for every type, so that id / neach is the cluster of any
+// sphere as impl:485-611 computes it).  Clusters of type t start at
+// first[t] and place their members at rloc[(t*neach + j)*3] in the body
+// frame.  ns == 0: no clusters.
+struct ClusterTab {
+    unsigned int ns = 0, neach = 0, ntype = 0;
+    unsigned int first[kMaxClusterTypes + 1] = {};
+};
+__host__ __device__ inline unsigned int cluster_type(const ClusterTab& t, unsigned int cid)
+{
+    unsigned int k = 0;
+    for (unsigned int i = 1; i < t.ntype; ++i)
+        if (cid >= t.first[i]) k = i;
+    return k;
+}
 constexpr unsigned int kBboxBlocks = 1024;
 constexpr int kPlaneF = 16;  // floats per plane in the prefilter table
 
@@ -100,6 +120,7 @@ struct FusedState {
     bool have_prev = false;    // skey_prev lists the occupied cells of the last step
     unsigned int np = 0, nentry = 0;
     double* pos_alt = nullptr;  // [np*4] other position buffer
+    double* cpos_alt = nullptr; // [ns*4] other cluster-centre buffer (clusters)
     double* ep_alt = nullptr;   // [np*4] other Euler-parameter buffer
     // FP64 snapshot (sorted order)
     double* snap_pos = nullptr; // [nentry*4] x, y, z, r
@@ -127,6 +148,10 @@ struct FusedState {
     float* vl_xb = nullptr;          // [np*4]
     unsigned int* vl_flag = nullptr; // [kVlWords], indices kVl* below
     bool any_coh = false;            // cohesion in a particle-pair material (no lists)
+    // bounding sphere of each mesh (centre relative to the grid origin,
+    // radius): a sphere that cannot reach it skips the triangle search
+    float4* d_mesh_bs = nullptr;     // [kMaxFusedMeshes]
+    float4 h_mesh_bs[kMaxFusedMeshes] = {};
     // body wrench reduction: per-chunk sums and per-body finish counters
     double* wsum = nullptr;          // [wsum_cap * kWrenchChunks * 6]
     unsigned int* wcnt = nullptr;    // [wsum_cap]
@@ -186,9 +211,16 @@ struct FusedArgs {
     unsigned int nscene = 1;
     const unsigned int* scene_of = nullptr;          // [np]
     const unsigned int* scene_plane_first = nullptr; // [nscene + 1]
+    // clusters (mixed form only); ns_state: length of the per-body state
+    // arrays (vel, ep, mass, ...), np for sphere scenes
+    unsigned int ns_state = 0;
+    ClusterTab cl;
+    double** cpos = nullptr;    // [ns*4]: swapped with the alternate buffer
+    const double* rloc = nullptr;
 };
 
-int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st);
+int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st,
+                unsigned int ns = 0);
 void fused_free(FusedState& fs);
 void fused_invalidate(FusedState& fs);
 // host_mp holds nscene particle-pair entries followed by one per body.
@@ -199,6 +231,12 @@ int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned i
 // stream; the host copy it uploads from stays owned by the state.
 int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh,
                        cudaStream_t st);
+// Bounding sphere of mesh m (centre relative to the grid origin, radius;
+// a radius of 1e18 searches every sphere): refreshed on the stream.
+int fused_set_mesh_bounds(FusedState& fs, unsigned int m, float4 b, cudaStream_t st);
+// The next step sorts the cell table even when the candidate lists hold
+// (a mesh moved: its spheres' cells changed).
+int fused_force_sort(FusedState& fs, cudaStream_t st);
 // Runs one step.  When e0/e1 are given they bracket the contact kernel.
 int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1,
                unsigned int* nlaunch);
@@ -278,6 +316,8 @@ struct ContactLaunch {
     const device_triangle_info* tri;
     unsigned int *ms_count, *ms_id;
     double* ms_tsd;
+    const float4* mesh_bs;  // [nmesh] bounding spheres (see FusedState)
+    const double* tri_sphere;  // [ntri*4] fitted sphere of every triangle (x, y, z, r)
     const double* body;
     const mat_pair* mp;
     const MatF* mpf;
@@ -289,6 +329,14 @@ struct ContactLaunch {
     unsigned int nscene;
     const unsigned int* scene_of;          // [np] or null (one scene)
     const unsigned int* scene_plane_first; // [nscene + 1] or null
+    // clusters (cl.ns > 0).  The records of a member carry its cluster's
+    // mass, spin and velocity at the member's centre, so the particle-pair
+    // kernels treat members as spheres apart from the exclusion of partners
+    // |id - k| <= neach (impl:556-558)
+    ClusterTab cl;
+    const double* rloc;
+    const double* cpos_cur;  // x_c of this step
+    double* cpos_next;       // x_c of the next step out
 };
 
 // Scene of a particle and the range of planes it sees.

@@ -86,6 +86,54 @@ __global__ void k_prologue(device_dem_parameters p, const double* pos, const dou
     val[i] = i;
 }
 
+// Position update of the first step for clusters (impl:149-190): centre and
+// Euler parameters into the alternate buffers, member centres x_c + A(e)
+// rloc, and the members' FP32 records and cell hashes.  A member's record
+// carries its cluster's mass and spin and the cluster's velocity at the
+// member's centre, v + w x (x_m - x_c): the velocity of a contact point at
+// x is then the record's velocity + w x (x - x_m), as impl:485-611 forms it
+// from the cluster centre.
+__global__ void k_prologue_cluster(device_dem_parameters p, ClusterTab t, const double* cpos, const double* ep,
+                                   const double* vel, const double* ev, const double* acc, const double* ea,
+                                   const double* mass, const double* rloc, const double* pos, double* cpos_next,
+                                   double* ep_next, double* pos_next, unsigned int* key, unsigned int* val,
+                                   unsigned int* status, float4* rec)
+{
+    const unsigned int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= t.ns) return;
+    const double dt = p.dt, h = p.half2dt;
+    const d4 cp = ld4(cpos, c);
+    const d3 x = (mk3(cp.x, cp.y, cp.z) + dt * ld3(vel, c)) + h * ld3(acc, c);
+    st4(cpos_next, c, mk4(x.x, x.y, x.z, cp.w));
+    const d4 w = ld4(ev, c);
+    const d4 e = (ld4(ep, c) + dt * w) + h * ld4(ea, c);
+    const double l = sqrt(dot(e, e));
+    const d4 en = mk4(e.x / l, e.y / l, e.z / l, e.w / l);
+    st4(ep_next, c, en);
+    if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) atomicOr(status, (unsigned int)XDEM_ERR_NONFINITE);
+    const d3 v = ld3(vel, c);
+    const d3 om = ang_vel(en, w);
+    const double m = mass[c];
+    const unsigned int type = cluster_type(t, c);
+    for (unsigned int j = 0; j < t.neach; ++j) {
+        const size_t i = (size_t)c * t.neach + j;
+        const d3 d = to_global(ld3(rloc, (size_t)type * t.neach + j), en);
+        const d3 xm = x + d;
+        const double r = pos[4 * i + 3];
+        st4(pos_next, i, mk4(xm.x, xm.y, xm.z, r));
+        float4 A, L, B, C;
+        unsigned int T;
+        const int3v g = mixed_record(p, 1.0 / p.cell_size, xm, r, v + cross(om, d), m, om, A, L, B, C, T);
+        C.w = __uint_as_float(T);
+        rec[4 * i + kRecA] = A;
+        rec[4 * i + kRecL] = L;
+        rec[4 * i + kRecB] = B;
+        rec[4 * i + kRecC] = C;
+        key[i] = grid_hash(p, g.x, g.y, g.z);
+        val[i] = (unsigned int)i;
+    }
+}
+
 // Bounding box of the positions: block min/max into out[block*6].
 __global__ void k_bbox(const double* pos, unsigned int n, double* out)
 {
@@ -189,14 +237,18 @@ __global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk
 // memory), the last block of a body to finish adds the chunk sums in chunk
 // order.  The order of every addition is fixed: the result does not depend
 // on which block finishes last.
-__global__ void k_body_sums(const double* bsums, unsigned int nblocks, double* wrench, double* chunk,
-                            unsigned int* done)
+__global__ void k_body_sums(const double* bsums, unsigned int nblocks, unsigned int nplane, unsigned int rows_plane,
+                            unsigned int rows_mesh, double* wrench, double* chunk, unsigned int* done)
 {
     __shared__ double sm[8 * 6];
     __shared__ bool last;
     const unsigned int b = blockIdx.x / kWrenchChunks, q = blockIdx.x % kWrenchChunks;
-    const unsigned int per = (nblocks + kWrenchChunks - 1) / kWrenchChunks;
-    const unsigned int i0 = q * per, i1 = min(nblocks, i0 + per);
+    // rows of body b: one per block of the kernel that does its contacts
+    // (planes: the body kernel, meshes: the pair kernel); nblocks is the
+    // row stride
+    const unsigned int rows = b < nplane ? rows_plane : rows_mesh;
+    const unsigned int per = (rows + kWrenchChunks - 1) / kWrenchChunks;
+    const unsigned int i0 = q * per, i1 = min(rows, i0 + per);
     double s[6] = {0, 0, 0, 0, 0, 0};
     for (unsigned int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const double* r = bsums + ((size_t)b * nblocks + i) * 6;
@@ -319,13 +371,14 @@ int fused_scene_energy(const double* vel, const double* ep, const double* ev, co
     return XDEM_OK;
 }
 
-int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st)
+int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed, cudaStream_t st, unsigned int ns)
 {
     fs.mixed = mixed;
     fs.np = np;
     fs.nentry = nentry;
     cudaError_t e = dalloc(fs.pos_alt, (size_t)np * 4);
     if (e == cudaSuccess) e = dalloc(fs.ep_alt, (size_t)np * 4);
+    if (e == cudaSuccess && ns) e = dalloc(fs.cpos_alt, (size_t)ns * 4);
     if (mixed) {
         if (e == cudaSuccess) e = dalloc(fs.mA, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mL, (size_t)nentry * 4);
@@ -342,6 +395,12 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.vl_xb, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.vl_flag, kVlWords);
         if (e == cudaSuccess) e = cudaMemsetAsync(fs.vl_flag, 0, kVlWords * sizeof(unsigned int), st);
+        // until the handle sets them, every mesh is searched by every sphere
+        for (unsigned int m = 0; m < kMaxFusedMeshes; ++m) fs.h_mesh_bs[m] = make_float4(0.f, 0.f, 0.f, 1e18f);
+        if (e == cudaSuccess) e = dalloc(fs.d_mesh_bs, kMaxFusedMeshes);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(fs.d_mesh_bs, fs.h_mesh_bs, sizeof(fs.h_mesh_bs), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     } else {
         if (e == cudaSuccess) e = dalloc(fs.snap_pos, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.snap_vel, (size_t)nentry * 4);
@@ -362,10 +421,11 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 
 void fused_free(FusedState& fs)
 {
-    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
+    void* ps[] = {fs.pos_alt, fs.ep_alt, fs.cpos_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
                   fs.mC, fs.mIT, fs.rec, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
                   fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag,
-                  fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf, fs.wsum, fs.wcnt};
+                  fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf, fs.wsum, fs.wcnt,
+                  fs.d_mesh_bs};
     for (void* q : ps)
         if (q) cudaFree(q);
     fs = FusedState{};
@@ -490,6 +550,22 @@ int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& 
     return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
 }
 
+int fused_set_mesh_bounds(FusedState& fs, unsigned int m, float4 b, cudaStream_t st)
+{
+    if (m >= kMaxFusedMeshes || !fs.d_mesh_bs) return XDEM_OK;  // tables not built yet
+    fs.h_mesh_bs[m] = b;
+    const cudaError_t e =
+        cudaMemcpyAsync(fs.d_mesh_bs + m, &fs.h_mesh_bs[m], sizeof(float4), cudaMemcpyHostToDevice, st);
+    return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
+}
+
+int fused_force_sort(FusedState& fs, cudaStream_t st)
+{
+    if (!fs.vl_flag) return XDEM_OK;
+    return cudaMemsetAsync(fs.vl_flag + kVlSort, 1, sizeof(unsigned int), st) == cudaSuccess ? XDEM_OK
+                                                                                          : XDEM_ERR_CUDA;
+}
+
 int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, unsigned int* nlaunch)
 {
     cudaError_t e = cudaSuccess;
@@ -500,14 +576,26 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     };
     const unsigned int np = a.np, n = a.nentry;
     const double* org = &a.prm.world_origin.x;
+    const bool clusters = a.cl.ns != 0;
+    // per-body arrays shorter than the sphere count are cluster state: only
+    // the cluster form may run on them
+    if (a.ns_state != np && (!clusters || a.cl.ns != a.ns_state)) return XDEM_ERR_ARG;
+    if (clusters && (!fs.mixed || !fs.cpos_alt || !a.cpos || !a.rloc || !a.cl.neach ||
+                     (unsigned long long)a.cl.ns * a.cl.neach != np))
+        return XDEM_ERR_ARG;
     if (!fs.primed) {
         // empty cell table, first position update + hash, and the extent of
         // the FP32 frame (grid origin to the far side of the particle cloud)
         ok(launch_fill_u32(a.cstart, 0xffffffffu, a.ncell, st));
         ok(cudaMemsetAsync(a.cend, 0, a.ncell * sizeof(unsigned int), st));
         fs.have_prev = false;
-        k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, a.mass,
-                                                        fs.pos_alt, fs.ep_alt, a.k0, a.v0, np, a.status, fs.rec);
+        if (clusters)
+            k_prologue_cluster<<<blocks_for(a.cl.ns), kThreads, 0, st>>>(
+                a.prm, a.cl, *a.cpos, *a.ep, a.vel, a.ev, a.acc, a.ea, a.mass, a.rloc, *a.pos, fs.cpos_alt,
+                fs.ep_alt, fs.pos_alt, a.k0, a.v0, a.status, fs.rec);
+        else
+            k_prologue<<<blocks_for(np), kThreads, 0, st>>>(a.prm, *a.pos, *a.ep, a.vel, a.ev, a.acc, a.ea, a.mass,
+                                                            fs.pos_alt, fs.ep_alt, a.k0, a.v0, np, a.status, fs.rec);
         ok(cudaGetLastError());
         const unsigned int nbb = std::min(kBboxBlocks, std::max(1u, blocks_for(np, 256)));
         k_bbox<<<nbb, 256, 0, st>>>(*a.pos, np, fs.d_bbox);
@@ -551,6 +639,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     // here; the contact kernel then writes x_{n+2} into the old buffers.
     std::swap(*a.pos, fs.pos_alt);
     std::swap(*a.ep, fs.ep_alt);
+    if (clusters) std::swap(*a.cpos, fs.cpos_alt);
     // mesh spheres join the sort at entries np + first (xIntegratorVV.cpp:32-43)
     for (unsigned int m = 0; m < a.nmesh; ++m)
         ok(launch_hash(a.prm, a.k0, a.v0, a.tri_sphere + 4 * (size_t)a.mesh_first[m], np + a.mesh_first[m],
@@ -558,7 +647,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     // With candidate lists the cell sort is only read by the stencil walk of
     // a rebuild step (or of a sphere whose list overflowed at the last
     // build): the device skips the clear, sort and reorder otherwise.
-    const bool use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && a.nmesh == 0 && !fs.any_coh && fs.vl_flag;
+    const bool use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && !fs.any_coh && fs.vl_flag;
     const unsigned int* sort_gate = use_list ? fs.vl_flag + kVlSort : nullptr;
     if (fs.have_prev) ok(launch_clear_cells(fs.skey_prev, n, a.cstart, a.cend, st, sort_gate));
     unsigned int *sk = nullptr, *sv = nullptr;
@@ -621,6 +710,8 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     }
     c.pl_count = a.pl_count; c.pl_id = a.pl_id; c.pl_tsd = a.pl_tsd;
     c.tri = a.tri; c.ms_count = a.ms_count; c.ms_id = a.ms_id; c.ms_tsd = a.ms_tsd;
+    c.mesh_bs = fs.d_mesh_bs;
+    c.tri_sphere = a.tri_sphere;
     c.body = a.body; c.mp = a.mp;
     // body wrench partials: one row entry per block of the emitting kernel
     // (the mixed pair and body kernels share their block size whenever the
@@ -628,6 +719,21 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.tune = fs.tune;
     const unsigned int nt_emit = fs.mixed ? fs.tune.nt_bodies : (unsigned int)kFusedThreads;
     c.nblocks = (n + nt_emit - 1) / nt_emit;
+    unsigned int rows_plane = c.nblocks, rows_mesh = c.nblocks;
+    c.cl = a.cl;
+    c.rloc = a.rloc;
+    c.cpos_cur = clusters ? *a.cpos : nullptr;
+    c.cpos_next = clusters ? fs.cpos_alt : nullptr;
+    if (fs.mixed) {
+        // rows of partial wrench sums: one per block of the kernel doing the
+        // body's contacts -- planes: the body kernel (sorted entries, or
+        // clusters); meshes: the pair kernel (sorted entries on the walk,
+        // spheres with candidate lists); the row stride covers both
+        const unsigned int nt_b = fs.tune.nt_bodies, nt_p = fs.tune.nt_pairs;
+        rows_plane = clusters ? (a.cl.ns + nt_b - 1) / nt_b : (n + nt_b - 1) / nt_b;
+        rows_mesh = use_list ? (np + nt_p - 1) / nt_p : (n + nt_p - 1) / nt_p;
+        c.nblocks = std::max(rows_plane, rows_mesh);
+    }
     c.bsums = a.bsums;
     c.status = a.status;
     c.nscene = a.nscene ? a.nscene : 1;
@@ -641,7 +747,8 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody && c.nscene == 1) {  // batched handles keep no body wrenches
         if (a.nbody > fs.wsum_cap) return XDEM_ERR_ARG;  // fused_set_bodies sizes the chunk sums
-        k_body_sums<<<a.nbody * kWrenchChunks, 256, 0, st>>>(a.bsums, c.nblocks, a.wrench, fs.wsum, fs.wcnt);
+        k_body_sums<<<a.nbody * kWrenchChunks, 256, 0, st>>>(a.bsums, c.nblocks, a.nplane, rows_plane, rows_mesh,
+                                                             a.wrench, fs.wsum, fs.wcnt);
         ok(cudaGetLastError());
     }
     if (e != cudaSuccess) return XDEM_ERR_CUDA;

@@ -38,6 +38,8 @@ __device__ __forceinline__ V3<float> qdiv(V3<float> a, float b)
 {
     return v3<float>(qdiv(a.x, b), qdiv(a.y, b), qdiv(a.z, b));
 }
+__device__ __forceinline__ unsigned int umax(unsigned int a, unsigned int b) { return a > b ? a : b; }
+__device__ __forceinline__ unsigned int umin(unsigned int a, unsigned int b) { return a < b ? a : b; }
 
 // Asynchronous global -> shared copies (cp.async, sm_80+): the thread's old
 // pair list is fetched while it walks its stencil.  Each thread copies and
@@ -337,6 +339,9 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
     const float screen = 1.0f + 0x1p-11f;
     const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
     const unsigned int sid = oid * MAX_P2P_COUNT;
+    // partners k with |oid - k| <= excl are skipped: the sphere itself, and
+    // for clusters every sphere up to neach ids away (impl:556-558)
+    const unsigned int excl = c.cl.neach;
     unsigned int old_count = c.pp_count_old[oid];
     if (old_count > MAX_P2P_COUNT) old_count = MAX_P2P_COUNT;
     // the old partner ids travel to shared memory while the stencil is walked
@@ -394,7 +399,9 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
                         const uint2 it = j == rs[r] ? it0[r] : reinterpret_cast<const uint2*>(c.mIT)[j];
                         const float4 Aj = j == rs[r] ? A0[r] : reinterpret_cast<const float4*>(c.mA)[j];
                         const unsigned int xs = (it.y - ux + 1u) & 2047u;  // x step + 1 unless an alias
-                        if ((it.y & ~2047u) != want_yz || xs > 2u || it.x == oid || it.x >= c.np) continue;
+                        if ((it.y & ~2047u) != want_yz || xs > 2u || umax(it.x, oid) - umin(it.x, oid) <= excl ||
+                            it.x >= c.np)
+                            continue;
                         if (!coh) {
                             const float dx = Aj.x + ((xs == 0u ? -cs : (xs == 2u ? cs : 0.f)) - Ai.x);
                             const float dy = Aj.y + sy, dz = Aj.z + sz;
@@ -570,10 +577,14 @@ __device__ __forceinline__ BodyF load_body_f(const double* dbi)
 // The plane slots (impl:950-1080 slot rule) are read from memory when a
 // plane needs them: the thread owns its slots and writes them as it goes, so
 // memory holds exactly what the reference's next plane launch re-reads.
+// Cluster members (impl:817-948) differ in two places: the body's lever arm
+// is taken from the member's centre (dcpr_j before the contact normal is
+// known, impl:881-882), and the body's mass enters the effective mass.
 __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int k, unsigned int kbeg,
                                             unsigned int oid, d4 ip, V3<float> ivel, V3<float> iom, float im,
                                             unsigned int& pl_cnt, Acc& acc, float f6[6], unsigned int& bits)
 {
+    const bool member = c.cl.neach != 0;
     const device_dem_parameters& p = c.prm;
     const device_plane_info& pl = c.planes[k];
     const PlaneDF& pd = c.planedf[k];
@@ -612,7 +623,7 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
     if (!hit) return false;
     const float r = df_f(rd);
     const V3<float> dcpr = r * un;
-    const V3<float> dcpr_j = rel + dcpr;
+    const V3<float> dcpr_j = member ? rel : rel + dcpr;
     float sd0 = 0.f, sd1 = 0.f;
     V3<float> mf;
     if (cdd > 0) {
@@ -623,7 +634,7 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
                 break;
             }
         const V3<float> dv = (b.v + tcross(b.om, dcpr_j)) - (ivel + tcross(iom, dcpr));
-        const FC<float> fc = fconst_r<float>(mr, p.contact_model, r, 0.f, im, 0.f);
+        const FC<float> fc = fconst_r<float>(mr, p.contact_model, r, 0.f, im, member ? b.m : 0.f);
         float fca = 0.f;
         if (mr.coh) {
             const double fsn = -(double)fc.kn * (cdd * sqrt(cdd));
@@ -687,6 +698,11 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
     d3 prev_line = mk3(0, 0, 0), prev_point = mk3(0, 0, 0);
     double cs = 0.0;
     if (mr.coh) cs = limit_cohesion_depth(mp, ir, 0.0);
+    // FP32 screen of a triangle by its fitted sphere, which contains it: a
+    // sphere of the particle farther than r_tri + r from the centre cannot
+    // touch the triangle (off with cohesion, which reaches beyond contact)
+    const float xf = d2f_rn(ipos.x), yf = d2f_rn(ipos.y), zf = d2f_rn(ipos.z), rf = d2f_rn(ir);
+    const double* sph = c.tri_sphere + 4 * (size_t)c.mesh_first[m];
     for (int z = -1; z <= 1; ++z)
         for (int y = -1; y <= 1; ++y)
             for (int x = -1; x <= 1; ++x) {
@@ -694,10 +710,22 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
                 const unsigned int start = c.cstart[h];
                 if (start == 0xffffffffu) continue;
                 const unsigned int end = c.cend[h];
-                for (unsigned int j = start; j < end; ++j) {
+                // a cell's entries are in ascending id (stable sort of an
+                // id-ordered input): this mesh's spheres, ids lo .. lo + ntri
+                // - 1, follow every particle; later meshes follow them
+                unsigned int jm = end;
+                while (jm > start && c.sorted_index[jm - 1] >= lo) --jm;
+                for (unsigned int j = jm; j < end; ++j) {
                     unsigned int tk = c.sorted_index[j];
-                    if (!(tk >= lo && tk < lo + ntri)) continue;
+                    if (tk >= lo + ntri) break;
                     tk -= lo;
+                    if (!mr.coh) {
+                        const double2 q0 = reinterpret_cast<const double2*>(sph)[2 * tk];
+                        const double2 q1 = reinterpret_cast<const double2*>(sph)[2 * tk + 1];
+                        const float dx = d2f_rn(q0.x) - xf, dy = d2f_rn(q0.y) - yf, dz = d2f_rn(q1.x) - zf;
+                        const float lim = d2f_rn(q1.y) + rf + 1e-5f;
+                        if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+                    }
                     int t = -1;
                     const d3 cpt = closest_pt_triangle(c.tri[c.mesh_first[m] + tk], ipos, t);
                     const double cd = ir - length(ipos - cpt);
@@ -776,39 +804,49 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
     return touched;
 }
 
-// Velocity update, next Euler parameters and position, the next cell and the
-// next step's FP32 records (impl:192-222, 135-147, 290-302).  FP64 work: the
-// 14 additions of FP32 increments to the FP64 state.  The Euler parameters
-// are renormalised to second order, 1/sqrt(1 + eps) ~ 1 - eps/2 + 3/8 eps^2,
+// Velocity update, next Euler parameters and centre of body i -- a sphere,
+// or a cluster's centre -- (impl:192-222 and 224-287, 135-147 and 149-190)
+// from its force Ff and moment Mf (global frame).  FP64 work: the 14
+// additions of FP32 increments to the FP64 state.  The Euler parameters are
+// renormalised to second order, 1/sqrt(1 + eps) ~ 1 - eps/2 + 3/8 eps^2,
 // with eps = |e + de|^2 - 1 formed in float pairs from the FP64 e.
-__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float4 Ai, float4 Li,
-                                           float4 Bi, V3<float> Ff, V3<float> Mf, unsigned int& bits)
+// Writes vel, acc, ev, ea and ep_next of body i; returns the next centre,
+// the next Euler parameters (FP64, as stored, and FP32), their new rates and
+// the new velocity in FP32.
+struct NextBody {
+    d3 x;
+    d4 e;
+    float4 ef, ev;
+    V3<float> v;
+};
+__device__ __forceinline__ NextBody integrate_f(const ContactLaunch& c, unsigned int i, d3 xi, float m,
+                                                V3<float> Ff, V3<float> Mf, bool apply_vel)
 {
-    const device_dem_parameters& p = c.prm;
     const float dt = c.dt_f, hdt = c.hdt_f, h2 = c.h2_f;
-    const float inv_m = 1.f / Bi.w;
+    const float inv_m = 1.f / m;
     const V3<float> a_new = v3<float>(Ff.x * inv_m + c.g_f[0], Ff.y * inv_m + c.g_f[1], Ff.z * inv_m + c.g_f[2]);
+    NextBody o;
     // translation
-    const d3 v = ld3(c.vel, oid);
+    const d3 v = ld3(c.vel, i);
     V3<float> vn = vf(d2f3(v));
-    if (!c.vel_compat) {
-        const V3<float> dv = hdt * (vf(d2f3(ld3(c.acc, oid))) + a_new);
-        st3(c.vel, oid, mk3(v.x + f2d(dv.x), v.y + f2d(dv.y), v.z + f2d(dv.z)));
+    if (apply_vel) {
+        const V3<float> dv = hdt * (vf(d2f3(ld3(c.acc, i))) + a_new);
+        st3(c.vel, i, mk3(v.x + f2d(dv.x), v.y + f2d(dv.y), v.z + f2d(dv.z)));
         vn = vn + dv;
     }
-    st3(c.acc, oid, mk3(f2d(a_new.x), f2d(a_new.y), f2d(a_new.z)));
+    st3(c.acc, i, mk3(f2d(a_new.x), f2d(a_new.y), f2d(a_new.z)));
     // rotation
-    const d4 e = ld4(c.ep_cur, oid);
+    const d4 e = ld4(c.ep_cur, i);
     const df e0 = split_d(e.x), e1 = split_d(e.y), e2 = split_d(e.z), e3 = split_d(e.w);
     const float4 ef = make_float4(df_f(e0), df_f(e1), df_f(e2), df_f(e3));
-    const d4 ev = ld4(c.ev, oid);
+    const d4 ev = ld4(c.ev, i);
     const float4 evf = d2f4(ev);
-    const float4 eaf = d2f4(ld4(c.ea, oid));
-    const float3 J = d2f3(ld3(c.inertia, oid));
+    const float4 eaf = d2f4(ld4(c.ea, i));
+    const float3 J = d2f3(ld3(c.inertia, i));
     const float4 q = uceom_f(J, ef, evf, to_local_f(make_float3(Mf.x, Mf.y, Mf.z), ef));
     const float4 dev = make_float4(hdt * (eaf.x + q.x), hdt * (eaf.y + q.y), hdt * (eaf.z + q.z), hdt * (eaf.w + q.w));
-    st4(c.ev, oid, mk4(ev.x + f2d(dev.x), ev.y + f2d(dev.y), ev.z + f2d(dev.z), ev.w + f2d(dev.w)));
-    st4(c.ea, oid, mk4(f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w)));
+    st4(c.ev, i, mk4(ev.x + f2d(dev.x), ev.y + f2d(dev.y), ev.z + f2d(dev.z), ev.w + f2d(dev.w)));
+    st4(c.ea, i, mk4(f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w)));
     const float4 evn = make_float4(evf.x + dev.x, evf.y + dev.y, evf.z + dev.z, evf.w + dev.w);
     const float4 de = make_float4(dt * evn.x + h2 * q.x, dt * evn.y + h2 * q.y, dt * evn.z + h2 * q.z,
                                   dt * evn.w + h2 * q.w);
@@ -828,23 +866,33 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
     const float kk = eps * (-0.5f + 0.375f * eps);
     const float4 dn = make_float4(de.x + kk * (ef.x + de.x), de.y + kk * (ef.y + de.y), de.z + kk * (ef.z + de.z),
                                   de.w + kk * (ef.w + de.w));
-    st4(c.ep_next, oid, mk4(e.x + f2d(dn.x), e.y + f2d(dn.y), e.z + f2d(dn.z), e.w + f2d(dn.w)));
-    const float4 en = make_float4(ef.x + dn.x, ef.y + dn.y, ef.z + dn.z, ef.w + dn.w);
-    // position
+    o.e = mk4(e.x + f2d(dn.x), e.y + f2d(dn.y), e.z + f2d(dn.z), e.w + f2d(dn.w));
+    st4(c.ep_next, i, o.e);
+    o.ef = make_float4(ef.x + dn.x, ef.y + dn.y, ef.z + dn.z, ef.w + dn.w);
+    o.ev = evn;
+    o.v = vn;
+    // centre
     const V3<float> inc = dt * vn + h2 * a_new;
-    const d3 xn = mk3(ip.x + f2d(inc.x), ip.y + f2d(inc.y), ip.z + f2d(inc.z));
-    st4(c.pos_next, oid, mk4(xn.x, xn.y, xn.z, ip.w));
-    // cell of the new centre and the offset from its corner, in float pairs:
-    // the offset is exact to ~1e-15 m and in [0, cell size), so the binning
-    // agrees with the offsets the neighbour loop uses
+    o.x = mk3(xi.x + f2d(inc.x), xi.y + f2d(inc.y), xi.z + f2d(inc.z));
+    return o;
+}
+
+// The next step's FP32 record of sphere oid centred at X (offset from the
+// grid origin, float pairs): the cell of the centre and the offset from its
+// corner -- exact to ~1e-15 m and in [0, cell size), so the binning agrees
+// with the offsets the neighbour loop uses -- radius (rh + rl), velocity,
+// mass and spin; the key and value of the next cell sort (impl:290-302);
+// and the candidate lists' displacement check.
+__device__ __forceinline__ void emit_rec(const ContactLaunch& c, unsigned int oid, const df X[3], float rh, float rl,
+                                         V3<float> vn, float m, float3 w, unsigned int& bits)
+{
     const df csd = df{c.cs_f, c.cs_lo};
     int cell[3];
     df A[3];
     bool fin = true;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        const double xi = i == 0 ? xn.x : (i == 1 ? xn.y : xn.z);
-        const df rx = df_sub(split_d(xi), df{c.o_hi[i], c.o_lo[i]});
+        const df rx = X[i];
         if (!isfinite(rx.hi)) {
             fin = false;
             cell[i] = 0;
@@ -867,13 +915,12 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
         A[i] = off;
     }
     if (!fin) bits |= XDEM_ERR_NONFINITE;
-    c.k_out[oid] = grid_hash(p, cell[0], cell[1], cell[2]);
+    c.k_out[oid] = grid_hash(c.prm, cell[0], cell[1], cell[2]);
     c.v_out[oid] = oid;
-    const float3 w = ang_vel_f(en, evn);
     float4* r = c.rec + 4 * (size_t)oid;
-    r[kRecA] = make_float4(A[0].hi, A[1].hi, A[2].hi, Ai.w);
-    r[kRecL] = make_float4(A[0].lo, A[1].lo, A[2].lo, Li.w);
-    r[kRecB] = make_float4(vn.x, vn.y, vn.z, Bi.w);
+    r[kRecA] = make_float4(A[0].hi, A[1].hi, A[2].hi, rh);
+    r[kRecL] = make_float4(A[0].lo, A[1].lo, A[2].lo, rl);
+    r[kRecB] = make_float4(vn.x, vn.y, vn.z, m);
     r[kRecC] = make_float4(w.x, w.y, w.z, __uint_as_float(pack_cell(cell[0], cell[1], cell[2])));
     if (c.use_list) {
         // distance from the centre at the last list build, in the lists'
@@ -884,6 +931,18 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
         const float dz = (float)(cell[2] & 1023) * c.cs_f + A[2].hi - xb.z;
         if (!(dx * dx + dy * dy + dz * dz < c.half_skin2_f)) atomicOr(c.vl_flag + kVlMoved, 1u);
     }
+}
+
+// Sphere tail: integration, the next position and the next record.
+__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float4 Ai, float4 Li,
+                                           float4 Bi, V3<float> Ff, V3<float> Mf, unsigned int& bits)
+{
+    const NextBody nx = integrate_f(c, oid, mk3(ip.x, ip.y, ip.z), Bi.w, Ff, Mf, !c.vel_compat);
+    st4(c.pos_next, oid, mk4(nx.x.x, nx.x.y, nx.x.z, ip.w));
+    const df X[3] = {df_sub(split_d(nx.x.x), df{c.o_hi[0], c.o_lo[0]}),
+                     df_sub(split_d(nx.x.y), df{c.o_hi[1], c.o_lo[1]}),
+                     df_sub(split_d(nx.x.z), df{c.o_hi[2], c.o_lo[2]})};
+    emit_rec(c, oid, X, Ai.w, Li.w, nx.v, Bi.w, ang_vel_f(nx.ef, nx.ev), bits);
     if (bits) atomicOr(c.status, bits);
 }
 
@@ -919,6 +978,79 @@ __device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned in
     o.tm[0] = a.tm.x; o.tm[1] = a.tm.y; o.tm[2] = a.tm.z;
     o.rs = a.rs;
     return o;
+}
+
+// One sphere against mesh m behind a call boundary (few spheres are near a
+// mesh, and the triangle search holds three candidate arrays): the same
+// value-in, value-out form as plane_call.  Both pair kernels go through it,
+// so the walk and the candidate-list forms sum mesh contacts alike.
+struct MeshOut {
+    float f[3], m[3], w[6], tm[3], rs;
+    unsigned int bits;
+    int touched;
+};
+__device__ __noinline__ MeshOut mesh_call(const ContactLaunch* cp, unsigned int m, unsigned int oid, unsigned int gx,
+                                          unsigned int gy, unsigned int gz, d4 ip, float4 Bi, float4 Ci)
+{
+    Acc a;
+    a.tm = v3<float>(0.f, 0.f, 0.f);
+    a.rs = 0.f;
+    float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    MeshOut o;
+    o.bits = 0;
+    o.touched = mesh_mixed(*cp, m, oid, gx, gy, gz, ip, v3<float>(Bi.x, Bi.y, Bi.z), v3<float>(Ci.x, Ci.y, Ci.z),
+                           Bi.w, a, f6, o.bits);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        o.f[i] = a.f[i].value();
+        o.m[i] = a.m[i].value();
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.w[i] = f6[i];
+    o.tm[0] = a.tm.x; o.tm[1] = a.tm.y; o.tm[2] = a.tm.z;
+    o.rs = a.rs;
+    return o;
+}
+
+// Sphere (centre ip, radius ip.w) against the meshes, in mesh order: a mesh
+// whose bounding sphere the sphere cannot reach (c.mesh_bs: centre relative
+// to the grid origin, radius with the FP32 slack) holds no contact of it, so
+// only its pair count is written (0, as the search would leave it); the rest
+// search the grid for triangles.  Every thread of the block takes part (the
+// body wrench partials are block sums).
+__device__ __forceinline__ void meshes_mixed(const ContactLaunch& c, bool live, unsigned int oid, unsigned int gx,
+                                             unsigned int gy, unsigned int gz, d4 ip, float4 Bi, float4 Ci,
+                                             Acc& acc, unsigned int& bits, float* smf)
+{
+    const float xf = d2f_rn(ip.x) - c.o_hi[0], yf = d2f_rn(ip.y) - c.o_hi[1], zf = d2f_rn(ip.z) - c.o_hi[2];
+    const float rf = d2f_rn(ip.w);
+    for (unsigned int m = 0; m < c.nmesh; ++m) {
+        float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        bool touched = false;
+        if (live) {
+            const float4 b = c.mesh_bs[m];
+            const float dx = xf - b.x, dy = yf - b.y, dz = zf - b.z, lim = b.w + rf;
+            if (dx * dx + dy * dy + dz * dz <= lim * lim) {
+                const MeshOut o = mesh_call(&c, m, oid, gx, gy, gz, ip, Bi, Ci);
+                bits |= o.bits;
+                if (o.touched) {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        acc.f[i].add(o.f[i]);
+                        acc.m[i].add(o.m[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) f6[i] = o.w[i];
+                    acc.tm = acc.tm + v3<float>(o.tm[0], o.tm[1], o.tm[2]);
+                    acc.rs += o.rs;
+                    touched = true;
+                }
+            } else {
+                c.ms_count[oid] = 0u;
+            }
+        }
+        emit_body_f(f6, touched, c.bsums + ((size_t)(c.mesh_body[m]) * c.nblocks + blockIdx.x) * 6, smf);
+    }
 }
 
 // Kernel 1 of the mixed step: one thread per cell-sorted entry, particle-
@@ -971,12 +1103,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
     if (MESH) {
         d4 ip = mk4(0, 0, 0, 0);
         if (live) ip = ld4(c.pos_cur, oid);
-        for (unsigned int m = 0; m < c.nmesh; ++m) {
-            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            bool touched = false;
-            if (live) touched = mesh_mixed(c, m, oid, gx, gy, gz, ip, ivel, iom, Bi.w, acc, f6, bits);
-            emit_body_f(f6, touched, c.bsums + ((size_t)(c.mesh_body[m]) * c.nblocks + blockIdx.x) * 6, smf);
-        }
+        meshes_mixed(c, live, oid, gx, gy, gz, ip, Bi, Ci, acc, bits, smf);
     }
     if (!live) return;
     reinterpret_cast<float4*>(c.fA)[oid] = make_float4(acc.f[0].value(), acc.f[1].value(), acc.f[2].value(), acc.rs);
@@ -990,30 +1117,44 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
 // otherwise its contacts come from the list (a sphere whose list overflowed
 // walks; the cell sort is kept up to date for it).  Writes the same sums as
 // k_mixed_pairs for kernel 2.
-template <unsigned int NT, unsigned int OCC>
+template <bool MESH, unsigned int NT, unsigned int OCC>
 __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
 {
+    __shared__ float smf[MESH ? (NT / 32) * 6 * 2 : 1];
     __shared__ unsigned int stage[16 * NT];                   // walk fallback candidates, [slot][thread]
     __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
     const bool rebuild = c.vl_flag[kVlRebuild] != 0u;
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (oid >= c.np) return;
-    const float4* r = c.rec + 4 * (size_t)oid;
-    const float4 Ai = r[kRecA], Li = r[kRecL], Bi = r[kRecB], Ci = r[kRecC];
+    const bool live = oid < c.np;
+    if (!MESH && !live) return;
+    float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
+    if (live) {
+        const float4* r = c.rec + 4 * (size_t)oid;
+        Ai = r[kRecA]; Li = r[kRecL]; Bi = r[kRecB]; Ci = r[kRecC];
+    }
     const unsigned int Ti = rec_cell(Ci);
+    const device_dem_parameters& p = c.prm;
+    const unsigned int gx = (Ti & 2047u) & (p.grid_size.x - 1), gy = ((Ti >> 11) & 2047u) & (p.grid_size.y - 1);
+    const unsigned int gz = (Ti >> 22) & (p.grid_size.z - 1);
     Acc acc;
     acc.tm = v3<float>(0.f, 0.f, 0.f);
     acc.rs = 0.f;
     unsigned int bits = 0;
-    if (!rebuild && c.vl_cnt[oid] <= kListCap) {
-        p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, acc, bits);
-    } else {
-        const device_dem_parameters& p = c.prm;
-        const unsigned int gx = (Ti & 2047u) & (p.grid_size.x - 1), gy = ((Ti >> 11) & 2047u) & (p.grid_size.y - 1);
-        const unsigned int gz = (Ti >> 22) & (p.grid_size.z - 1);
-        p2p_mixed<NT, 16>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
-                          bits, rebuild);
+    if (live) {
+        if (!rebuild && c.vl_cnt[oid] <= kListCap)
+            p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, acc, bits);
+        else
+            p2p_mixed<NT, 16>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
+                              bits, rebuild);
     }
+    // triangle meshes (impl:1930-2109): the cell table holds the mesh
+    // spheres as of the last sort, and a moved mesh forces a sort
+    if (MESH) {
+        d4 ip = mk4(0, 0, 0, 0);
+        if (live) ip = ld4(c.pos_cur, oid);
+        meshes_mixed(c, live, oid, gx, gy, gz, ip, Bi, Ci, acc, bits, smf);
+    }
+    if (!live) return;
     reinterpret_cast<float4*>(c.fA)[oid] = make_float4(acc.f[0].value(), acc.f[1].value(), acc.f[2].value(), acc.rs);
     reinterpret_cast<float4*>(c.fB)[oid] = make_float4(acc.m[0].value(), acc.m[1].value(), acc.m[2].value(), 0.f);
     if (c.rolling) reinterpret_cast<float4*>(c.fC)[oid] = make_float4(acc.tm.x, acc.tm.y, acc.tm.z, 0.f);
@@ -1140,6 +1281,133 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     mixed_tail(c, oid, ip, Ai, Li, Bi, Ff, Mf, bits);
 }
 
+// Kernel 2 for clusters (impl:817-948, 224-287, 149-190): one thread per
+// cluster.  The cluster's force is the sum of its members' particle-pair and
+// plane forces, its moment the sum of the members' moments about their
+// centres plus (x_m - x_c) x F_m, so the moment is taken about the cluster
+// centre as impl:485-611 and 817-948 take it.  Then the velocity update and
+// the next centre and Euler parameters, and for each member its next centre
+// x_c + A(e) rloc -- formed in float pairs, so a member sits on its cluster
+// to ~1e-15 m -- and its next record.  Members' plane slots follow the
+// sphere rule, the count kept in pl_count between planes.
+template <unsigned int NT, unsigned int OCC>
+__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_cluster_bodies(const __grid_constant__ ContactLaunch c)
+{
+    __shared__ float smf[(NT / 32) * 6 * 2];
+    const unsigned int cid = blockIdx.x * NT + threadIdx.x;
+    const bool live = cid < c.cl.ns;
+    const unsigned int ne = c.cl.neach;
+    d4 xc = mk4(0, 0, 0, 0);
+    V3<float> vc = v3<float>(0.f, 0.f, 0.f), om = vc;
+    float m = 1.f;
+    if (live) {
+        xc = ld4(c.cpos_cur, cid);
+        vc = vf(d2f3(ld3(c.vel, cid)));
+        om = vf(ang_vel_f(d2f4(ld4(c.ep_cur, cid)), d2f4(ld4(c.ev, cid))));
+        m = d2f_rn(c.mass[cid]);
+    }
+    const df xcd[3] = {split_d(xc.x), split_d(xc.y), split_d(xc.z)};
+    CSum F[3], M[3];
+    unsigned int bits = 0;
+    // lever arm of member j about the cluster centre (FP32)
+    auto arm = [&](d4 ip) {
+        return v3<float>(df_f(df_sub(split_d(ip.x), xcd[0])), df_f(df_sub(split_d(ip.y), xcd[1])),
+                         df_f(df_sub(split_d(ip.z), xcd[2])));
+    };
+    auto add_member = [&](V3<float> d, V3<float> f, V3<float> mm) {
+        const V3<float> t = mm + tcross(d, f);
+        F[0].add(f.x); F[1].add(f.y); F[2].add(f.z);
+        M[0].add(t.x); M[1].add(t.y); M[2].add(t.z);
+    };
+
+    // ------------------------------------------------ planes in id order (impl:817-948)
+    if (c.nplane) {
+        for (unsigned int k = 0; k < c.nplane; ++k) {
+            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool touched = false;
+            for (unsigned int j = 0; live && j < ne; ++j) {
+                const unsigned int id = cid * ne + j;
+                if (k == 0) c.pl_count[id] = 0u;  // the first plane restarts the list (impl:989)
+                const d4 ip = ld4(c.pos_cur, id);
+                bool near = true;
+                if (!c.planedf[k].coh) {
+                    const PlaneF& pf = c.planef[k];
+                    const float dx = (d2f_rn(ip.x) - c.o_hi[0]) - pf.v[0];
+                    const float dy = (d2f_rn(ip.y) - c.o_hi[1]) - pf.v[1];
+                    const float dz = (d2f_rn(ip.z) - c.o_hi[2]) - pf.v[2];
+                    const float wx = dx * pf.v[3] + dy * pf.v[4] + dz * pf.v[5];
+                    const float wy = dx * pf.v[6] + dy * pf.v[7] + dz * pf.v[8];
+                    const float wz = dx * pf.v[9] + dy * pf.v[10] + dz * pf.v[11];
+                    const float lim = d2f_rn(ip.w) + c.margin;
+                    near = fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim &&
+                           wy <= pf.v[13] + lim;
+                }
+                if (!near) continue;
+                const V3<float> d = arm(ip);
+                const V3<float> vm = vc + tcross(om, d);
+                const unsigned int cnt = k == 0 ? 0u : c.pl_count[id];
+                const PlaneOut o = plane_call(&c, k, 0, id, ip, make_float4(vm.x, vm.y, vm.z, m),
+                                              make_float4(om.x, om.y, om.z, 0.f), cnt);
+                bits |= o.bits;
+                if (o.cnt != cnt) c.pl_count[id] = o.cnt;
+                if (o.touched) {
+                    add_member(d, v3<float>(o.f[0], o.f[1], o.f[2]), v3<float>(o.m[0], o.m[1], o.m[2]));
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) f6[q] += o.w[q];
+                    touched = true;
+                }
+            }
+            emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
+        }
+    }
+    if (!live) return;
+
+    // ------------------------------------------------ members' particle-pair and mesh sums
+    for (unsigned int j = 0; j < ne; ++j) {
+        const unsigned int id = cid * ne + j;
+        const float4 fa = reinterpret_cast<const float4*>(c.fA)[id];
+        const float4 fb = reinterpret_cast<const float4*>(c.fB)[id];
+        add_member(arm(ld4(c.pos_cur, id)), v3<float>(fa.x, fa.y, fa.z), v3<float>(fb.x, fb.y, fb.z));
+    }
+
+    // ------------------------------------------------ integration (impl:224-287, 149-190)
+    const V3<float> Ff = v3<float>(F[0].value(), F[1].value(), F[2].value());
+    const V3<float> Mf = v3<float>(M[0].value(), M[1].value(), M[2].value());
+    const NextBody nx = integrate_f(c, cid, mk3(xc.x, xc.y, xc.z), m, Ff, Mf, true);
+    st4(c.cpos_next, cid, mk4(nx.x.x, nx.x.y, nx.x.z, xc.w));
+    // A(e) of the next Euler parameters in float pairs (rows as rot_rows)
+    const df e0 = split_d(nx.e.x), e1 = split_d(nx.e.y), e2 = split_d(nx.e.z), e3 = split_d(nx.e.w);
+    auto twice = [](df a) { return df{2.f * a.hi, 2.f * a.lo}; };
+    const df p00 = df_mul(e0, e0), p11 = df_mul(e1, e1), p22 = df_mul(e2, e2), p33 = df_mul(e3, e3);
+    const df p01 = df_mul(e0, e1), p02 = df_mul(e0, e2), p03 = df_mul(e0, e3);
+    const df p12 = df_mul(e1, e2), p13 = df_mul(e1, e3), p23 = df_mul(e2, e3);
+    const df R[9] = {twice(df_add_f(df_add(p00, p11), -0.5f)), twice(df_sub(p12, p03)), twice(df_add(p13, p02)),
+                     twice(df_add(p12, p03)), twice(df_add_f(df_add(p00, p22), -0.5f)), twice(df_sub(p23, p01)),
+                     twice(df_sub(p13, p02)), twice(df_add(p23, p01)), twice(df_add_f(df_add(p00, p33), -0.5f))};
+    const df X0[3] = {df_sub(split_d(nx.x.x), df{c.o_hi[0], c.o_lo[0]}),
+                      df_sub(split_d(nx.x.y), df{c.o_hi[1], c.o_lo[1]}),
+                      df_sub(split_d(nx.x.z), df{c.o_hi[2], c.o_lo[2]})};
+    const float3 w = ang_vel_f(nx.ef, nx.ev);
+    const V3<float> wn = vf(w);
+    const double* rl = c.rloc + (size_t)cluster_type(c.cl, cid) * ne * 3;
+    for (unsigned int j = 0; j < ne; ++j) {
+        const unsigned int id = cid * ne + j;
+        const df r0 = split_d(rl[3 * j]), r1 = split_d(rl[3 * j + 1]), r2 = split_d(rl[3 * j + 2]);
+        df d[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            d[a] = df_add(df_add(df_mul(R[3 * a], r0), df_mul(R[3 * a + 1], r1)), df_mul(R[3 * a + 2], r2));
+        const double rad = c.pos_cur[4 * (size_t)id + 3];
+        st4(c.pos_next, id, mk4(nx.x.x + (f2d(d[0].hi) + f2d(d[0].lo)), nx.x.y + (f2d(d[1].hi) + f2d(d[1].lo)),
+                                nx.x.z + (f2d(d[2].hi) + f2d(d[2].lo)), rad));
+        const df X[3] = {df_add(X0[0], d[0]), df_add(X0[1], d[1]), df_add(X0[2], d[2])};
+        const V3<float> dm = v3<float>(d[0].hi, d[1].hi, d[2].hi);
+        const float rh = d2f_rn(rad);
+        emit_rec(c, id, X, rh, d2f_rn(rad - f2d(rh)), nx.v + tcross(wn, dm), m, w, bits);
+    }
+    if (bits) atomicOr(c.status, bits);
+}
+
 template <bool MESH, unsigned int NT, unsigned int STAGE, unsigned int OCC>
 cudaError_t launch_pairs(const ContactLaunch& c, cudaStream_t st)
 {
@@ -1166,25 +1434,29 @@ cudaError_t launch_pairs_nt(const ContactLaunch& c, cudaStream_t st)
     default: return launch_pairs_stage<MESH, 128>(c, st);
     }
 }
-template <unsigned int NT, unsigned int OCC>
+template <bool MESH, unsigned int NT, unsigned int OCC>
 cudaError_t launch_list(const ContactLaunch& c, cudaStream_t st)
 {
-    k_mixed_pairs_list<NT, OCC><<<(c.np + NT - 1) / NT, NT, 0, st>>>(c);
+    k_mixed_pairs_list<MESH, NT, OCC><<<(c.np + NT - 1) / NT, NT, 0, st>>>(c);
     return cudaGetLastError();
 }
-inline cudaError_t launch_list_nt(const ContactLaunch& c, cudaStream_t st)
+template <bool MESH>
+cudaError_t launch_list_nt(const ContactLaunch& c, cudaStream_t st)
 {
     const bool hi = c.tune.occ_pairs == 1024;
     switch (c.tune.nt_pairs) {
-    case 64: return hi ? launch_list<64, 1024>(c, st) : launch_list<64, 768>(c, st);
-    case 256: return hi ? launch_list<256, 1024>(c, st) : launch_list<256, 768>(c, st);
-    default: return hi ? launch_list<128, 1024>(c, st) : launch_list<128, 768>(c, st);
+    case 64: return hi ? launch_list<MESH, 64, 1024>(c, st) : launch_list<MESH, 64, 768>(c, st);
+    case 256: return hi ? launch_list<MESH, 256, 1024>(c, st) : launch_list<MESH, 256, 768>(c, st);
+    default: return hi ? launch_list<MESH, 128, 1024>(c, st) : launch_list<MESH, 128, 768>(c, st);
     }
 }
 template <unsigned int NT, unsigned int OCC>
 cudaError_t launch_bodies(const ContactLaunch& c, cudaStream_t st)
 {
-    k_mixed_bodies<NT, OCC><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
+    if (c.cl.ns)
+        k_mixed_cluster_bodies<NT, OCC><<<(c.cl.ns + NT - 1) / NT, NT, 0, st>>>(c);
+    else
+        k_mixed_bodies<NT, OCC><<<(c.nentry + NT - 1) / NT, NT, 0, st>>>(c);
     return cudaGetLastError();
 }
 template <unsigned int NT>
@@ -1208,7 +1480,7 @@ cudaError_t launch_bodies_occ(const ContactLaunch& c, cudaStream_t st)
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st)
 {
     if (c.nentry == 0) return cudaSuccess;
-    cudaError_t e = c.use_list ? launch_list_nt(c, st)
+    cudaError_t e = c.use_list ? (c.nmesh ? launch_list_nt<true>(c, st) : launch_list_nt<false>(c, st))
                                : (c.nmesh ? launch_pairs_nt<true>(c, st) : launch_pairs_nt<false>(c, st));
     if (e != cudaSuccess) return e;
     switch (c.tune.nt_bodies) {

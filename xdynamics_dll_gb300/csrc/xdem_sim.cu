@@ -130,11 +130,34 @@ int ensure_tables(xdem_sim* s)
     if (e == cudaSuccess)
         e = cudaMemsetAsync(s->bsums, 0, (size_t)nb * 6 * (s->nscene > 1 ? 1 : nbody) * sizeof(double), s->st);
     if (e != cudaSuccess) return XDEM_ERR_ALLOC;
-    if (int r = fused_alloc(s->fs, n, s->nentry, s->precision_mixed(), s->st)) return r;
+    if (int r = fused_alloc(s->fs, n, s->nentry, s->precision_mixed(), s->st,
+                            s->clusters && s->precision_mixed() ? s->ns : 0))
+        return r;
     s->skey = nullptr;
     s->cells_clean = false;
     s->dirty_alloc = false;
+    s->dirty_mesh_bs = true;
     return XDEM_OK;
+}
+
+// Bounding sphere of mesh m at its body's pose for the fused step: centre
+// p + A(e) c_local relative to the grid origin, radius = reach plus the FP32
+// slack of the test (a cohesive mesh material reaches beyond contact: every
+// sphere searches it).
+int push_mesh_bounds(xdem_sim* s, unsigned int m)
+{
+    const SimMesh& sm = s->meshes[m];
+    const double* rec = s->bodies[sm.body].rec;
+    h3 R[3];
+    hrot(rec + XDEM_E0, R);
+    const h3 c = hadd(h3{rec[XDEM_PX], rec[XDEM_PY], rec[XDEM_PZ]},
+                      hglobal(R, h3{sm.c_local[0], sm.c_local[1], sm.c_local[2]}));
+    const h3 rel = hsub(c, h3{s->prm.world_origin.x, s->prm.world_origin.y, s->prm.world_origin.z});
+    const double slack = 1e-6 + 1e-6 * (hlen(rel) + sm.reach);
+    const bool coh = s->body_cp[sm.body].coh != 0.0;
+    const float4 b = make_float4((float)rel.x, (float)rel.y, (float)rel.z,
+                                 coh ? 1e18f : (float)(sm.reach + slack));
+    return fused_set_mesh_bounds(s->fs, m, b, s->st);
 }
 
 int upload_bodies(xdem_sim* s)
@@ -263,6 +286,44 @@ int step_launcher(xdem_sim* s, cudaEvent_t e0, cudaEvent_t e1)
     return cerr(e);
 }
 
+// The cluster table of the mixed step, when the handle's clusters fit it:
+// every type with the same member count (so id / neach is the cluster of any
+// sphere, as impl:485-611 takes it), types tiling the clusters and spheres
+// in order, member offsets for every type, no rolling resistance and no
+// cohesion (the FP64 launcher kernels carry those).  XDEM_ERR_ARG otherwise.
+int mixed_cluster_tab(const xdem_sim* s, ClusterTab& t)
+{
+    t = ClusterTab{};
+    const size_t nco = s->h_xci.size();
+    if (!nco || nco > kMaxClusterTypes) return XDEM_ERR_ARG;
+    const unsigned int neach = s->h_xci[0].neach;
+    if (!neach || s->nrloc < nco * neach) return XDEM_ERR_ARG;
+    unsigned long long ncl = 0;
+    for (size_t k = 0; k < nco; ++k) {
+        const xClusterInformation& x = s->h_xci[k];
+        if (x.neach != neach || x.scid != ncl || (unsigned long long)x.sid != ncl * neach) return XDEM_ERR_ARG;
+        t.first[k] = x.scid;
+        ncl += x.count;
+    }
+    if (ncl != s->ns || ncl * neach != s->np) return XDEM_ERR_ARG;
+    auto plain = [](const device_contact_property& c) { return c.rfric == 0.0 && c.coh == 0.0; };
+    if (s->has_pp && !plain(s->pp_cp)) return XDEM_ERR_ARG;
+    for (const device_contact_property& c : s->body_cp)
+        if (!plain(c)) return XDEM_ERR_ARG;
+    t.ns = s->ns;
+    t.neach = neach;
+    t.ntype = (unsigned int)nco;
+    t.first[nco] = s->ns;
+    return XDEM_OK;
+}
+
+// Steps run on the fused step (sphere scenes of either precision, and
+// mixed cluster scenes) unless the launcher path was asked for.
+bool fused_path(const xdem_sim* s)
+{
+    return !s->cfg.launcher_path && (!s->clusters || s->precision_mixed());
+}
+
 FusedArgs fused_args(xdem_sim* s)
 {
     FusedArgs a{};
@@ -298,6 +359,12 @@ FusedArgs fused_args(xdem_sim* s)
     a.nscene = s->nscene;
     a.scene_of = s->d_scene_of;
     a.scene_plane_first = s->d_scene_plane_first;
+    a.ns_state = s->ns;
+    if (s->clusters) {
+        mixed_cluster_tab(s, a.cl);
+        a.cpos = &s->cpos;
+        a.rloc = s->rloc;
+    }
     return a;
 }
 
@@ -334,6 +401,7 @@ void step_swaps(xdem_sim* s)
 {
     std::swap(s->pos, s->fs.pos_alt);
     std::swap(s->ep, s->fs.ep_alt);
+    if (s->clusters) std::swap(s->cpos, s->fs.cpos_alt);
     if (s->has_pp) {
         std::swap(s->pp_count, s->fs.pp_count2);
         std::swap(s->pp_id, s->fs.pp_id2);
@@ -352,6 +420,7 @@ int capture_step_graph(xdem_sim* s, int slot)
     const void* key[8];
     graph_key(s, key);
     double *pos = s->pos, *pos_alt = s->fs.pos_alt, *ep = s->ep, *ep_alt = s->fs.ep_alt;
+    double *cpos = s->cpos, *cpos_alt = s->fs.cpos_alt;
     unsigned int *c0 = s->pp_count, *c1 = s->fs.pp_count2, *i0 = s->pp_id, *i1 = s->fs.pp_id2;
     double *t0 = s->pp_tsd, *t1 = s->fs.pp_tsd2;
     cudaGraph_t g = nullptr;
@@ -367,6 +436,7 @@ int capture_step_graph(xdem_sim* s, int slot)
     if (g) cudaGraphDestroy(g);
     if (r != XDEM_OK) {
         s->pos = pos; s->fs.pos_alt = pos_alt; s->ep = ep; s->fs.ep_alt = ep_alt;
+        s->cpos = cpos; s->fs.cpos_alt = cpos_alt;
         s->pp_count = c0; s->fs.pp_count2 = c1; s->pp_id = i0; s->fs.pp_id2 = i1;
         s->pp_tsd = t0; s->fs.pp_tsd2 = t1;
         cudaGetLastError();
@@ -388,9 +458,6 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
 {
     if (!cfg || !out || cfg->np == 0 || !(cfg->cell_size > 0) || !(cfg->dt > 0)) return XDEM_ERR_ARG;
     if (cfg->precision != XDEM_FP64 && cfg->precision != XDEM_MIXED) return XDEM_ERR_ARG;
-    // clusters run on the launcher kernels, which are FP64 only: a mixed
-    // request is refused rather than run in another precision
-    if (cfg->precision == XDEM_MIXED && cfg->ns != 0 && cfg->ns != cfg->np) return XDEM_ERR_ARG;
     for (int i = 0; i < 3; ++i) {
         const unsigned int g = cfg->grid_size[i];
         if (!g || (g & (g - 1))) return XDEM_ERR_ARG;
@@ -544,6 +611,7 @@ XDEM_API int xdem_sim_set_clusters(xdem_sim* s, const double* cpos, const xClust
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     s->nco = nco;
     s->nrloc = nrloc;
+    s->h_xci.assign(xci, xci + nco);
     s->prm.nClusterObject = nco;
     s->dirty_bodies = true;
     fused_invalidate(s->fs);
@@ -651,6 +719,15 @@ XDEM_API int xdem_sim_add_mesh(xdem_sim* s, unsigned int ntri, const double* vli
         s->h_dlocal.push_back(loc.x); s->h_dlocal.push_back(loc.y); s->h_dlocal.push_back(loc.z);
         for (int k = 0; k < 9; ++k) s->h_vlist.push_back(v[k]);
     }
+    // bounding sphere of the vertices in the body frame (centroid, reach)
+    double cl[3] = {0.0, 0.0, 0.0};
+    for (unsigned int i = 0; i < 3 * ntri; ++i)
+        for (int k = 0; k < 3; ++k) cl[k] += vlist_local[3 * (size_t)i + k] / (3.0 * ntri);
+    double reach = 0.0;
+    for (unsigned int i = 0; i < 3 * ntri; ++i) {
+        const double* v = vlist_local + 3 * (size_t)i;
+        reach = std::max(reach, hlen(hsub(h3{v[0], v[1], v[2]}, h3{cl[0], cl[1], cl[2]})));
+    }
     s->ntri_total += ntri;
     const size_t nt = s->ntri_total;
     cudaError_t e = dalloc(s->d_tri, nt);
@@ -668,7 +745,8 @@ XDEM_API int xdem_sim_add_mesh(xdem_sim* s, unsigned int ntri, const double* vli
     std::memcpy(b.rec, body, sizeof(b.rec));
     s->bodies.push_back(b);
     s->body_cp.push_back(*cp);
-    s->meshes.push_back(SimMesh{ntri, first, (int)s->bodies.size() - 1});
+    s->meshes.push_back(SimMesh{ntri, first, (int)s->bodies.size() - 1, {cl[0], cl[1], cl[2]}, reach});
+    s->dirty_mesh_bs = true;
     s->dirty_bodies = true;
     s->dirty_alloc = true;
     if (body_index) *body_index = (int)s->bodies.size() - 1;
@@ -714,6 +792,10 @@ XDEM_API int xdem_sim_set_body(xdem_sim* s, int body_index, const double body[15
         e = launch_update_mesh(s->d_body + 15 * body_index, s->d_vlist + 9 * (size_t)m.first,
                                s->d_sphere + 4 * (size_t)m.first, s->d_dlocal + 3 * (size_t)m.first,
                                s->d_tri + m.first, m.ntri, s->st);
+        // the fused step: the mesh spheres change cells, so the next step
+        // sorts, and the mesh's bounding sphere moves with it
+        if (e == cudaSuccess && fused_force_sort(s->fs, s->st) != XDEM_OK) e = cudaErrorUnknown;
+        if (e == cudaSuccess && push_mesh_bounds(s, b.index) != XDEM_OK) e = cudaErrorUnknown;
     }
     // the pinned-free host record must stay valid until the copy ran
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
@@ -724,6 +806,12 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->clusters && !s->xci) return XDEM_ERR_ARG;
+    // mixed clusters: the fused step's cluster form (one member count, no
+    // rolling resistance or cohesion)
+    if (s->clusters && s->precision_mixed()) {
+        ClusterTab t;
+        if (int r = mixed_cluster_tab(s, t)) return r;
+    }
     // a batch needs its planes in place and no meshes (no body wrenches)
     if (s->nscene > 1 && (s->scene_plane_first.back() != s->planes.size() || !s->meshes.empty()))
         return XDEM_ERR_ARG;
@@ -732,6 +820,11 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
     if (s->dirty_alloc || s->dirty_bodies || !s->fs.primed) drop_graph(s);
     if (int r = ensure_tables(s)) return r;
     if (int r = upload_bodies(s)) return r;
+    if (s->dirty_mesh_bs) {
+        for (unsigned int m = 0; m < s->meshes.size(); ++m)
+            if (int r = push_mesh_bounds(s, m)) return r;
+        s->dirty_mesh_bs = false;
+    }
     s->launches = 0;
     if (s->profiling && !s->pe0[0]) {
         for (int i = 0; i < xdem_sim::kProfEvents; ++i) {
@@ -740,7 +833,7 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
         }
     }
     unsigned int recorded = 0;
-    const bool fused = !s->cfg.launcher_path && !s->clusters;
+    const bool fused = fused_path(s);
     if (s->use_graph && fused && !s->profiling) {
         // eager steps until the step has been primed, then one graph per
         // arrangement of the double buffers, each replayed with the host
@@ -785,7 +878,7 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
         int r;
         const bool rec = s->profiling && recorded < (unsigned int)xdem_sim::kProfEvents;
         cudaEvent_t e0 = rec ? s->pe0[recorded] : nullptr, e1 = rec ? s->pe1[recorded] : nullptr;
-        if (s->cfg.launcher_path || s->clusters) {
+        if (!fused) {
             r = step_launcher(s, e0, e1);
         } else {
             FusedArgs a = fused_args(s);

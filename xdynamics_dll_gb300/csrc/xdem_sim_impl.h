@@ -26,6 +26,8 @@ struct SimBody {
 struct SimMesh {
     unsigned int ntri, first;  // triangles [first, first + ntri) of the global arrays
     int body;
+    double c_local[3];         // centroid of the vertices (body frame)
+    double reach;              // largest vertex distance from it
 };
 
 struct xdem_sim {
@@ -42,6 +44,7 @@ struct xdem_sim {
     double *force = nullptr, *moment = nullptr, *mass = nullptr, *inertia = nullptr, *tmax = nullptr,
            *rres = nullptr, *rloc = nullptr;
     xClusterInformation* xci = nullptr;
+    std::vector<xClusterInformation> h_xci;  // host copy of the cluster table
     // grid
     unsigned int nentry = 0;
     size_t ncell = 0;
@@ -75,6 +78,7 @@ struct xdem_sim {
     unsigned int* d_status = nullptr;
     bool dirty_bodies = true;      // device body tables need upload
     bool dirty_alloc = true;       // contact tables need (re)allocation
+    bool dirty_mesh_bs = true;     // the fused step's mesh bounding spheres need refreshing
     // fused path
     FusedState fs{};
     bool precision_mixed() const;

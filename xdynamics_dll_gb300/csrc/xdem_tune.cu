@@ -26,7 +26,7 @@ struct Snapshot {
         const size_t bytes[] = {n * 32, ns * 24, ns * 24, ns * 32, ns * 32, ns * 32,
                                 n * 4, n * MAX_P2P_COUNT * 4, n * MAX_P2P_COUNT * 16,
                                 n * 4, n * MAX_P2PL_COUNT * 4, n * MAX_P2PL_COUNT * 16,
-                                n * 4, n * MAX_P2MS_COUNT * 4, n * MAX_P2MS_COUNT * 16};
+                                n * 4, n * MAX_P2MS_COUNT * 4, n * MAX_P2MS_COUNT * 16, ns * 32};
         void** fields[] = {reinterpret_cast<void**>(&s->pos), reinterpret_cast<void**>(&s->vel),
                            reinterpret_cast<void**>(&s->acc), reinterpret_cast<void**>(&s->ep),
                            reinterpret_cast<void**>(&s->ev), reinterpret_cast<void**>(&s->ea),
@@ -34,7 +34,7 @@ struct Snapshot {
                            reinterpret_cast<void**>(&s->pp_tsd), reinterpret_cast<void**>(&s->pl_count),
                            reinterpret_cast<void**>(&s->pl_id), reinterpret_cast<void**>(&s->pl_tsd),
                            reinterpret_cast<void**>(&s->ms_count), reinterpret_cast<void**>(&s->ms_id),
-                           reinterpret_cast<void**>(&s->ms_tsd)};
+                           reinterpret_cast<void**>(&s->ms_tsd), reinterpret_cast<void**>(&s->cpos)};
         for (size_t i = 0; i < sizeof(bytes) / sizeof(bytes[0]); ++i) {
             if (!*fields[i]) continue;
             void* c = nullptr;
@@ -106,7 +106,7 @@ XDEM_API int xdem_sim_autotune(xdem_sim* s, unsigned int trial_steps, xdem_tune*
 {
     if (!s || !best || trial_steps == 0) return XDEM_ERR_ARG;
     // only the mixed fused step has shapes to choose
-    if (!s->precision_mixed() || s->cfg.launcher_path || s->clusters) {
+    if (!s->precision_mixed() || s->cfg.launcher_path) {
         xdem_sim_get_tune(s, best);
         if (nall) *nall = 0;
         return XDEM_OK;

@@ -371,6 +371,128 @@ def wheel_mesh(radius=0.15, width=0.1, n_around=100, n_width=4):
     return np.array(tris, dtype=np.float64).reshape(-1, 9)
 
 
+def tyre_mesh(radius=0.15, width=0.1, n_around=320, n_width=32):
+    """Tyre surface of a wheel (open cylinder, axis along z, body frame):
+    n_around x n_width quads, each split into two triangles, wound so that
+    the normals (P->Q x P->R) point outward."""
+    ang = 2 * np.pi * np.arange(n_around + 1) / n_around
+    zs = np.linspace(-0.5 * width, 0.5 * width, n_width + 1)
+    cx, cy = radius * np.cos(ang), radius * np.sin(ang)
+    tris = np.empty((n_around * n_width * 2, 9))
+    t = 0
+    for k in range(n_width):
+        for j in range(n_around):
+            a = (cx[j], cy[j], zs[k]); b = (cx[j + 1], cy[j + 1], zs[k])
+            c = (cx[j + 1], cy[j + 1], zs[k + 1]); d = (cx[j], cy[j], zs[k + 1])
+            tris[t] = (*a, *c, *b)
+            tris[t + 1] = (*a, *d, *c)
+            t += 2
+    return tris
+
+
+def fit_sphere_radius(tris, ft=0.8):
+    """Radius of the sphere FitSphereToTriangle(P, Q, R, ft) fits to each
+    triangle (xUtilityFunction.cpp:379-416): its iteration converges to the
+    sphere through the circumcircle whose centre lies on the normal at
+    distance d with d / r = ft, i.e. r = (circumradius) / sqrt(1 - ft^2)."""
+    P, Q, R = tris[:, 0:3], tris[:, 3:6], tris[:, 6:9]
+    a = np.linalg.norm(Q - R, axis=1)
+    b = np.linalg.norm(R - P, axis=1)
+    c = np.linalg.norm(P - Q, axis=1)
+    area = 0.5 * np.linalg.norm(np.cross(Q - P, R - P), axis=1)
+    return (a * b * c) / (4.0 * area) / np.sqrt(1.0 - ft * ft)
+
+
+def wheel_testbed(ncluster=2_000_000, neach=3, sub_r=2e-3, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3,
+                  dt=1e-5, trough=(1.0, 0.3, 0.15), wheel_r=0.15, wheel_w=0.1, n_around=320, n_width=32,
+                  omega=2.0, wheel_mass=20.0, sink=1e-4, seed=2024):
+    """Wheel on a bed of rigid clumps of `neach` spheres (sub-radius sub_r)
+    in a trough of five planes, x along the trough.
+
+    Clumps lie along x (members 1.9 sub_r apart, as cluster_bed) with a
+    seeded spin about that axis, in columns: clumps of one column touch with
+    1e-3 sub_r overlap (so every member has a contact above and below from
+    t = 0), neighbouring columns are 0.1 mm apart in z and 0.2 mm end to end
+    in x.  Clumps are numbered layer by layer, x fastest, so that clumps
+    touching in a column are far apart in id and the reference's skip of
+    partners with |id - k| <= neach (impl:556-558) drops none of their
+    contacts.  The bed fills the trough's footprint and rises above it: the
+    walls are extended to the bed's height (2,000,000 clumps of 2 mm spheres
+    stand about 2.6 m tall on a 1.0 x 0.15 m floor).
+
+    The wheel: a tyre surface of n_around x n_width quads (20,480 triangles
+    by default) of radius wheel_r and width wheel_w, axis along z, centred
+    over the trough at x = trough/2, sunk `sink` (0.1 mm: the spheres of
+    the top layer within about 5 mm of the tyre's lowest line touch it) into
+    the top of the bed's last complete layer, driven at `omega` rad/s
+    (rolling toward +x) through its body record.  Its
+    surface is invariant under rotation about the axis, so the drive needs
+    no re-posing of the triangles between steps.  The cell size follows
+    xDiscreteElementMethodSimulation.cpp:91-99: twice the largest radius of
+    particles and mesh spheres."""
+    rng = np.random.default_rng(seed)
+    sp = 2.0 * sub_r * 0.95
+    rloc = np.zeros((neach, 3))
+    rloc[:, 0] = (np.arange(neach) - 0.5 * (neach - 1)) * sp
+    half = float(np.abs(rloc[:, 0]).max()) + sub_r
+    px = 2.0 * half + 2e-4
+    pz = 2.0 * sub_r + 1e-4
+    py = 2.0 * sub_r * (1.0 - 1e-3)
+    nx = max(1, int(np.floor(trough[0] / px)))
+    nz = max(1, int(np.floor(trough[2] / pz)))
+    per_layer = nx * nz
+    ny = -(-ncluster // per_layer)
+    k = np.arange(ncluster)
+    ix, iz, iy = k % nx, (k // nx) % nz, k // per_layer
+    x0 = 0.5 * (trough[0] - nx * px)
+    z0 = 0.5 * (trough[2] - nz * pz)
+    cent = np.stack([x0 + (ix + 0.5) * px, sub_r * (1.0 - 1e-3) + iy * py, z0 + (iz + 0.5) * pz], 1)
+    # spin about x: e = (cos a/2, sin a/2, 0, 0)
+    a = rng.uniform(0.0, 2.0 * np.pi, ncluster)
+    q = np.zeros((ncluster, 4))
+    q[:, 0] = np.cos(0.5 * a)
+    q[:, 1] = np.sin(0.5 * a)
+    ns = ncluster
+    N = ns * neach
+    pos = np.empty((N, 4))
+    pos[:, 0] = (cent[:, None, 0] + rloc[None, :, 0]).ravel()
+    pos[:, 1] = np.repeat(cent[:, 1], neach)
+    pos[:, 2] = np.repeat(cent[:, 2], neach)
+    pos[:, 3] = sub_r
+    cpos = np.zeros((ns, 4))
+    cpos[:, :3] = cent
+    cpos[:, 3] = sub_r
+    m1 = rho * (4.0 / 3.0) * np.pi * sub_r ** 3
+    mass = np.full(ns, m1 * neach)
+    J3 = np.array([m1 * np.sum(rloc[:, 1] ** 2 + rloc[:, 2] ** 2), m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 2] ** 2),
+                   m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 1] ** 2)])
+    J3 = J3 + (2.0 / 5.0) * m1 * sub_r ** 2 * neach  # as cluster_bed: a row of spheres gets its own spin inertia
+    inertia = np.tile(J3, ns)
+    vel, acc, ep, ev, ea = _init_state(ns)
+    ep = q.ravel().copy()
+    xci = np.array([0, 0, ns, neach], dtype=np.uint32)
+    # the wheel rests on the last complete layer (a partial top layer fills
+    # rows from z = 0 and need not reach under the tyre)
+    full = max(1, ncluster // per_layer)
+    top = sub_r * (1.0 - 1e-3) + (full - 1) * py + sub_r
+    tyre = tyre_mesh(wheel_r, wheel_w, n_around, n_width)
+    r_ms = float(fit_sphere_radius(tyre).max())
+    cell = 2.0 * max(sub_r, r_ms)
+    wc = (0.5 * trough[0], top + wheel_r - sink, 0.5 * trough[2])
+    height = max(trough[1], wc[1] + wheel_r + 0.05)
+    cp = default_material(E, nu, rest, fric)
+    planes = open_box_planes(0.0, trough[0], 0.0, height, 0.0, trough[2])
+    origin = (-0.02, -0.02, -0.02)
+    grid = tuple(pow2_at_least(int(np.ceil((ext + 0.04) / cell)) + 1) for ext in (trough[0], height, trough[2]))
+    body = T.body_record(mass=wheel_mass, pos=wc, ed=(0.0, 0.0, 0.0, -0.5 * omega))
+    return Scene(np_=N, ns=ns, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=mass,
+                 inertia=inertia, dt=dt, cell_size=cell, grid=grid, origin=origin, pp_cp=cp, planes=planes,
+                 plane_cp=[cp] * len(planes), plane_body=[T.body_record() for _ in planes],
+                 meshes=[dict(vlist_local=tyre, body=body, cp=cp)], cpos=cpos.ravel(), xci=xci,
+                 rloc=rloc.ravel(), name="wheel_testbed",
+                 note=f"{ns} clumps x {neach} spheres, {ny} layers, tyre {tyre.shape[0]} triangles")
+
+
 def column_collapse(n_target=65536, r=1.5e-3, R=0.1, H=0.3, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3,
                     dt=1e-5, seed=5150, v0=0.0, floor_half=0.5, jitter=0.1):
     """Column collapse of the differentiable-calibration configuration:
