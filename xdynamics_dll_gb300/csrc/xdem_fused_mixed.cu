@@ -819,30 +819,42 @@ struct NextBody {
     float4 ef, ev;
     V3<float> v;
 };
+// The state integrate_f reads for body i (FP64, reference layout).
+struct BodyIn {
+    d3 v, a, J;
+    d4 e, ev, ea;
+};
+__device__ __forceinline__ BodyIn body_in(const ContactLaunch& c, unsigned int i)
+{
+    BodyIn b;
+    b.v = ld3(c.vel, i); b.a = ld3(c.acc, i); b.J = ld3(c.inertia, i);
+    b.e = ld4(c.ep_cur, i); b.ev = ld4(c.ev, i); b.ea = ld4(c.ea, i);
+    return b;
+}
 __device__ __forceinline__ NextBody integrate_f(const ContactLaunch& c, unsigned int i, d3 xi, float m,
-                                                V3<float> Ff, V3<float> Mf, bool apply_vel)
+                                                V3<float> Ff, V3<float> Mf, bool apply_vel, const BodyIn& in)
 {
     const float dt = c.dt_f, hdt = c.hdt_f, h2 = c.h2_f;
     const float inv_m = 1.f / m;
     const V3<float> a_new = v3<float>(Ff.x * inv_m + c.g_f[0], Ff.y * inv_m + c.g_f[1], Ff.z * inv_m + c.g_f[2]);
     NextBody o;
     // translation
-    const d3 v = ld3(c.vel, i);
+    const d3 v = in.v;
     V3<float> vn = vf(d2f3(v));
     if (apply_vel) {
-        const V3<float> dv = hdt * (vf(d2f3(ld3(c.acc, i))) + a_new);
+        const V3<float> dv = hdt * (vf(d2f3(in.a)) + a_new);
         st3(c.vel, i, mk3(v.x + f2d(dv.x), v.y + f2d(dv.y), v.z + f2d(dv.z)));
         vn = vn + dv;
     }
     st3(c.acc, i, mk3(f2d(a_new.x), f2d(a_new.y), f2d(a_new.z)));
     // rotation
-    const d4 e = ld4(c.ep_cur, i);
+    const d4 e = in.e;
     const df e0 = split_d(e.x), e1 = split_d(e.y), e2 = split_d(e.z), e3 = split_d(e.w);
     const float4 ef = make_float4(df_f(e0), df_f(e1), df_f(e2), df_f(e3));
-    const d4 ev = ld4(c.ev, i);
+    const d4 ev = in.ev;
     const float4 evf = d2f4(ev);
-    const float4 eaf = d2f4(ld4(c.ea, i));
-    const float3 J = d2f3(ld3(c.inertia, i));
+    const float4 eaf = d2f4(in.ea);
+    const float3 J = d2f3(in.J);
     const float4 q = uceom_f(J, ef, evf, to_local_f(make_float3(Mf.x, Mf.y, Mf.z), ef));
     const float4 dev = make_float4(hdt * (eaf.x + q.x), hdt * (eaf.y + q.y), hdt * (eaf.z + q.z), hdt * (eaf.w + q.w));
     st4(c.ev, i, mk4(ev.x + f2d(dev.x), ev.y + f2d(dev.y), ev.z + f2d(dev.z), ev.w + f2d(dev.w)));
@@ -934,15 +946,17 @@ __device__ __forceinline__ void emit_rec(const ContactLaunch& c, unsigned int oi
 }
 
 // Sphere tail: integration, the next position and the next record.
-__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float4 Ai, float4 Li,
-                                           float4 Bi, V3<float> Ff, V3<float> Mf, unsigned int& bits)
+// rh + rl: the radius as the record's float pair; m: the mass in FP32.
+__device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int oid, d4 ip, float rh, float rl,
+                                           float m, V3<float> Ff, V3<float> Mf, unsigned int& bits,
+                                           const BodyIn& in)
 {
-    const NextBody nx = integrate_f(c, oid, mk3(ip.x, ip.y, ip.z), Bi.w, Ff, Mf, !c.vel_compat);
+    const NextBody nx = integrate_f(c, oid, mk3(ip.x, ip.y, ip.z), m, Ff, Mf, !c.vel_compat, in);
     st4(c.pos_next, oid, mk4(nx.x.x, nx.x.y, nx.x.z, ip.w));
     const df X[3] = {df_sub(split_d(nx.x.x), df{c.o_hi[0], c.o_lo[0]}),
                      df_sub(split_d(nx.x.y), df{c.o_hi[1], c.o_lo[1]}),
                      df_sub(split_d(nx.x.z), df{c.o_hi[2], c.o_lo[2]})};
-    emit_rec(c, oid, X, Ai.w, Li.w, nx.v, Bi.w, ang_vel_f(nx.ef, nx.ev), bits);
+    emit_rec(c, oid, X, rh, rl, nx.v, m, ang_vel_f(nx.ef, nx.ev), bits);
     if (bits) atomicOr(c.status, bits);
 }
 
@@ -1188,18 +1202,26 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     __shared__ float smf[(NT / 32) * 6 * 2];
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = oid < c.np;
-    float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
+    // the record's velocity + mass (B) and spin (C) are read only by a sphere
+    // that meets a plane or has rolling resistance (one 32-byte sector); the
+    // radius and mass come from the FP64 state, rounded as the record holds them
+    float4 Bi = make_float4(0.f, 0.f, 0.f, 0.f), Ci = Bi;
+    bool have_bc = false;
+    auto need_bc = [&]() {
+        if (have_bc) return;
+        const float4* r = c.rec + 4 * (size_t)oid;
+        Bi = r[kRecB];
+        Ci = r[kRecC];
+        have_bc = true;
+    };
     d4 ip = mk4(0, 0, 0, 0);
+    float rh = 0.f;
     Acc acc;
     acc.tm = v3<float>(0.f, 0.f, 0.f);
     acc.rs = 0.f;
     if (live) {
-        const float4* r = c.rec + 4 * (size_t)oid;
-        Ai = r[kRecA];
-        Li = r[kRecL];
-        Bi = r[kRecB];
-        Ci = r[kRecC];
         ip = ld4(c.pos_cur, oid);
+        rh = d2f_rn(ip.w);
         const float4 fa = reinterpret_cast<const float4*>(c.fA)[oid];
         const float4 fb = reinterpret_cast<const float4*>(c.fB)[oid];
         acc.f[0].hi = fa.x; acc.f[1].hi = fa.y; acc.f[2].hi = fa.z;
@@ -1211,13 +1233,12 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
         }
     }
     unsigned int bits = 0;
-    const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
 
     // ------------------------------------------------ planes in id order (impl:950-1080)
     if (c.nplane) {
         float4 ipf = make_float4(0.f, 0.f, 0.f, -1.f);
         if (live)
-            ipf = make_float4(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2], Ai.w);
+            ipf = make_float4(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2], rh);
         unsigned int pl_cnt = 0;
         // a batched scene sees only its own planes and keeps no wrenches (no
         // block reduction, so threads may walk different plane ranges)
@@ -1241,6 +1262,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
                 near = fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
             }
             if (live && near) {
+                need_bc();
                 const PlaneOut o = plane_call(&c, k, kbeg, oid, ip, Bi, Ci, pl_cnt);
                 touched = o.touched != 0;
                 pl_cnt = o.cnt;
@@ -1267,6 +1289,8 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     // ------------------------------------------------ rolling resistance (impl:2420-2454)
     V3<float> Mf = v3<float>(acc.m[0].value(), acc.m[1].value(), acc.m[2].value());
     if (acc.rs != 0.f) {
+        need_bc();
+        const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
         const float J = d2f_rn(c.inertia[oid]);  // scalar read of the double3 array, as impl:2434
         const V3<float> T = (J * c.dt_f) * iom - acc.tm;
         const float lT2 = tdot(T, T);
@@ -1278,7 +1302,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
         }
     }
     const V3<float> Ff = v3<float>(acc.f[0].value(), acc.f[1].value(), acc.f[2].value());
-    mixed_tail(c, oid, ip, Ai, Li, Bi, Ff, Mf, bits);
+    mixed_tail(c, oid, ip, rh, d2f_rn(ip.w - f2d(rh)), d2f_rn(c.mass[oid]), Ff, Mf, bits, body_in(c, oid));
 }
 
 // Kernel 2 for clusters (impl:817-948, 224-287, 149-190): one thread per
@@ -1373,7 +1397,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_cluster_bodies(const __g
     // ------------------------------------------------ integration (impl:224-287, 149-190)
     const V3<float> Ff = v3<float>(F[0].value(), F[1].value(), F[2].value());
     const V3<float> Mf = v3<float>(M[0].value(), M[1].value(), M[2].value());
-    const NextBody nx = integrate_f(c, cid, mk3(xc.x, xc.y, xc.z), m, Ff, Mf, true);
+    const NextBody nx = integrate_f(c, cid, mk3(xc.x, xc.y, xc.z), m, Ff, Mf, true, body_in(c, cid));
     st4(c.cpos_next, cid, mk4(nx.x.x, nx.x.y, nx.x.z, xc.w));
     // A(e) of the next Euler parameters in float pairs (rows as rot_rows)
     const df e0 = split_d(nx.e.x), e1 = split_d(nx.e.y), e2 = split_d(nx.e.z), e3 = split_d(nx.e.w);
