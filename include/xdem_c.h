@@ -44,6 +44,7 @@ extern "C" {
 /* Pair-list capacities per particle (decl:13-16). */
 #define MAX_P2P_COUNT 12
 #define MAX_P2PL_COUNT 3
+#define MAX_P2CY_COUNT 3
 #define MAX_P2MS_COUNT 5
 /* Size in bytes of the 15-double rigid-body record (decl:18). */
 #define DEVICE_BODY_MEM_SIZE 120
@@ -62,6 +63,10 @@ enum {
     XDEM_ERR_P2MS_OVERFLOW = 1 << 2,  /* > MAX_P2MS_COUNT triangle contacts  */
     XDEM_ERR_TRI_CANDIDATES = 1 << 3, /* > 20 face/edge/vertex candidates    */
     XDEM_ERR_NONFINITE     = 1 << 4,  /* NaN/Inf position seen by the hash   */
+    XDEM_ERR_P2CY_OVERFLOW = 1 << 5,  /* > MAX_P2CY_COUNT cylinder contacts
+                                         (the reference writes on past the
+                                         particle's slots; here they are
+                                         dropped and this bit is raised)     */
     XDEM_ERR_CUDA          = 1 << 8,  /* a CUDA runtime call failed          */
     XDEM_ERR_ARG           = 1 << 9,  /* invalid argument (null, size, mode) */
     XDEM_ERR_NOT_SET       = 1 << 10, /* setDEMSymbolicParameter not called  */
@@ -108,6 +113,19 @@ typedef struct device_plane_info {
     double l1, l2;
     xdem_double3 u1, u2, uw, xw, pa, pb, w2, w3, w4;
 } device_plane_info;
+
+/* decl:220-228: a cylinder in its body frame -- base and top centres,
+ * len_rr = (length, base radius, top radius), wall thickness, and which part
+ * is open (empty_part, xCylinderObject.h:14: 0 none, 1 top circle, 2 bottom
+ * circle, 3 both, 4 radial wall; the contact kernels test 1 and 2) */
+typedef struct device_cylinder_info {
+    unsigned int id;
+    unsigned int empty_part;
+    double thickness;
+    xdem_double3 len_rr;
+    xdem_double3 pbase;
+    xdem_double3 ptop;
+} device_cylinder_info;
 
 /* decl:230-243; filled in the order of xContact.cpp:308-312 */
 typedef struct device_contact_property {
@@ -270,6 +288,31 @@ XDEM_API int cu_cluster_plane_contact(device_plane_info* plan, double* dbi,
                                       unsigned int* pair_id, double* tsd,
                                       xClusterInformation* xci,
                                       unsigned int np);
+/* decl:326-335, def:209-238: particles against one cylinder posed by the
+ * 15-double record bi; pairs in MAX_P2CY_COUNT slots per particle (the
+ * reference's xParticleCylinderContact arrays); body force partials as the
+ * plane launcher */
+XDEM_API int cu_cylinder_contact_force(device_cylinder_info* cyl, double* bi,
+                                       device_contact_property* cp,
+                                       double* pos, double* ep, double* vel,
+                                       double* omega, double* force,
+                                       double* moment, double* mass,
+                                       double* tmax, double* rres,
+                                       unsigned int* pair_count,
+                                       unsigned int* pair_id, double* tsd,
+                                       unsigned int np);
+/* decl:366-373, def:395-420 */
+XDEM_API int cu_cluster_cylinder_contact(device_cylinder_info* cyl, double* bi,
+                                         xClusterInformation* xci,
+                                         device_contact_property* cp,
+                                         double* pos, double* cpos,
+                                         double* ep, double* vel,
+                                         double* omega, double* force,
+                                         double* moment, double* mass,
+                                         double* tmax, double* rres,
+                                         unsigned int* pair_count,
+                                         unsigned int* pair_id, double* tsd,
+                                         unsigned int np);
 /* decl:373-381, def:422-471 */
 XDEM_API int cu_cluster_meshes_contact(
     device_triangle_info* dpi, double* dbi, double* pos, double* cpos,

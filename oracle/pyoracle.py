@@ -120,6 +120,15 @@ class Oracle:
                                  C.c_uint(np_), C.c_uint(ntri), C.byref(st))
         return st.value
 
+    def cylinder(self, prm, cyl, dbi, cp, bf, pos, cpos, ep, vel, ev, force, moment, mass, tmax, rres, pc, pid,
+                 tsd, xci, np_):
+        """xo_cylinder: cpos None for free spheres."""
+        st = C.c_uint(0)
+        self.lib.xo_cylinder(C.byref(prm), C.byref(cyl), _p(dbi), C.byref(cp), *[_p(b) for b in bf], _p(pos),
+                             _p(cpos), _p(ep), _p(vel), _p(ev), _p(force), _p(moment), _p(mass), _p(tmax), _p(rres),
+                             _p(pc), _p(pid), _p(tsd), _p(xci), C.c_uint(np_), C.byref(st))
+        return st.value
+
     def cluster_rolling(self, prm, tmax, rres, inertia, ep, ev, moment, xci, np_):
         self.lib.xo_cluster_rolling(C.byref(prm), _p(tmax), _p(rres), _p(inertia), _p(ep), _p(ev), _p(moment),
                                     _p(xci), C.c_uint(np_))

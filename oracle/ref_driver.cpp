@@ -196,6 +196,34 @@ void ref_cluster_mesh(void* dti, double* dbi, double* fx, double* fy, double* fz
     });
 }
 
+void ref_cylinder(void* cyl, double* bi, double* fx, double* fy, double* fz, double* mx, double* my, double* mz,
+                  double* pos, double* ep, double* vel, double* ev, double* force, double* moment, void* cp,
+                  double* mass, double* tmax, double* rres, unsigned int* pair_count, unsigned int* pair_id,
+                  double* tsd, unsigned int np)
+{
+    launch(np, [&] {
+        cylinder_contact_force_kernel((device_cylinder_info*)cyl, bi, fx, fy, fz, mx, my, mz, (double4*)pos,
+                                      (double4*)ep, (double3*)vel, (double4*)ev, (double3*)force,
+                                      (double3*)moment, (device_contact_property*)cp, mass, (double3*)tmax, rres,
+                                      pair_count, pair_id, (double2*)tsd, np);
+    });
+}
+
+void ref_cluster_cylinder(void* cyl, double* bi, double* fx, double* fy, double* fz, double* mx, double* my,
+                          double* mz, double* pos, double* cpos, double* ep, double* vel, double* ev,
+                          double* force, double* moment, void* xci, void* cp, double* mass, double* tmax,
+                          double* rres, unsigned int* pair_count, unsigned int* pair_id, double* tsd,
+                          unsigned int np)
+{
+    launch(np, [&] {
+        cluster_cylinder_contact_force_kernel((device_cylinder_info*)cyl, bi, fx, fy, fz, mx, my, mz,
+                                              (double4*)pos, (double4*)cpos, (double4*)ep, (double3*)vel,
+                                              (double4*)ev, (double3*)force, (double3*)moment,
+                                              (xClusterInformation*)xci, (device_contact_property*)cp, mass,
+                                              (double3*)tmax, rres, pair_count, pair_id, (double2*)tsd, np);
+    });
+}
+
 void ref_cluster_rolling(double* tmax, double* rres, double* inertia, double* ep, double* ev, double* moment,
                          void* xci, unsigned int np)
 {

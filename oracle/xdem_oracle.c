@@ -1196,6 +1196,245 @@ void xo_cluster_plane(const device_dem_parameters* prm, const device_plane_info*
     }
 }
 
+/* ======================================================================== */
+/* Cylinders (impl:1083-1600)                                                */
+/* ======================================================================== */
+/* Base and top centres of the cylinder at its body pose. */
+static void cylinder_ends(const device_cylinder_info* cy, const double* bi, v3* pos, v4* e, v3* base, v3* top)
+{
+    *pos = mk3(bi[XDEM_PX], bi[XDEM_PY], bi[XDEM_PZ]);
+    *e = mk4(bi[XDEM_E0], bi[XDEM_E1], bi[XDEM_E2], bi[XDEM_E3]);
+    *base = add3(*pos, to_global(dv3(cy->pbase), *e));
+    *top = add3(*pos, to_global(dv3(cy->ptop), *e));
+}
+
+/* impl:1189-1288.  Depth of sphere (p, r) against the cylinder and the unit
+ * vector of the contact: on the side (the axis parameter t in [0, 1]) the
+ * radial direction, the depth measured against len_rr.y and the inside test
+ * against len_rr.z (an inside contact flips the normal); beyond the ends the
+ * annulus of the wall thickness, else the rim point found through the angle
+ * atan(x / z) of the local offset, as the reference forms it. */
+static double cylinder_detection(const device_cylinder_info* cy, const double* bi, v3 p, v3* u, double r,
+                                 int* inner)
+{
+    v3 cyl_pos, base, top;
+    v4 e;
+    cylinder_ends(cy, bi, &cyl_pos, &e, &base, &top);
+    v3 ab = sub3(top, base);
+    double t = dot3(sub3(p, base), ab) / dot3(ab, ab);
+    v3 c = add3(base, mul3(t, ab));
+    double dist = len3(sub3(p, c));
+    if (t >= 0 && t <= 1) {
+        if (dist == 0) {
+            *inner = 1;
+            return 0;
+        }
+        *u = div3(sub3(c, p), dist);
+        if (dist < cy->len_rr.z) {
+            *inner = 1;
+            *u = neg3(*u);
+            return dist + r - cy->len_rr.y;
+        }
+        return cy->len_rr.y + r - dist;
+    }
+    double thick = cy->thickness;
+    int one = thick != 0.0 ? 1 : 0;
+    if (dist < cy->len_rr.z + thick && dist > one * cy->len_rr.z) {
+        v3 o2c = sub3(cyl_pos, c);
+        double l = len3(o2c);
+        *u = div3(o2c, l);
+        return cy->len_rr.x * 0.5 + r - l;
+    }
+    v3 at = to_local(sub3(p, top), e);
+    v3 cp = top;
+    if (fabs(at.y) > cy->len_rr.x) {
+        at = to_local(sub3(p, base), e);
+        cp = base;
+    }
+    double pi = atan(at.x / at.z);
+    v3 q = mk3(0, 0, 0);
+    if (pi < 0 && at.z < 0) q.x = cy->len_rr.z * sin(-pi);
+    else if (pi > 0 && at.x < 0 && at.z < 0) q.x = cy->len_rr.z * sin(-pi);
+    else q.x = cy->len_rr.z * sin(pi);
+    q.z = cy->len_rr.z * cos(pi);
+    if (at.z < 0 && q.z > 0) q.z = -q.z;
+    else if (at.z > 0 && q.z < 0) q.z = -q.z;
+    q.y = 0.;
+    cp = add3(cp, to_global(q, e));
+    v3 dv = sub3(cp, p);
+    dist = len3(dv);
+    *u = div3(dv, dist);
+    if (dist < r) return r - dist;
+    return -1.0;
+}
+
+/* impl:1290-1322.  Inside a cylinder, the cap the sphere faces: none near
+ * an open end (empty 1: top, t > 0.6; empty 2: base, t < 0.4). */
+static double cylinder_inner_cap(const device_cylinder_info* cy, const double* bi, v3 p, v3* u, v3* cpt,
+                                 unsigned int empty, double r)
+{
+    v3 cyl_pos, base, top;
+    v4 e;
+    cylinder_ends(cy, bi, &cyl_pos, &e, &base, &top);
+    v3 ab = sub3(top, base);
+    double t = dot3(sub3(p, base), ab) / dot3(ab, ab);
+    v3 c = add3(base, mul3(t, ab));
+    double dist = len3(sub3(p, c));
+    if (empty == 1 && t > 0.6) return 0.0;
+    if (empty == 2 && t < 0.4) return 0.0;
+    double gab = -1.0;
+    if (dist < cy->len_rr.z) {
+        v3 o2c = sub3(cyl_pos, c);
+        double l = len3(o2c);
+        *u = neg3(div3(o2c, l));
+        *cpt = add3(p, mul3(r, *u));
+        gab = r + l - cy->len_rr.x * 0.5;
+    }
+    return gab;
+}
+
+typedef struct {
+    v3 sum_f, sum_m, tma;
+    double res;
+    unsigned int cnt;   /* slots used (the reference's new_count - sid) */
+} cyl_acc;
+
+/* One stored cylinder pair (slots without the reference's missing bound:
+ * a contact past MAX_P2CY_COUNT is dropped and flagged). */
+static void cylinder_store(unsigned int* pair_id, double* tsd, unsigned int sid, cyl_acc* a, unsigned int pid,
+                           double sd0, double sd1, unsigned int* bits)
+{
+    if (a->cnt < MAX_P2CY_COUNT) {
+        tsd[2 * (sid + a->cnt)] = sd0;
+        tsd[2 * (sid + a->cnt) + 1] = sd1;
+        pair_id[sid + a->cnt] = pid;
+        a->cnt++;
+    } else {
+        *bits |= XDEM_ERR_P2CY_OVERFLOW;
+    }
+}
+
+/* impl:1111-1187: the contact force of one cylinder contact.  `ipos` is the
+ * sphere's centre, or for a cluster member its cluster's centre (the lever
+ * arm rc = cpt - ipos); the body's mass does not enter the effective mass. */
+static void cylinder_force(int model, double dt, const device_contact_property* cp, const double* bi, v3 ipos,
+                           v3 ivel, v3 iom, v3 cpt, v3 unit, double cdist, unsigned int id, unsigned int pid,
+                           const unsigned int* old_id, double (*old_sd)[2], unsigned int* pair_id, double* tsd,
+                           unsigned int sid, double r, double m, double* fx, double* fy, double* fz, double* mx,
+                           double* my, double* mz, cyl_acc* a, unsigned int* bits)
+{
+    double sd0 = 0.0, sd1 = 0.0;
+    v3 bp, bv, bom;
+    double bm;
+    body_rec(bi, &bp, &bv, &bom, &bm);
+    v3 po2cp = sub3(cpt, bp);
+    v3 Fn = mk3(0, 0, 0), Ft = mk3(0, 0, 0);
+    for (int i = 0; i < MAX_P2CY_COUNT; ++i)
+        if (old_id[i] == pid) { sd0 = old_sd[i][0]; sd1 = old_sd[i][1]; break; }
+    v3 rc = sub3(cpt, ipos);
+    v3 dv = sub3(add3(bv, cross3(bom, po2cp)), add3(ivel, cross3(iom, rc)));
+    fconst c = get_constant(model, r, 0.0, m, 0.0, cp->Ei, cp->Ej, cp->pri, cp->prj, cp->rest, cp->fric,
+                            cp->s_fric, cp->rfric, cp->sratio);
+    contact_model(model, c, r, 0.0, cp, dt, cdist, &sd0, &sd1, dv, unit, &Ft, &Fn);
+    rolling_accumulate(cp->rfric, r, 0.0, rc, Fn, Ft, &a->res, &a->tma);
+    v3 mf = add3(Fn, Ft);
+    a->sum_f = add3(a->sum_f, mf);
+    a->sum_m = add3(a->sum_m, cross3(rc, mf));
+    fx[id] += -mf.x; fy[id] += -mf.y; fz[id] += -mf.z;
+    v3 bmo = neg3(cross3(po2cp, mf));
+    mx[id] += bmo.x; my[id] += bmo.y; mz[id] += bmo.z;
+    cylinder_store(pair_id, tsd, sid, a, pid, sd0, sd1, bits);
+}
+
+/* impl:1324-1601.  One launch for one cylinder over all particles: the side
+ * (or annulus, or rim) contact with pair id k = cyl->id, then, for a sphere
+ * inside, the cap it faces with pair id k + 1000.  Slots follow the plane
+ * rule (k == 0 restarts the list, k > 0 appends to it).  cpos == NULL: free
+ * spheres (cylinder_contact_force_kernel); else cluster members
+ * (cluster_cylinder_contact_force_kernel: cluster mass, velocity, spin, and
+ * lever arms from the cluster centre). */
+void xo_cylinder(const device_dem_parameters* prm, const device_cylinder_info* cyl, const double* bi,
+                 const device_contact_property* cp, double* fx, double* fy, double* fz, double* mx, double* my,
+                 double* mz, const double* pos, const double* cpos, const double* ep, const double* vel,
+                 const double* ev, double* force, double* moment, const double* mass, double* tmax, double* rres,
+                 unsigned int* pair_count, unsigned int* pair_id, double* tsd, const xClusterInformation* xci,
+                 unsigned int np, unsigned int* status)
+{
+    const int model = prm->contact_model;
+    const double dt = prm->dt;
+    v3 bp, bv, bom;
+    double bm;
+    body_rec(bi, &bp, &bv, &bom, &bm);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (long ii = 0; ii < (long)np; ++ii) {
+        unsigned int id = (unsigned int)ii;
+        unsigned int sid = id * MAX_P2CY_COUNT;
+        unsigned int old_id[MAX_P2CY_COUNT];
+        double old_sd[MAX_P2CY_COUNT][2];
+        for (int i = 0; i < MAX_P2CY_COUNT; ++i) {
+            old_id[i] = pair_id[sid + i];
+            old_sd[i][0] = tsd[2 * (sid + i)];
+            old_sd[i][1] = tsd[2 * (sid + i) + 1];
+        }
+        unsigned int ci = id;
+        if (cpos) {
+            unsigned int neach = 0;
+            for (unsigned int i = 0; i < prm->nClusterObject; ++i)
+                if (id >= xci[i].sid && id < xci[i].sid + xci[i].count * xci[i].neach) { neach = xci[i].neach; break; }
+            ci = neach ? id / neach : 0;
+        }
+        fx[id] = fy[id] = fz[id] = 0.0;
+        mx[id] = my[id] = mz[id] = 0.0;
+        unsigned int old_count = pair_count[id];
+        unsigned int k = cyl->id;
+        double m = mass[ci];
+        v4 ip4 = ld4(pos, id);
+        v3 ipos = mk3(ip4.x, ip4.y, ip4.z);
+        double r = ip4.w;
+        v3 ivel = ld3(vel, ci);
+        v3 iom = ang_vel(ld4(ep, ci), ld4(ev, ci));
+        v3 arm0 = cpos ? ld4xyz(cpos, ci) : ipos;
+        cyl_acc a;
+        memset(&a, 0, sizeof(a));
+        a.cnt = k ? old_count : 0;
+        unsigned int bits = 0;
+        int inner = 0;
+        double coh_s = 0;
+        v3 unit = mk3(0, 0, 0);
+        double cdist = cylinder_detection(cyl, bi, ipos, &unit, r, &inner);
+        if (cp->coh) coh_s = limit_cohesion_depth(r, 0, cp->Ei, cp->Ej, cp->pri, cp->prj, cp->coh);
+        v3 cpt = add3(ipos, mul3(r, unit));
+        for (int pass = 0; pass < 2; ++pass) {
+            unsigned int pid = pass ? k + 1000 : k;
+            if (pass) {
+                if (!inner) break;
+                cdist = cylinder_inner_cap(cyl, bi, ipos, &unit, &cpt, cyl->empty_part, r);
+            }
+            if (cdist > 0) {
+                cylinder_force(model, dt, cp, bi, arm0, ivel, iom, cpt, unit, cdist, id, pid, old_id, old_sd,
+                               pair_id, tsd, sid, r, m, fx, fy, fz, mx, my, mz, &a, &bits);
+            } else if (cdist <= 0 && fabs(cdist) < fabs(coh_s)) {
+                double f = jkr_separation_force(r, 0, cp->coh);
+                double cf = cohesion_force(r, 0, cp->Ei, cp->Ej, cp->pri, cp->prj, cp->coh, f);
+                v3 mf = mul3(-cf, unit);
+                a.sum_f = add3(a.sum_f, mf);
+                fx[id] += -mf.x; fy[id] += -mf.y; fz[id] += -mf.z;
+                v3 mo = neg3(cross3(sub3(cpt, bp), mf));
+                mx[id] += mo.x; my[id] += mo.y; mz[id] += mo.z;
+                cylinder_store(pair_id, tsd, sid, &a, pid, 0.0, 0.0, &bits);
+            }
+        }
+        addto3(force, id, a.sum_f);
+        addto3(moment, id, a.sum_m);
+        pair_count[id] = a.cnt;
+        addto3(tmax, id, a.tma);
+        rres[id] += a.res;
+        raise_status(status, bits);
+    }
+}
+
 /* Locates cluster id i in the cluster-object table (impl:158-172). */
 static void cluster_slot(const xClusterInformation* xci, unsigned int nco, unsigned int i,
                          unsigned int* neach, unsigned int* seach, unsigned int* sbegin,

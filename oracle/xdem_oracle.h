@@ -115,6 +115,17 @@ void xo_cluster_plane(const device_dem_parameters* prm,
                       unsigned int* pair_id, double* tsd,
                       const xClusterInformation* xci, unsigned int np,
                       unsigned int* status);
+/* impl:1083-1601: one cylinder against every particle; cpos == NULL for
+ * free spheres, else cluster members (xci, cluster state) */
+void xo_cylinder(const device_dem_parameters* prm, const device_cylinder_info* cyl,
+                 const double* bi, const device_contact_property* cp, double* fx,
+                 double* fy, double* fz, double* mx, double* my, double* mz,
+                 const double* pos, const double* cpos, const double* ep,
+                 const double* vel, const double* ev, double* force,
+                 double* moment, const double* mass, double* tmax, double* rres,
+                 unsigned int* pair_count, unsigned int* pair_id, double* tsd,
+                 const xClusterInformation* xci, unsigned int np,
+                 unsigned int* status);
 /* impl:2111-2268 */
 void xo_cluster_mesh(const device_dem_parameters* prm,
                      const device_triangle_info* dti, const double* dbi,

@@ -11,6 +11,8 @@ reference sources are present; the fixtures are committed).
                     kernels (oracle/_ref) for every launcher of the step.
   ref_cluster.npz   the same for a three-sphere cluster bed with planes and a
                     mesh.
+  ref_cylinder.npz  one launch of the reference's particle-cylinder kernels
+                    (spheres and cluster members, four material cases).
 
 Usage:  make -C oracle all ref && python tests/golden/make_golden.py
 """
@@ -166,10 +168,53 @@ def run_ref_pair(sc, kind):
     np.savez_compressed(os.path.join(HERE, f"ref_{kind}.npz"), **out)
 
 
+def make_cylinder():
+    """ref_cylinder.npz: one launch of the reference's cylinder kernels
+    (cylinder_contact_force_kernel / cluster_cylinder_contact_force_kernel,
+    impl:1324-1601) for spheres and for cluster members, with Hertz-Mindlin
+    and DHS, rolling friction and cohesion, on the seeded inputs of
+    kseq.cylinder_inputs (every detection region); inputs and outputs."""
+    ref = pyoracle.RefKernels()
+    out = {}
+    for ci, cluster in enumerate((False, True)):
+        for mi, (model, rf, coh) in enumerate(kseq.CYLINDER_CASES):
+            inp = kseq.cylinder_inputs(3 + model, cluster=cluster, n_per=24)
+            cp = scenes.default_material(rfric=rf)
+            cp.coh = coh
+
+            def run(prm, cyl, body, cp, bf, st, pr):
+                ref.set_params(prm)
+                n = len(st["pos"]) // 4
+                if st["cpos"] is None:
+                    ref.cylinder(cyl, body, *bf, st["pos"], st["ep"], st["vel"], st["ev"], st["force"],
+                                 st["moment"], cp, st["mass"], st["tmax"], st["rres"], pr["pair_count"],
+                                 pr["pair_id"], pr["tsd"], n)
+                else:
+                    ref.cluster_cylinder(cyl, body, *bf, st["pos"], st["cpos"], st["ep"], st["vel"], st["ev"],
+                                         st["force"], st["moment"], st["xci"], cp, st["mass"], st["tmax"],
+                                         st["rres"], pr["pair_count"], pr["pair_id"], pr["tsd"], n)
+                return 0
+
+            res, _ = kseq.run_cylinder(run, inp, cp, model)
+            key = f"c{ci}m{mi}_"
+            for k in ("pos", "vel", "ep", "ev", "mass", "pair_count", "pair_id", "tsd", "body"):
+                out[key + "in_" + k] = inp[k]
+            if cluster:
+                out[key + "in_cpos"] = inp["cpos"]
+                out[key + "in_xci"] = inp["xci"]
+            out[key + "cyl"] = struct_bytes(inp["cyl"])
+            out[key + "cp"] = struct_bytes(cp)
+            out[key + "model"] = np.array(model)
+            for k, v in res.items():
+                out[key + "out_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "ref_cylinder.npz"), **out)
+
+
 def main():
     make_kat()
     run_ref_pair(sphere_scene(), "sphere")
     run_ref_pair(cluster_scene(), "cluster")
+    make_cylinder()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -385,3 +385,129 @@ def check_outputs(s, g, exp, *, kind, ftol=1e-12, skip=()):
         scale = max(float(np.max(np.abs(b))) if b.size else 0.0, 1e-300)
         err = float(np.max(np.abs(a - b))) / scale if b.size else 0.0
         assert err <= ftol, f"{k}: max abs diff {np.max(np.abs(a - b)):.3e} (scale {scale:.3e})"
+
+
+# ---------------------------------------------------------------- cylinders
+# (contact model, rolling friction, cohesion) of the cylinder fixtures
+CYLINDER_CASES = [(1, 0.0, 0.0), (0, 0.0, 0.0), (1, 0.2, 0.0), (1, 0.0, 5e4)]
+
+
+def load_cylinder_fixture():
+    """Cases of ref_cylinder.npz: (inputs as cylinder_inputs returns them,
+    contact property, contact model, the reference kernels' outputs)."""
+    import os
+    d = np.load(os.path.join(GOLDEN, "ref_cylinder.npz"))
+    cases = []
+    for ci in range(2):
+        for mi in range(len(CYLINDER_CASES)):
+            key = f"c{ci}m{mi}_"
+            inp = {k: d[key + "in_" + k].copy() for k in ("pos", "vel", "ep", "ev", "mass", "pair_count",
+                                                           "pair_id", "tsd", "body")}
+            inp["cpos"] = d[key + "in_cpos"].copy() if ci else None
+            inp["xci"] = d[key + "in_xci"].copy() if ci else None
+            inp["n"] = inp["pos"].size // 4
+            inp["ns"] = inp["mass"].size
+            inp["cyl"] = _struct(T.CylinderInfo, d[key + "cyl"])
+            cp = _struct(T.ContactProperty, d[key + "cp"])
+            exp = {k[len(key) + 4:]: d[k] for k in d.files if k.startswith(key + "out_")}
+            cases.append((inp, cp, int(d[key + "model"]), exp))
+    return cases
+
+
+def cylinder_inputs(seed, cluster=False, n_per=48):
+    """Inputs of one cylinder launch (impl:1324-1601) whose spheres sit in
+    every region of the detection: outside and inside the wall, near the
+    inner caps (top open: empty_part 1), in the inner corner of the base
+    (wall and cap at once), on the annulus beyond an end, near the rim, and
+    far away; a rotated, moving, spinning cylinder body; old
+    pair lists holding ids k and k + 1000 with history.  cluster=True makes
+    every sphere a member of a three-member cluster whose centre, mass,
+    velocity and spin the kernel reads instead."""
+    rng = np.random.default_rng(seed)
+    L, R, th = 0.04, 0.015, 0.002
+    cyl = T.CylinderInfo()
+    cyl.id = 0
+    cyl.empty_part = 1
+    cyl.thickness = th
+    cyl.len_rr = T.d3((L, R, R))
+    cyl.pbase = T.d3((0.0, -0.5 * L, 0.0))
+    cyl.ptop = T.d3((0.0, 0.5 * L, 0.0))
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    body = T.body_record(mass=0.7, pos=(0.01, 0.02, -0.005), vel=(0.01, -0.02, 0.03), ep=tuple(q),
+                         ed=tuple(0.5 * rng.normal(size=4)))
+    A = rot(q)
+    pts, rad = [], []
+
+    def add(rho, y, r):
+        ph = rng.uniform(0, 2 * np.pi)
+        pts.append(np.array([rho * np.cos(ph), y, rho * np.sin(ph)]))
+        rad.append(r)
+
+    for _ in range(n_per):
+        r = rng.uniform(1e-3, 2e-3)
+        add(R + r * rng.uniform(0.3, 1.3), rng.uniform(-0.5 * L + 2 * r, 0.5 * L - 2 * r), r)   # outside wall
+        r = rng.uniform(1e-3, 2e-3)
+        add(R - r * rng.uniform(0.2, 1.3), rng.uniform(-0.5 * L + 0.5 * r, 0.5 * L - 0.5 * r), r)  # inside wall
+        r = rng.uniform(1e-3, 2e-3)
+        add(rng.uniform(0.1 * R, R - 2 * r), rng.choice([-1, 1]) * (0.5 * L - r * rng.uniform(0.3, 1.3)), r)  # caps
+        r = rng.uniform(1e-3, 2e-3)
+        add(rng.uniform(R + 0.1 * th, R + 0.9 * th), rng.choice([-1, 1]) * (0.5 * L + r * rng.uniform(0.2, 1.2)), r)
+        r = rng.uniform(1e-3, 2e-3)
+        add(R + th + r * rng.uniform(0.1, 0.9), rng.choice([-1, 1]) * (0.5 * L + r * rng.uniform(0.1, 0.9)), r)
+        r = rng.uniform(1e-3, 2e-3)
+        add(R - r * rng.uniform(0.3, 0.9), -0.5 * L + r * rng.uniform(0.3, 0.9), r)  # inner base corner: wall + cap
+        r = rng.uniform(1e-3, 2e-3)
+        add(rng.uniform(0, 0.1), rng.uniform(0.1, 0.2), r)                                       # far
+    loc = np.array(pts)
+    n = len(rad)
+    pos = np.zeros((n, 4))
+    pos[:, :3] = body[1:4] + loc @ A.T
+    pos[:, 3] = rad
+    ns = n // 3 if cluster else n
+    if cluster:
+        n = 3 * ns
+        pos = pos[:n]
+    vel = rng.normal(0, 0.05, size=(ns, 3))
+    ep = rng.normal(size=(ns, 4))
+    ep /= np.linalg.norm(ep, axis=1, keepdims=True)
+    ev = rng.normal(0, 2.0, size=(ns, 4))
+    mass = rng.uniform(1e-5, 5e-5, size=ns)
+    out = dict(cyl=cyl, body=body, pos=pos.ravel().copy(), vel=vel.ravel(), ep=ep.ravel(), ev=ev.ravel(),
+               mass=mass, n=n, ns=ns, cpos=None, xci=None)
+    if cluster:
+        cpos = np.zeros((ns, 4))
+        cpos[:, :3] = pos.reshape(ns, 3, 4)[:, 1, :3] + rng.normal(0, 1e-3, size=(ns, 3))
+        cpos[:, 3] = pos.reshape(ns, 3, 4)[:, 1, 3]
+        out["cpos"] = cpos.ravel()
+        out["xci"] = np.array([0, 0, ns, 3], dtype=np.uint32)
+    pc = rng.integers(0, 3, size=n).astype(np.uint32)
+    pid = np.where(rng.random(n * 3) < 0.5, 0, 1000).astype(np.uint32)
+    pid[rng.random(n * 3) < 0.2] = 7
+    tsd = rng.normal(0, 1e-5, size=n * 6)
+    out.update(pair_count=pc, pair_id=pid, tsd=tsd)
+    return out
+
+
+def cylinder_params(inp, model=1):
+    prm = T.make_params(np_=inp["n"], dt=1e-5, cell_size=0.004, contact_model=model,
+                        ncluster=inp["ns"] if inp["cpos"] is not None else 0,
+                        nco=1 if inp["cpos"] is not None else 0)
+    return prm
+
+
+def run_cylinder(run, inp, cp, model=1):
+    """One cylinder launch through `run(prm, cyl, body, cp, bf, state, pairs)`
+    on copies of the inputs; returns every output array."""
+    n = inp["n"]
+    st = {k: inp[k].copy() for k in ("pos", "vel", "ep", "ev", "mass")}
+    st["cpos"] = None if inp["cpos"] is None else inp["cpos"].copy()
+    st["xci"] = inp["xci"]
+    st.update(force=np.full(n * 3, 0.25), moment=np.full(n * 3, -0.5), tmax=np.zeros(n * 3), rres=np.zeros(n))
+    pairs = dict(pair_count=inp["pair_count"].copy(), pair_id=inp["pair_id"].copy(), tsd=inp["tsd"].copy())
+    bf = [np.full(n, 9.0) for _ in range(6)]
+    status = run(cylinder_params(inp, model), inp["cyl"], inp["body"].copy(), cp, bf, st, pairs)
+    out = dict(force=st["force"], moment=st["moment"], tmax=st["tmax"], rres=st["rres"], **pairs)
+    for i, k in enumerate(("fx", "fy", "fz", "mx", "my", "mz")):
+        out[k] = bf[i]
+    return out, status

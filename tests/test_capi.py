@@ -31,7 +31,8 @@ def test_reference_launcher_names_present(L):
                  "cu_particle_polygonObject_collision", "cu_decide_rolling_friction_moment", "reduction",
                  "cu_update_meshObjectData", "cu_clusters_contact", "cu_cluster_plane_contact",
                  "cu_cluster_meshes_contact", "cu_decide_cluster_rolling_friction_moment",
-                 "vv_update_cluster_position", "vv_update_cluster_velocity"]:
+                 "vv_update_cluster_position", "vv_update_cluster_velocity", "cu_cylinder_contact_force",
+                 "cu_cluster_cylinder_contact"]:
         assert hasattr(L, name), name
 
 
@@ -42,6 +43,8 @@ def test_struct_layouts():
     assert T.DemParameters.dt.offset == 64
     assert T.DemParameters.world_origin.offset == 120
     assert C.sizeof(T.PlaneInfo) == 240 and T.PlaneInfo.l1.offset == 8 and T.PlaneInfo.w4.offset == 216
+    assert C.sizeof(T.CylinderInfo) == 88 and T.CylinderInfo.thickness.offset == 8
+    assert T.CylinderInfo.len_rr.offset == 16 and T.CylinderInfo.ptop.offset == 64
     assert C.sizeof(T.TriangleInfo) == 80 and T.TriangleInfo.P.offset == 8
     assert C.sizeof(T.ContactProperty) == 13 * 8
     assert C.sizeof(T.ClusterInformation) == 16

@@ -52,3 +52,21 @@ def test_step_matches_reference_kernels(oracle, kind):
     # everything else follows the reference's operation order
     kseq.check_outputs(s, g, exp, kind=kind, ftol=1e-12)
     assert np.allclose(np.array([np.stack(p) for p in partials]), exp["partials"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", range(8))
+def test_cylinder_matches_reference_kernels(oracle, case):
+    """The oracle's cylinder contact (xo_cylinder) against the reference's
+    own cylinder kernels (ref_cylinder.npz): every output bit for bit."""
+    inp, cp, model, exp = kseq.load_cylinder_fixture()[case]
+
+    def run(prm, cyl, body, cp, bf, s, p):
+        return oracle.cylinder(prm, cyl, body, cp, bf, s["pos"], s["cpos"], s["ep"], s["vel"], s["ev"], s["force"],
+                               s["moment"], s["mass"], s["tmax"], s["rres"], p["pair_count"], p["pair_id"], p["tsd"],
+                               s["xci"], len(s["pos"]) // 4)
+
+    out, st = kseq.run_cylinder(run, inp, cp, model)
+    assert st == 0
+    assert int(out["pair_count"].sum()) > 0
+    for k, v in exp.items():
+        assert np.array_equal(out[k], v), k

@@ -44,6 +44,8 @@ _SIGS = {
     "cu_update_meshObjectData": ([vp] * 5 + [u32], i32),
     "cu_clusters_contact": ([vp] * 18 + [u32], i32),
     "cu_cluster_plane_contact": ([vp] * 17 + [u32], i32),
+    "cu_cylinder_contact_force": ([vp] * 15 + [u32], i32),
+    "cu_cluster_cylinder_contact": ([vp] * 17 + [u32], i32),
     "cu_cluster_meshes_contact": ([vp] * 20 + [u32, u32], i32),
     "cu_decide_cluster_rolling_friction_moment": ([vp] * 7 + [u32], i32),
     "vv_update_cluster_position": ([vp] * 9 + [u32], i32),

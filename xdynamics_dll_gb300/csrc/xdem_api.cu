@@ -341,6 +341,47 @@ XDEM_API int cu_plane_contact_force(device_plane_info* plan, double* dbi, device
     return set_status(finish_wrench(c));
 }
 
+XDEM_API int cu_cylinder_contact_force(device_cylinder_info* cyl, double* bi, device_contact_property* cp,
+                                       double* pos, double* ep, double* vel, double* omega, double* force,
+                                       double* moment, double* mass, double* tmax, double* rres,
+                                       unsigned int* pair_count, unsigned int* pair_id, double* tsd, unsigned int np)
+{
+    if (int s = need_params()) return set_status(s);
+    if (!cyl || !bi || !cp) return set_status(XDEM_ERR_ARG);
+    int err = 0;
+    DevCtx* c = ctx(&err);
+    if (!c) return set_status(err);
+    BodyPartials bp{};
+    if (int s = body_partials(c, np, bp)) return set_status(s);
+    cudaError_t e = launch_make_mat_pair(cp, g_params.contact_model, 0, c->mp, t_stream);
+    if (e == cudaSuccess)
+        e = launch_cylinder(g_params, cyl, bi, c->mp, bp, pos, nullptr, ep, vel, omega, force, moment, mass, tmax,
+                            rres, pair_count, pair_id, tsd, nullptr, np, c->status, t_stream);
+    if (e != cudaSuccess) return set_status(cuda_status(e));
+    return set_status(finish_wrench(c));
+}
+
+XDEM_API int cu_cluster_cylinder_contact(device_cylinder_info* cyl, double* bi, xClusterInformation* xci,
+                                         device_contact_property* cp, double* pos, double* cpos, double* ep,
+                                         double* vel, double* omega, double* force, double* moment, double* mass,
+                                         double* tmax, double* rres, unsigned int* pair_count,
+                                         unsigned int* pair_id, double* tsd, unsigned int np)
+{
+    if (int s = need_params()) return set_status(s);
+    if (!cyl || !bi || !cp || !xci || !cpos) return set_status(XDEM_ERR_ARG);
+    int err = 0;
+    DevCtx* c = ctx(&err);
+    if (!c) return set_status(err);
+    BodyPartials bp{};
+    if (int s = body_partials(c, np, bp)) return set_status(s);
+    cudaError_t e = launch_make_mat_pair(cp, g_params.contact_model, 0, c->mp, t_stream);
+    if (e == cudaSuccess)
+        e = launch_cylinder(g_params, cyl, bi, c->mp, bp, pos, cpos, ep, vel, omega, force, moment, mass, tmax,
+                            rres, pair_count, pair_id, tsd, xci, np, c->status, t_stream);
+    if (e != cudaSuccess) return set_status(cuda_status(e));
+    return set_status(finish_wrench(c));
+}
+
 XDEM_API int cu_particle_polygonObject_collision(device_triangle_info* dpi, double* dbi, double* pos, double* ep,
                                                  double* vel, double* omega, double* force, double* moment,
                                                  double* mass, double* tmax, double* rres, unsigned int* pair_count,

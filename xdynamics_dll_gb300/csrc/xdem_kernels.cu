@@ -342,6 +342,194 @@ k_plane(device_dem_parameters p, const device_plane_info* planep, const double* 
     emit_body_partials(bp, id, valid, f6);
 }
 
+// ---------------------------------------------------------------- cylinders (impl:1083-1601)
+// Base and top centres of a cylinder at its body pose.
+__device__ __forceinline__ void cylinder_ends(const device_cylinder_info& cy, const double* bi, d3& pos, d4& e,
+                                              d3& base, d3& top)
+{
+    pos = mk3(bi[XDEM_PX], bi[XDEM_PY], bi[XDEM_PZ]);
+    e = mk4(bi[XDEM_E0], bi[XDEM_E1], bi[XDEM_E2], bi[XDEM_E3]);
+    base = pos + to_global(dv3(cy.pbase), e);
+    top = pos + to_global(dv3(cy.ptop), e);
+}
+
+// impl:1189-1288: depth and unit vector of sphere (p, r) against the
+// cylinder -- side (axis parameter in [0, 1]; an inside contact flips the
+// normal and sets `inner`), the wall annulus beyond the ends, else the rim
+// point through the angle atan(x / z) of the local offset, as the reference
+// forms it.
+__device__ double cylinder_detection(const device_cylinder_info& cy, const double* bi, d3 p, d3& u, double r,
+                                     bool& inner)
+{
+    d3 cyl_pos, base, top;
+    d4 e;
+    cylinder_ends(cy, bi, cyl_pos, e, base, top);
+    const d3 ab = top - base;
+    const double t = dot(p - base, ab) / dot(ab, ab);
+    const d3 c = base + t * ab;
+    double dist = length(p - c);
+    if (t >= 0 && t <= 1) {
+        if (dist == 0) {
+            inner = true;
+            return 0;
+        }
+        u = (c - p) / dist;
+        if (dist < cy.len_rr.z) {
+            inner = true;
+            u = -u;
+            return dist + r - cy.len_rr.y;
+        }
+        return cy.len_rr.y + r - dist;
+    }
+    const double thick = cy.thickness;
+    const int one = thick != 0.0 ? 1 : 0;
+    if (dist < cy.len_rr.z + thick && dist > one * cy.len_rr.z) {
+        const d3 o2c = cyl_pos - c;
+        const double l = length(o2c);
+        u = o2c / l;
+        return cy.len_rr.x * 0.5 + r - l;
+    }
+    d3 at = to_local(p - top, e);
+    d3 cp = top;
+    if (fabs(at.y) > cy.len_rr.x) {
+        at = to_local(p - base, e);
+        cp = base;
+    }
+    const double pi = atan(at.x / at.z);
+    d3 q = mk3(0, 0, 0);
+    if (pi < 0 && at.z < 0) q.x = cy.len_rr.z * sin(-pi);
+    else if (pi > 0 && at.x < 0 && at.z < 0) q.x = cy.len_rr.z * sin(-pi);
+    else q.x = cy.len_rr.z * sin(pi);
+    q.z = cy.len_rr.z * cos(pi);
+    if (at.z < 0 && q.z > 0) q.z = -q.z;
+    else if (at.z > 0 && q.z < 0) q.z = -q.z;
+    q.y = 0.;
+    cp = cp + to_global(q, e);
+    const d3 dv = cp - p;
+    dist = length(dv);
+    u = dv / dist;
+    if (dist < r) return r - dist;
+    return -1.0;
+}
+
+// impl:1290-1322: the cap a sphere inside the cylinder faces (none near an
+// open end: empty 1 top for t > 0.6, empty 2 base for t < 0.4).
+__device__ double cylinder_inner_cap(const device_cylinder_info& cy, const double* bi, d3 p, d3& u, d3& cpt,
+                                     unsigned int empty, double r)
+{
+    d3 cyl_pos, base, top;
+    d4 e;
+    cylinder_ends(cy, bi, cyl_pos, e, base, top);
+    const d3 ab = top - base;
+    const double t = dot(p - base, ab) / dot(ab, ab);
+    const d3 c = base + t * ab;
+    const double dist = length(p - c);
+    if (empty == 1 && t > 0.6) return 0.0;
+    if (empty == 2 && t < 0.4) return 0.0;
+    double gab = -1.0;
+    if (dist < cy.len_rr.z) {
+        const d3 o2c = cyl_pos - c;
+        const double l = length(o2c);
+        u = -(o2c / l);
+        cpt = p + r * u;
+        gab = r + l - cy.len_rr.x * 0.5;
+    }
+    return gab;
+}
+
+// impl:1324-1601: one cylinder against every particle.  The side/annulus/
+// rim contact carries pair id k = cyl->id, the inner cap of a sphere inside
+// k + 1000; slots follow the plane rule (k == 0 restarts the list), bounded
+// by MAX_P2CY_COUNT here (the reference writes on without a bound).
+// CLUSTER: members with their cluster's mass, velocity and spin, lever arms
+// from the cluster centre.  The body's mass does not enter the effective
+// mass (getConstant(r, 0, m, 0, ...)).
+template <bool CLUSTER>
+__global__ void __launch_bounds__(kThreads)
+k_cylinder(device_dem_parameters p, const device_cylinder_info* cylp, const double* bi, const mat_pair* mpp,
+           BodyPartials bp, const double* pos, const double* cpos, const double* ep, const double* vel,
+           const double* ev, double* force, double* moment, const double* mass, double* tmax, double* rres,
+           unsigned int* pair_count, unsigned int* pair_id, double* tsd, const xClusterInformation* xci,
+           unsigned int n, unsigned int* status)
+{
+    const unsigned int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = id < n;
+    double f6[6] = {0, 0, 0, 0, 0, 0};
+    if (valid) {
+        const mat_pair mp = *mpp;
+        const device_cylinder_info cy = *cylp;
+        const int model = p.contact_model;
+        const double dt = p.dt;
+        const body_state b = load_body(bi);
+        const unsigned int sid = id * MAX_P2CY_COUNT;
+        OldPairs<MAX_P2CY_COUNT> old;
+        const unsigned int old_count = pair_count[id];
+        old.load(pair_id, tsd, sid, old_count);
+        unsigned int ci = id;
+        if (CLUSTER) {
+            const unsigned int ne = cluster_neach(xci, p.nClusterObject, id);
+            ci = ne ? id / ne : 0;
+        }
+        const double m = mass[ci];
+        const d4 ip4 = ld4(pos, id);
+        const d3 ipos = mk3(ip4.x, ip4.y, ip4.z);
+        const double r = ip4.w;
+        const unsigned int k = cy.id;
+        const d3 ivel = ld3(vel, ci);
+        const d3 iom = ang_vel(ld4(ep, ci), ld4(ev, ci));
+        const d3 arm0 = CLUSTER ? ld4xyz(cpos, ci) : ipos;
+        d3 sumF = mk3(0, 0, 0), sumM = mk3(0, 0, 0), tma = mk3(0, 0, 0);
+        double res = 0.0;
+        unsigned int cnt = k ? old_count : 0, bits = 0;
+        bool inner = false;
+        d3 unit = mk3(0, 0, 0);
+        double cdist = cylinder_detection(cy, bi, ipos, unit, r, inner);
+        double cs = 0.0;
+        if (mp.coh) cs = limit_cohesion_depth(mp, r, 0.0);
+        d3 cpt = ipos + r * unit;
+        for (int pass = 0; pass < 2; ++pass) {
+            const unsigned int pid = pass ? k + 1000 : k;
+            if (pass) {
+                if (!inner) break;
+                cdist = cylinder_inner_cap(cy, bi, ipos, unit, cpt, cy.empty_part, r);
+            }
+            d3 mf = mk3(0, 0, 0);
+            double sd0 = 0.0, sd1 = 0.0;
+            if (cdist > 0) {
+                old.find(pid, MAX_P2CY_COUNT, sd0, sd1);
+                const d3 po2cp = cpt - b.p;
+                const d3 rc = cpt - arm0;
+                const d3 dv = (b.v + cross(b.om, po2cp)) - (ivel + cross(iom, rc));
+                const fconst c = get_constant(mp, model, r, 0.0, m, 0.0);
+                d3 Fn = mk3(0, 0, 0), Ft = mk3(0, 0, 0);
+                contact_model(model, c, mp, r, 0.0, dt, cdist, sd0, sd1, dv, unit, Ft, Fn);
+                rolling_accumulate(mp.rfric, r, 0.0, rc, Fn, Ft, res, tma);
+                mf = Fn + Ft;
+                sumF = sumF + mf;
+                sumM = sumM + cross(rc, mf);
+            } else if (cdist <= 0 && fabs(cdist) < fabs(cs)) {
+                const double f = jkr_separation_force(mp, r, 0.0);
+                const double cf = cohesion_force(mp, r, 0.0, f);
+                mf = (-cf) * unit;
+                sumF = sumF + mf;
+            } else {
+                continue;
+            }
+            f6[0] += -mf.x; f6[1] += -mf.y; f6[2] += -mf.z;
+            const d3 bm = -cross(cpt - b.p, mf);
+            f6[3] += bm.x; f6[4] += bm.y; f6[5] += bm.z;
+            store_pair(pair_id, tsd, sid, cnt, MAX_P2CY_COUNT, pid, sd0, sd1, bits, XDEM_ERR_P2CY_OVERFLOW);
+        }
+        add3to(force, id, sumF);
+        add3to(moment, id, sumM);
+        pair_count[id] = cnt;
+        add3to(tmax, id, tma);
+        rres[id] += res;
+        if (bits) atomicOr(status, bits);
+    }
+    emit_body_partials(bp, id, valid, f6);
+}
+
 // ---------------------------------------------------------------- meshes (impl:1748-2268)
 struct TriHit { unsigned int id; d3 cpt; };
 
@@ -804,6 +992,20 @@ cudaError_t launch_cluster_plane(const device_dem_parameters& p, const device_pl
 {
     XDEM_LAUNCH(k_plane<true>, n, p, plane, dbi, mp, bp, pos, cpos, ep, vel, ev, force, moment, mass, tmax, rres,
                 pair_count, pair_id, tsd, xci, n, status);
+}
+
+cudaError_t launch_cylinder(const device_dem_parameters& p, const device_cylinder_info* cyl, const double* bi,
+                            const mat_pair* mp, const BodyPartials& bp, const double* pos, const double* cpos,
+                            const double* ep, const double* vel, const double* ev, double* force, double* moment,
+                            const double* mass, double* tmax, double* rres, unsigned int* pair_count,
+                            unsigned int* pair_id, double* tsd, const xClusterInformation* xci, unsigned int n,
+                            unsigned int* status, cudaStream_t st)
+{
+    if (cpos)
+        XDEM_LAUNCH(k_cylinder<true>, n, p, cyl, bi, mp, bp, pos, cpos, ep, vel, ev, force, moment, mass, tmax,
+                    rres, pair_count, pair_id, tsd, xci, n, status);
+    XDEM_LAUNCH(k_cylinder<false>, n, p, cyl, bi, mp, bp, pos, nullptr, ep, vel, ev, force, moment, mass, tmax,
+                rres, pair_count, pair_id, tsd, nullptr, n, status);
 }
 
 cudaError_t launch_mesh(const device_dem_parameters& p, const device_triangle_info* dti, unsigned int lo_base,

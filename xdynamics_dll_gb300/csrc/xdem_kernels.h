@@ -74,6 +74,13 @@ cudaError_t launch_clusters_p2p(const device_dem_parameters& p, const double* po
                                 const unsigned int* cend, const mat_pair* mp,
                                 const xClusterInformation* xci, unsigned int n, unsigned int* status,
                                 cudaStream_t st);
+// impl:1324-1601; cpos != null: cluster members (xci)
+cudaError_t launch_cylinder(const device_dem_parameters& p, const device_cylinder_info* cyl, const double* bi,
+                            const mat_pair* mp, const BodyPartials& bp, const double* pos, const double* cpos,
+                            const double* ep, const double* vel, const double* ev, double* force, double* moment,
+                            const double* mass, double* tmax, double* rres, unsigned int* pair_count,
+                            unsigned int* pair_id, double* tsd, const xClusterInformation* xci, unsigned int n,
+                            unsigned int* status, cudaStream_t st);
 cudaError_t launch_cluster_plane(const device_dem_parameters& p, const device_plane_info* plane, const double* dbi,
                                  const mat_pair* mp, const BodyPartials& bp, const double* pos,
                                  const double* cpos, const double* ep, const double* vel, const double* ev,

@@ -153,6 +153,25 @@ class Launchers:
                                                  self.d(s["xci"]), s["np"]), "cu_cluster_plane_contact")
         return self._status()
 
+    def cylinder(self, s, cyl, bi, cp):
+        """cu_cylinder_contact_force, or cu_cluster_cylinder_contact when the
+        state has cluster centres (s["cpos"]); pairs in s["cy_count"],
+        s["cy_id"], s["cy_tsd"] (MAX_P2CY_COUNT slots a particle)."""
+        self._bf(s)
+        if s.get("cpos") is None:
+            r = self.L.cu_cylinder_contact_force(
+                self.d(cyl), self.d(bi), self.d(cp), self.d(s["pos"]), self.d(s["ep"]), self.d(s["vel"]),
+                self.d(s["ev"]), self.d(s["force"]), self.d(s["moment"]), self.d(s["mass"]), self.d(s["tmax"]),
+                self.d(s["rres"]), self.d(s["cy_count"]), self.d(s["cy_id"]), self.d(s["cy_tsd"]), s["np"])
+        else:
+            r = self.L.cu_cluster_cylinder_contact(
+                self.d(cyl), self.d(bi), self.d(s["xci"]), self.d(cp), self.d(s["pos"]), self.d(s["cpos"]),
+                self.d(s["ep"]), self.d(s["vel"]), self.d(s["ev"]), self.d(s["force"]), self.d(s["moment"]),
+                self.d(s["mass"]), self.d(s["tmax"]), self.d(s["rres"]), self.d(s["cy_count"]), self.d(s["cy_id"]),
+                self.d(s["cy_tsd"]), s["np"])
+        self._ck(r, "cu_cylinder_contact_force")
+        return self._status()
+
     def cluster_mesh(self, s, g, dti, dbi, cp, ntri):
         self._bf(s)
         self._ck(self.L.cu_cluster_meshes_contact(

@@ -11,6 +11,7 @@ import numpy as np
 
 MAX_P2P_COUNT = 12
 MAX_P2PL_COUNT = 3
+MAX_P2CY_COUNT = 3
 MAX_P2MS_COUNT = 5
 DEVICE_BODY_MEM_SIZE = 120
 
@@ -23,6 +24,7 @@ XDEM_ERR_P2PL_OVERFLOW = 1 << 1
 XDEM_ERR_P2MS_OVERFLOW = 1 << 2
 XDEM_ERR_TRI_CANDIDATES = 1 << 3
 XDEM_ERR_NONFINITE = 1 << 4
+XDEM_ERR_P2CY_OVERFLOW = 1 << 5
 XDEM_ERR_CUDA = 1 << 8
 XDEM_ERR_ARG = 1 << 9
 XDEM_ERR_NOT_SET = 1 << 10
@@ -83,6 +85,12 @@ class ContactProperty(C.Structure):
     _fields_ = [(n, C.c_double) for n in
                 ("Ei", "Ej", "pri", "prj", "Gi", "Gj", "rest", "fric", "s_fric",
                  "rfric", "coh", "sratio", "amp")]
+
+
+class CylinderInfo(C.Structure):
+    """device_cylinder_info (decl:220-228)."""
+    _fields_ = [("id", C.c_uint), ("empty_part", C.c_uint), ("thickness", C.c_double), ("len_rr", Double3),
+                ("pbase", Double3), ("ptop", Double3)]
 
 
 class ClusterInformation(C.Structure):
