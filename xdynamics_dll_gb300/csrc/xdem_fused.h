@@ -150,6 +150,7 @@ struct FusedState {
     bool any_coh = false;            // cohesion in a particle-pair material (no lists)
     // bounding sphere of each mesh (centre relative to the grid origin,
     // radius): a sphere that cannot reach it skips the triangle search
+    cudaStream_t side_st = nullptr;  // captures the conditional sort section of a step graph
     float4* d_mesh_bs = nullptr;     // [kMaxFusedMeshes]
     float4 h_mesh_bs[kMaxFusedMeshes] = {};
     // body wrench reduction: per-chunk sums and per-body finish counters

@@ -202,6 +202,13 @@ __global__ void k_reorder_fp64(const unsigned int* sk, const unsigned int* sv, u
     reinterpret_cast<float4*>(snap_f)[s] = f;
 }
 
+// Condition of the captured step's IF node around the gated clear, sort and
+// reorder: the gate (rebuild this step, or a list overflowed).
+__global__ void k_set_sort_cond(cudaGraphConditionalHandle h, const unsigned int* gate)
+{
+    cudaGraphSetConditional(h, *gate ? 1u : 0u);
+}
+
 // Mixed form: cell ranges and the FP32 records permuted into sorted order.
 __global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk, const unsigned int* sv,
                                 unsigned int n, unsigned int np,
@@ -390,6 +397,7 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.fB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.fC, (size_t)np * 4);
 
+        if (e == cudaSuccess && !fs.side_st) e = cudaStreamCreateWithFlags(&fs.side_st, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = dalloc(fs.vl_ids, (size_t)np * kListCap);
         if (e == cudaSuccess) e = dalloc(fs.vl_cnt, np);
         if (e == cudaSuccess) e = dalloc(fs.vl_xb, (size_t)np * 4);
@@ -428,6 +436,7 @@ void fused_free(FusedState& fs)
                   fs.d_mesh_bs};
     for (void* q : ps)
         if (q) cudaFree(q);
+    if (fs.side_st) cudaStreamDestroy(fs.side_st);
     fs = FusedState{};
 }
 
@@ -649,12 +658,46 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     // build): the device skips the clear, sort and reorder otherwise.
     const bool use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && !fs.any_coh && fs.vl_flag;
     const unsigned int* sort_gate = use_list ? fs.vl_flag + kVlSort : nullptr;
-    if (fs.have_prev) ok(launch_clear_cells(fs.skey_prev, n, a.cstart, a.cend, st, sort_gate));
+    // Captured into a graph, the gated section becomes the body of an IF
+    // node whose condition a one-thread kernel sets from the gate, so that
+    // between rebuilds the graph skips it instead of launching kernels that
+    // return at once.  The body is captured on a side stream.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (use_list && fs.side_st && cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
+    const bool cond = use_list && fs.side_st && cap == cudaStreamCaptureStatusActive;
+    cudaStream_t sst = st;
+    cudaGraphNode_t cnode = nullptr;
+    const unsigned int nl_before = nl;
+    if (cond) {
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaGraphConditionalHandle h = 0;
+        ok(cudaStreamGetCaptureInfo(st, &cap, nullptr, &g, nullptr, nullptr, nullptr));
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+        if (e == cudaSuccess) {
+            k_set_sort_cond<<<1, 1, 0, st>>>(h, sort_gate);
+            ok(cudaGetLastError());
+        }
+        if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(st, &cap, nullptr, &g, &deps, nullptr, &nd);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, deps, nullptr, nd, &cp);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(fs.side_st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return XDEM_ERR_CUDA;
+        sst = fs.side_st;
+    }
+    if (fs.have_prev) ok(launch_clear_cells(fs.skey_prev, n, a.cstart, a.cend, sst, sort_gate));
     unsigned int *sk = nullptr, *sv = nullptr;
-    ok(radix_sort_pairs(a.k0, a.v0, a.k1, a.v1, a.hist, n, a.sort_bits, &sk, &sv, st, sort_gate));
+    ok(radix_sort_pairs(a.k0, a.v0, a.k1, a.v1, a.hist, n, a.sort_bits, &sk, &sv, sst, sort_gate));
     nl += 3 * ((a.sort_bits + 7) / 8) - 1;
     if (fs.mixed) {
-        k_reorder_mixed<<<blocks_for(n), kThreads, 0, st>>>(
+        k_reorder_mixed<<<blocks_for(n), kThreads, 0, sst>>>(
             sort_gate, sk, sv, n, np, a.cstart, a.cend, a.sorted_index, fs.skey_prev,
             fs.rec, reinterpret_cast<float4*>(fs.mA),
             reinterpret_cast<float4*>(fs.mL), reinterpret_cast<float4*>(fs.mB), reinterpret_cast<float4*>(fs.mC),
@@ -666,6 +709,17 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
                                                            org[1], org[2], fs.frame_far2);
     }
     ok(cudaGetLastError());
+    if (cond) {
+        // the body's kernels run on rebuild steps only: a replayed step
+        // counts the condition kernel
+        nl = nl_before + 1;
+        cudaGraph_t body = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(fs.side_st, &body);
+        if (e == cudaSuccess) e = ee;
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) return XDEM_ERR_CUDA;
+    }
     fs.have_prev = true;
 
     ContactLaunch c{};
