@@ -410,6 +410,14 @@ XDEM_API int xdem_sim_add_plane(xdem_sim* sim, const device_plane_info* plane,
                                 const double body[15],
                                 const device_contact_property* cp,
                                 int* body_index);
+/* Adds a cylinder (xParticleCylinderContact): its id is its rank among the
+ * handle's cylinders.  Planes come first, then cylinders, then meshes.  A
+ * handle with cylinders steps on the FP64 launcher kernels; XDEM_MIXED
+ * handles with cylinders are refused by xdem_sim_step (XDEM_ERR_ARG). */
+XDEM_API int xdem_sim_add_cylinder(xdem_sim* sim, const device_cylinder_info* cyl,
+                                   const double body[15],
+                                   const device_contact_property* cp,
+                                   int* body_index);
 /* Adds a triangle mesh.  vlist_local[ntri*9] holds each triangle's P,Q,R in
  * the body frame (as xParticleMeshObjectContact::define uploads dvList). */
 XDEM_API int xdem_sim_add_mesh(xdem_sim* sim, unsigned int ntri,
@@ -436,7 +444,8 @@ XDEM_API int xdem_sim_body_wrench(xdem_sim* sim, int body_index,
 XDEM_API int xdem_sim_get_state(xdem_sim* sim, double* pos, double* vel,
                                 double* acc, double* ep, double* ev,
                                 double* ea, double* cpos);
-/* kind: 0 particle-particle, 1 particle-plane, 2 particle-triangle. */
+/* kind: 0 particle-particle, 1 particle-plane, 2 particle-triangle,
+ * 3 particle-cylinder (MAX_P2CY_COUNT slots). */
 XDEM_API int xdem_sim_get_pairs(xdem_sim* sim, int kind, unsigned int* count,
                                 unsigned int* ids, double* tsd);
 XDEM_API int xdem_sim_set_pairs(xdem_sim* sim, int kind,

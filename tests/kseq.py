@@ -56,6 +56,11 @@ class OracleBackend:
                             s["moment"], s["mass"], s["tmax"], s["rres"], s["pl_count"], s["pl_id"], s["pl_tsd"],
                             s["np"])
 
+    def cylinder(self, s, cyl, dbi, cp):
+        return self.o.cylinder(self.prm, cyl, dbi, cp, s["bf"], s["pos"], s.get("cpos"), s["ep"], s["vel"],
+                               s["ev"], s["force"], s["moment"], s["mass"], s["tmax"], s["rres"], s["cy_count"],
+                               s["cy_id"], s["cy_tsd"], s.get("xci"), s["np"])
+
     def mesh(self, s, g, dti, dbi, cp, ntri):
         return self.o.mesh(self.prm, dti, dbi, s["bf"], s["pos"], s["ep"], s["vel"], s["ev"], s["force"],
                            s["moment"], s["mass"], s["tmax"], s["rres"], s["ms_count"], s["ms_id"], s["ms_tsd"],
@@ -187,7 +192,9 @@ def state_arrays(scene, seed=None, history=True):
              pp_tsd=_zeros(n * T.MAX_P2P_COUNT * 2), pl_count=_zeros(n, np.uint32),
              pl_id=_zeros(n * T.MAX_P2PL_COUNT, np.uint32), pl_tsd=_zeros(n * T.MAX_P2PL_COUNT * 2),
              ms_count=_zeros(n, np.uint32), ms_id=_zeros(n * T.MAX_P2MS_COUNT, np.uint32),
-             ms_tsd=_zeros(n * T.MAX_P2MS_COUNT * 2), bf=[_zeros(n) for _ in range(6)])
+             ms_tsd=_zeros(n * T.MAX_P2MS_COUNT * 2), cy_count=_zeros(n, np.uint32),
+             cy_id=_zeros(n * T.MAX_P2CY_COUNT, np.uint32), cy_tsd=_zeros(n * T.MAX_P2CY_COUNT * 2),
+             bf=[_zeros(n) for _ in range(6)])
     if scene.cpos is not None:
         s["cpos"] = scene.cpos.copy()
         s["xci"] = scene.xci.copy()
@@ -257,6 +264,9 @@ def sphere_step(be, scene, s, meshes=(), compat=1, nplanes=None):
     for k, pl in enumerate(planes):
         st |= be.plane(s, pl, np.asarray(scene.plane_body[k]), scene.plane_cp[k])
         partials.append([b.copy() for b in s["bf"]])
+    for cy in getattr(scene, "cylinders", []):
+        st |= be.cylinder(s, cy["cyl"], np.asarray(cy["body"]), cy["cp"])
+        partials.append([b.copy() for b in s["bf"]])
     for m in meshes:
         s["dsph"] = m["sphere"]
         st |= be.mesh(s, g, m["dti"], m["body"], m["cp"], m["ntri"])
@@ -281,6 +291,9 @@ def cluster_step(be, scene, s, meshes=()):
     partials = []
     for k, pl in enumerate(scene.planes):
         st |= be.cluster_plane(s, pl, np.asarray(scene.plane_body[k]), scene.plane_cp[k])
+        partials.append([b.copy() for b in s["bf"]])
+    for cy in getattr(scene, "cylinders", []):
+        st |= be.cylinder(s, cy["cyl"], np.asarray(cy["body"]), cy["cp"])
         partials.append([b.copy() for b in s["bf"]])
     for m in meshes:
         st |= be.cluster_mesh(s, g, m["dti"], m["body"], m["cp"], m["ntri"])

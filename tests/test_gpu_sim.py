@@ -163,3 +163,110 @@ def test_caller_stream_survives_the_handle(simmod):
         else:
             assert np.array_equal(ref["pos"], st["pos"])
     stream.synchronize()
+
+
+def drum(n=1500, seed=31, cluster=False):
+    """Spheres (or three-sphere clusters) in a cylinder of radius 20 mm,
+    length 40 mm and 2 mm wall, open at the top, spinning slowly about its
+    axis (y) and drifting, with random velocities: contacts with the inner
+    wall, the base cap from inside and each other."""
+    rng = np.random.default_rng(seed)
+    L, R = 0.04, 0.02
+    cyl = T.CylinderInfo()
+    cyl.empty_part = 1
+    cyl.thickness = 0.002
+    cyl.len_rr = T.d3((L, R, R))
+    cyl.pbase = T.d3((0.0, -0.5 * L, 0.0))
+    cyl.ptop = T.d3((0.0, 0.5 * L, 0.0))
+    body = T.body_record(mass=0.5, pos=(0.001, 0.002, -0.001), vel=(0.0, 0.0, 0.01), ed=(0.0, 0.0, 1.5, 0.0))
+    if cluster:
+        sc = scenes.cluster_bed(n // 3, neach=3, sub_r=1e-3, seed=seed, trough=(0.03, 0.03, 0.03),
+                                spacing_factor=0.75, vel_scale=0.2)
+        # the bed centred on the axis with its lowest members 0.2 mm into
+        # the base, cluster centres spread by 1.2 about the axis (each
+        # cluster moved rigidly) so that the outer members reach the wall
+        p = sc.pos.reshape(-1, 3, 4)
+        c = sc.cpos.reshape(-1, 4)
+        low = np.array([p[..., 0].mean(), p[..., 1].min() - 0.8e-3, p[..., 2].mean()])
+        shift = body[1:4] + np.array([0.0, -0.5 * L, 0.0]) - low
+        p[..., :3] += shift
+        c[:, :3] += shift
+        move = np.zeros((c.shape[0], 3))
+        move[:, [0, 2]] = 0.2 * (c[:, [0, 2]] - body[[1, 3]])
+        c[:, :3] += move
+        p[..., :3] += move[:, None, :]
+        sc.pos, sc.cpos = p.ravel(), c.ravel()
+    else:
+        sc = scenes.random_packed(n, 0.8e-3, 1.2e-3, None, seed=seed, vel_scale=0.3)
+        rho = R * np.sqrt(rng.uniform(0, 1, n)) * 0.97
+        th = rng.uniform(0, 2 * np.pi, n)
+        p = sc.pos.reshape(-1, 4).copy()
+        p[:, 0] = body[1] + rho * np.cos(th)
+        p[:, 2] = body[3] + rho * np.sin(th)
+        p[:, 1] = body[2] + rng.uniform(-0.5 * L + 0.5e-3, 0.3 * L, n)
+        sc.pos = p.ravel()
+    sc.planes, sc.plane_cp, sc.plane_body = [], [], []
+    sc.cylinders = [dict(cyl=cyl, body=body, cp=sc.pp_cp)]
+    return sc
+
+
+@pytest.mark.parametrize("cluster", [False, True])
+def test_handle_with_cylinder_matches_oracle(simmod, oracle, cluster):
+    """A handle with a cylinder (launcher kernels, FP64) against the oracle's
+    step sequence with its cylinder contact (pinned to the reference's own
+    cylinder kernels), six steps; pair lists exact, state to 1e-11."""
+    sc = drum(cluster=cluster)
+    sm = simmod.Sim(sc, precision=T.XDEM_FP64)
+    s = kseq.state_arrays(sc)
+    be = kseq.OracleBackend(oracle)
+    touched = 0
+    for step in range(6):
+        sm.step(1)
+        if cluster:
+            kseq.cluster_step(be, sc, s, ())
+        else:
+            kseq.sphere_step(be, sc, s, (), compat=0)
+        st = sm.state()
+        for k in ("pos", "vel", "acc", "ep", "ev", "ea"):
+            scale = max(np.abs(s[k]).max(), 1e-300)
+            assert np.abs(st[k] - s[k]).max() <= 1e-11 * scale, (step, k)
+        for kind, (ck, ik, cap) in ((0, ("pp_count", "pp_id", 12)), (3, ("cy_count", "cy_id", 3))):
+            cnt, ids, _ = sm.pairs(kind)
+            assert kseq.pairs_equal(cnt, ids, s[ck], s[ik], cap) == sc.np_, (step, ck)
+        touched += int(s["cy_count"].sum())
+    assert sm.status() == 0
+    assert touched > 0
+    w = sm.wrench(sm.bodies[0])
+    assert np.abs(w).max() > 0
+
+
+def test_mixed_handle_with_cylinder_is_refused(simmod):
+    sm = simmod.Sim(drum(n=300), precision=T.XDEM_MIXED)
+    with pytest.raises(Exception):
+        sm.step(1)
+    sm.close()
+
+
+def test_cylinder_pairs_survive_a_part_file(simmod, tmp_path):
+    """save_part writes the cylinder block between the plane and triangle
+    blocks (xResultManager.cpp:897-902); a handle loaded from it continues
+    bit for bit."""
+    from xdynamics_dll_gb300 import partfile
+    sc = drum(n=800, seed=5)
+    a = simmod.Sim(sc, precision=T.XDEM_FP64)
+    a.step(5)
+    path = tmp_path / "cyl.bin"
+    a.save_part(path, 5e-5)
+    d = partfile.read(path, kinds=("pp", "cy"))
+    cnt, ids, tsd = a.pairs(3)
+    assert np.array_equal(d["cy_count"], cnt) and np.array_equal(d["cy_id"], ids) and np.array_equal(d["cy_tsd"], tsd)
+    assert cnt.sum() > 0
+    b = simmod.Sim(sc, precision=T.XDEM_FP64)
+    b.load_part(path)
+    a.step(4)
+    b.step(4)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+    a.close()
+    b.close()

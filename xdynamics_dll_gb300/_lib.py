@@ -58,6 +58,7 @@ _SIGS = {
     "xdem_sim_set_scenes": ([vp, u32, vp, vp, vp], i32),
     "xdem_sim_scene_energy": ([vp, vp, vp], i32),
     "xdem_sim_add_plane": ([vp] * 5, i32),
+    "xdem_sim_add_cylinder": ([vp] * 5, i32),
     "xdem_sim_add_mesh": ([vp, u32, vp, vp, vp, vp], i32),
     "xdem_sim_get_mesh": ([vp, i32, vp, vp, vp], i32),
     "xdem_sim_set_body": ([vp, i32, vp, vp], i32),

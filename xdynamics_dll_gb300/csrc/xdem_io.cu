@@ -10,6 +10,7 @@
 //   double   cpos[ns*4]                     (clusters only)
 //   uint32   p2p count[np], id[np*12]; double p2p tsd[np*24]    (particle pairs)
 //   uint32   p2pl count[np], id[np*3]; double p2pl tsd[np*6]    (planes)
+//   uint32   p2cyl count[np], id[np*3]; double p2cyl tsd[np*6]  (cylinders)
 //   uint32   p2tri count[np], id[np*5]; double p2tri tsd[np*10] (meshes)
 //
 // little-endian, no padding.  The reference writes the pair blocks of the
@@ -48,12 +49,17 @@ bool get(FILE* f, std::vector<T>& v)
     return v.empty() || std::fread(v.data(), sizeof(T), v.size(), f) == v.size();
 }
 
-// The pair blocks a handle's part file holds.
-void blocks(const xdem_sim* s, bool& pp, bool& pl, bool& ms)
+// The pair blocks a handle's part file holds, in file order, as pair kinds
+// of xdem_sim_get_pairs (0 particles, 1 planes, 3 cylinders, 2 meshes).
+constexpr int kBlocks = 4;
+const int kBlockKind[kBlocks] = {0, 1, 3, 2};
+const unsigned int kBlockCap[kBlocks] = {MAX_P2P_COUNT, MAX_P2PL_COUNT, MAX_P2CY_COUNT, MAX_P2MS_COUNT};
+void blocks(const xdem_sim* s, bool want[kBlocks])
 {
-    pp = s->has_pp;
-    pl = !s->planes.empty();
-    ms = !s->meshes.empty();
+    want[0] = s->has_pp;
+    want[1] = !s->planes.empty();
+    want[2] = !s->cylinders.empty();
+    want[3] = !s->meshes.empty();
 }
 
 }  // namespace
@@ -70,21 +76,19 @@ XDEM_API int xdem_sim_save_part(xdem_sim* s, const char* path, double time)
         return r;
     if (cudaMemcpy(mass.data(), s->mass, ns * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
         return XDEM_ERR_CUDA;
-    bool bpp, bpl, bms;
-    blocks(s, bpp, bpl, bms);
+    bool want[kBlocks];
+    blocks(s, want);
     File out(path, "wb");
     if (!out.f) return XDEM_ERR_ARG;
     const unsigned int n32[2] = {(unsigned int)np, (unsigned int)ns};
     bool ok = std::fwrite(&time, sizeof(double), 1, out.f) == 1 && std::fwrite(n32, sizeof(n32), 1, out.f) == 1;
     ok = ok && put(out.f, mass) && put(out.f, pos) && put(out.f, vel) && put(out.f, acc) && put(out.f, ep) &&
          put(out.f, ev) && put(out.f, ea) && put(out.f, cpos);
-    const bool want[3] = {bpp, bpl, bms};
-    const unsigned int cap[3] = {MAX_P2P_COUNT, MAX_P2PL_COUNT, MAX_P2MS_COUNT};
-    for (int kind = 0; kind < 3 && ok; ++kind) {
-        if (!want[kind]) continue;
-        std::vector<unsigned int> cnt(np), ids(np * cap[kind]);
-        std::vector<double> tsd(np * cap[kind] * 2);
-        if (int r = xdem_sim_get_pairs(s, kind, cnt.data(), ids.data(), tsd.data())) return r;
+    for (int b = 0; b < kBlocks && ok; ++b) {
+        if (!want[b]) continue;
+        std::vector<unsigned int> cnt(np), ids(np * kBlockCap[b]);
+        std::vector<double> tsd(np * kBlockCap[b] * 2);
+        if (int r = xdem_sim_get_pairs(s, kBlockKind[b], cnt.data(), ids.data(), tsd.data())) return r;
         ok = put(out.f, cnt) && put(out.f, ids) && put(out.f, tsd);
     }
     return ok ? XDEM_OK : XDEM_ERR_ARG;
@@ -106,18 +110,16 @@ XDEM_API int xdem_sim_load_part(xdem_sim* s, const char* path, double* time)
     bool ok = get(in.f, mass) && get(in.f, pos) && get(in.f, vel) && get(in.f, acc) && get(in.f, ep) &&
               get(in.f, ev) && get(in.f, ea) && get(in.f, cpos);
     if (!ok) return XDEM_ERR_ARG;
-    bool bpp, bpl, bms;
-    blocks(s, bpp, bpl, bms);
-    const bool want[3] = {bpp, bpl, bms};
-    const unsigned int cap[3] = {MAX_P2P_COUNT, MAX_P2PL_COUNT, MAX_P2MS_COUNT};
-    std::vector<unsigned int> cnt[3], ids[3];
-    std::vector<double> tsd[3];
-    for (int kind = 0; kind < 3; ++kind) {
-        if (!want[kind]) continue;
-        cnt[kind].resize(np);
-        ids[kind].resize(np * cap[kind]);
-        tsd[kind].resize(np * cap[kind] * 2);
-        if (!(get(in.f, cnt[kind]) && get(in.f, ids[kind]) && get(in.f, tsd[kind]))) return XDEM_ERR_ARG;
+    bool want[kBlocks];
+    blocks(s, want);
+    std::vector<unsigned int> cnt[kBlocks], ids[kBlocks];
+    std::vector<double> tsd[kBlocks];
+    for (int b = 0; b < kBlocks; ++b) {
+        if (!want[b]) continue;
+        cnt[b].resize(np);
+        ids[b].resize(np * kBlockCap[b]);
+        tsd[b].resize(np * kBlockCap[b] * 2);
+        if (!(get(in.f, cnt[b]) && get(in.f, ids[b]) && get(in.f, tsd[b]))) return XDEM_ERR_ARG;
     }
     char extra;
     if (std::fread(&extra, 1, 1, in.f) != 0) return XDEM_ERR_ARG;  // blocks this handle has no contacts for
@@ -133,9 +135,9 @@ XDEM_API int xdem_sim_load_part(xdem_sim* s, const char* path, double* time)
             return XDEM_ERR_CUDA;
     }
     if (int r = xdem_sim_step(s, 0)) return r;  // pair tables exist before they are filled
-    for (int kind = 0; kind < 3; ++kind) {
-        if (!want[kind]) continue;
-        if (int r = xdem_sim_set_pairs(s, kind, cnt[kind].data(), ids[kind].data(), tsd[kind].data())) return r;
+    for (int b = 0; b < kBlocks; ++b) {
+        if (!want[b]) continue;
+        if (int r = xdem_sim_set_pairs(s, kBlockKind[b], cnt[b].data(), ids[b].data(), tsd[b].data())) return r;
     }
     if (time) *time = t;
     return XDEM_OK;

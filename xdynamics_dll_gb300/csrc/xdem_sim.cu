@@ -175,6 +175,15 @@ int upload_bodies(xdem_sim* s)
             e = cudaMemcpyAsync(s->d_planes, s->planes.data(), s->planes.size() * sizeof(device_plane_info),
                                 cudaMemcpyHostToDevice, s->st);
     }
+    if (e == cudaSuccess && s->cylinders.size()) {
+        if (s->cylinders.size() > s->cyl_cap) {
+            e = dalloc(s->d_cyl, s->cylinders.size());
+            s->cyl_cap = e == cudaSuccess ? s->cylinders.size() : 0;
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d_cyl, s->cylinders.data(), s->cylinders.size() * sizeof(device_cylinder_info),
+                                cudaMemcpyHostToDevice, s->st);
+    }
     std::vector<double> rec(std::max<size_t>(nb, 1) * 15, 0.0);
     for (size_t i = 0; i < nb; ++i) std::memcpy(&rec[i * 15], s->bodies[i].rec, sizeof(double) * 15);
     if (e == cudaSuccess && rec.size() / 15 > s->body_cap) {
@@ -264,6 +273,10 @@ int step_launcher(xdem_sim* s, cudaEvent_t e0, cudaEvent_t e1)
             else
                 ok(launch_plane(p, pl, dbi, mp, bp, s->pos, s->ep, s->vel, s->ev, s->force, s->moment, s->mass,
                                 s->tmax, s->rres, s->pl_count, s->pl_id, s->pl_tsd, n, s->d_status, st));
+        } else if (bd.kind == 2) {
+            ok(launch_cylinder(p, s->d_cyl + bd.index, dbi, mp, bp, s->pos, s->clusters ? s->cpos : nullptr, s->ep,
+                               s->vel, s->ev, s->force, s->moment, s->mass, s->tmax, s->rres, s->cy_count, s->cy_id,
+                               s->cy_tsd, s->clusters ? s->xci : nullptr, n, s->d_status, st));
         } else {
             const SimMesh& m = s->meshes[bd.index];
             ok(launch_mesh(p, s->d_tri + m.first, n, s->clusters ? 2 : 1, dbi, mp, bp, s->pos,
@@ -317,11 +330,30 @@ int mixed_cluster_tab(const xdem_sim* s, ClusterTab& t)
     return XDEM_OK;
 }
 
+// Pair tables of one contact kind: 0 particle pairs, 1 planes, 2 triangle
+// meshes, 3 cylinders.
+struct PairTables {
+    unsigned int cap;
+    unsigned int *count, *id;
+    double* tsd;
+};
+PairTables pair_tables(xdem_sim* s, int kind)
+{
+    switch (kind) {
+    case 0: return PairTables{MAX_P2P_COUNT, s->pp_count, s->pp_id, s->pp_tsd};
+    case 1: return PairTables{MAX_P2PL_COUNT, s->pl_count, s->pl_id, s->pl_tsd};
+    case 2: return PairTables{MAX_P2MS_COUNT, s->ms_count, s->ms_id, s->ms_tsd};
+    default: return PairTables{MAX_P2CY_COUNT, s->cy_count, s->cy_id, s->cy_tsd};
+    }
+}
+
 // Steps run on the fused step (sphere scenes of either precision, and
-// mixed cluster scenes) unless the launcher path was asked for.
+// mixed cluster scenes) unless the launcher path was asked for or the scene
+// has cylinders.
 bool fused_path(const xdem_sim* s)
 {
-    return !s->cfg.launcher_path && (!s->clusters || s->precision_mixed());
+    // cylinders run on the launcher kernels (FP64)
+    return !s->cfg.launcher_path && s->cylinders.empty() && (!s->clusters || s->precision_mixed());
 }
 
 FusedArgs fused_args(xdem_sim* s)
@@ -495,6 +527,7 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
     A(s->pp_count, n); A(s->pp_id, n * MAX_P2P_COUNT); A(s->pp_tsd, n * MAX_P2P_COUNT * 2);
     A(s->pl_count, n); A(s->pl_id, n * MAX_P2PL_COUNT); A(s->pl_tsd, n * MAX_P2PL_COUNT * 2);
     A(s->ms_count, n); A(s->ms_id, n * MAX_P2MS_COUNT); A(s->ms_tsd, n * MAX_P2MS_COUNT * 2);
+    A(s->cy_count, n); A(s->cy_id, n * MAX_P2CY_COUNT); A(s->cy_tsd, n * MAX_P2CY_COUNT * 2);
     A(s->cstart, ncell); A(s->cend, ncell);
     A(s->d_status, 1);
     A(s->d_mp, 65);
@@ -514,6 +547,7 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out)
     Z(s->pp_count, n * 4); Z(s->pp_id, n * 4 * MAX_P2P_COUNT); Z(s->pp_tsd, n * 16 * MAX_P2P_COUNT);
     Z(s->pl_count, n * 4); Z(s->pl_id, n * 4 * MAX_P2PL_COUNT); Z(s->pl_tsd, n * 16 * MAX_P2PL_COUNT);
     Z(s->ms_count, n * 4); Z(s->ms_id, n * 4 * MAX_P2MS_COUNT); Z(s->ms_tsd, n * 16 * MAX_P2MS_COUNT);
+    Z(s->cy_count, n * 4); Z(s->cy_id, n * 4 * MAX_P2CY_COUNT); Z(s->cy_tsd, n * 16 * MAX_P2CY_COUNT);
     Z(s->d_status, 4);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) {
@@ -531,18 +565,19 @@ XDEM_API int xdem_sim_destroy(xdem_sim* s)
     drop_graph(s);
     fused_free(s->fs);
     double* dp[] = {s->pos, s->cpos, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass,
-                    s->inertia, s->tmax, s->rres, s->rloc, s->pp_tsd, s->pl_tsd, s->ms_tsd, s->d_body,
+                    s->inertia, s->tmax, s->rres, s->rloc, s->pp_tsd, s->pl_tsd, s->ms_tsd, s->cy_tsd, s->d_body,
                     s->d_vlist, s->d_dlocal, s->d_sphere, s->bsums, s->wrench, s->d_scene_energy};
     for (double* q : dp)
         if (q) cudaFree(q);
     unsigned int* up[] = {s->k0, s->v0, s->k1, s->v1, s->hist, s->cstart, s->cend, s->sorted_index, s->pp_count,
-                          s->pp_id, s->pl_count, s->pl_id, s->ms_count, s->ms_id, s->d_status,
+                          s->pp_id, s->pl_count, s->pl_id, s->ms_count, s->ms_id, s->cy_count, s->cy_id, s->d_status,
                           s->d_scene_of, s->d_scene_first, s->d_scene_plane_first};
     for (unsigned int* q : up)
         if (q) cudaFree(q);
     if (s->xci) cudaFree(s->xci);
     if (s->d_mp) cudaFree(s->d_mp);
     if (s->d_planes) cudaFree(s->d_planes);
+    if (s->d_cyl) cudaFree(s->d_cyl);
     if (s->d_tri) cudaFree(s->d_tri);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
@@ -674,7 +709,7 @@ XDEM_API int xdem_sim_add_plane(xdem_sim* s, const device_plane_info* plane, con
 {
     if (!s || !plane || !body || !cp) return XDEM_ERR_ARG;
     if (s->bodies.size() >= kMaxBodies) return XDEM_ERR_ARG;
-    if (!s->meshes.empty()) return XDEM_ERR_ARG;  // planes first, in id order, then meshes
+    if (!s->meshes.empty() || !s->cylinders.empty()) return XDEM_ERR_ARG;  // planes first, in id order
     SimBody b{};
     b.kind = 0;
     b.index = (int)s->planes.size();
@@ -685,6 +720,28 @@ XDEM_API int xdem_sim_add_plane(xdem_sim* s, const device_plane_info* plane, con
     s->bodies.push_back(b);
     s->body_cp.push_back(*cp);
     s->prm.nplane = (unsigned int)s->planes.size();
+    s->dirty_bodies = true;
+    s->dirty_alloc = true;
+    if (body_index) *body_index = (int)s->bodies.size() - 1;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_add_cylinder(xdem_sim* s, const device_cylinder_info* cyl, const double body[15],
+                                   const device_contact_property* cp, int* body_index)
+{
+    if (!s || !cyl || !body || !cp) return XDEM_ERR_ARG;
+    if (s->bodies.size() >= kMaxBodies) return XDEM_ERR_ARG;
+    if (!s->meshes.empty()) return XDEM_ERR_ARG;  // planes, then cylinders, then meshes
+    SimBody b{};
+    b.kind = 2;
+    b.index = (int)s->cylinders.size();
+    std::memcpy(b.rec, body, sizeof(b.rec));
+    device_cylinder_info c = *cyl;
+    c.id = (unsigned int)s->cylinders.size();  // ids in definition order, as xParticleCylinderContact counts them
+    s->cylinders.push_back(c);
+    s->bodies.push_back(b);
+    s->body_cp.push_back(*cp);
+    s->prm.ncylinder = (unsigned int)s->cylinders.size();
     s->dirty_bodies = true;
     s->dirty_alloc = true;
     if (body_index) *body_index = (int)s->bodies.size() - 1;
@@ -806,6 +863,8 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->clusters && !s->xci) return XDEM_ERR_ARG;
+    // cylinders run on the FP64 launcher kernels only
+    if (!s->cylinders.empty() && s->precision_mixed()) return XDEM_ERR_ARG;
     // mixed clusters: the fused step's cluster form (one member count, no
     // rolling resistance or cohesion)
     if (s->clusters && s->precision_mixed()) {
@@ -932,12 +991,13 @@ XDEM_API int xdem_sim_get_state(xdem_sim* s, double* pos, double* vel, double* a
 
 XDEM_API int xdem_sim_get_pairs(xdem_sim* s, int kind, unsigned int* count, unsigned int* ids, double* tsd)
 {
-    if (!s || kind < 0 || kind > 2) return XDEM_ERR_ARG;
+    if (!s || kind < 0 || kind > 3) return XDEM_ERR_ARG;
     const size_t n = s->np;
-    const unsigned int cap = kind == 0 ? MAX_P2P_COUNT : kind == 1 ? MAX_P2PL_COUNT : MAX_P2MS_COUNT;
-    const unsigned int* dc = kind == 0 ? s->pp_count : kind == 1 ? s->pl_count : s->ms_count;
-    const unsigned int* di = kind == 0 ? s->pp_id : kind == 1 ? s->pl_id : s->ms_id;
-    const double* dt = kind == 0 ? s->pp_tsd : kind == 1 ? s->pl_tsd : s->ms_tsd;
+    const PairTables t = pair_tables(s, kind);
+    const unsigned int cap = t.cap;
+    const unsigned int* dc = t.count;
+    const unsigned int* di = t.id;
+    const double* dt = t.tsd;
     cudaError_t e = cudaStreamSynchronize(s->st);
     if (e == cudaSuccess && count) e = cudaMemcpy(count, dc, n * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && ids) e = cudaMemcpy(ids, di, n * 4 * cap, cudaMemcpyDeviceToHost);
@@ -948,12 +1008,13 @@ XDEM_API int xdem_sim_get_pairs(xdem_sim* s, int kind, unsigned int* count, unsi
 XDEM_API int xdem_sim_set_pairs(xdem_sim* s, int kind, const unsigned int* count, const unsigned int* ids,
                                 const double* tsd)
 {
-    if (!s || kind < 0 || kind > 2 || !count || !ids || !tsd) return XDEM_ERR_ARG;
+    if (!s || kind < 0 || kind > 3 || !count || !ids || !tsd) return XDEM_ERR_ARG;
     const size_t n = s->np;
-    const unsigned int cap = kind == 0 ? MAX_P2P_COUNT : kind == 1 ? MAX_P2PL_COUNT : MAX_P2MS_COUNT;
-    unsigned int* dc = kind == 0 ? s->pp_count : kind == 1 ? s->pl_count : s->ms_count;
-    unsigned int* di = kind == 0 ? s->pp_id : kind == 1 ? s->pl_id : s->ms_id;
-    double* dt = kind == 0 ? s->pp_tsd : kind == 1 ? s->pl_tsd : s->ms_tsd;
+    const PairTables t = pair_tables(s, kind);
+    const unsigned int cap = t.cap;
+    unsigned int* dc = t.count;
+    unsigned int* di = t.id;
+    double* dt = t.tsd;
     cudaError_t e = cudaStreamSynchronize(s->st);
     if (e == cudaSuccess) e = cudaMemcpy(dc, count, n * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(di, ids, n * 4 * cap, cudaMemcpyHostToDevice);

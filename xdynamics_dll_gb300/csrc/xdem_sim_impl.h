@@ -18,7 +18,7 @@ using namespace xdem;
 constexpr size_t kMaxBodies = 1u << 16;
 
 struct SimBody {
-    int kind;              // 0 plane, 1 mesh
+    int kind;              // 0 plane, 1 mesh, 2 cylinder
     int index;             // plane index or mesh index
     double rec[15];
 };
@@ -62,8 +62,12 @@ struct xdem_sim {
     double* pl_tsd = nullptr;
     unsigned int *ms_count = nullptr, *ms_id = nullptr;
     double* ms_tsd = nullptr;
+    unsigned int *cy_count = nullptr, *cy_id = nullptr;  // cylinder pairs, MAX_P2CY_COUNT slots
+    double* cy_tsd = nullptr;
     std::vector<SimBody> bodies;
     std::vector<device_plane_info> planes;
+    std::vector<device_cylinder_info> cylinders;
+    device_cylinder_info* d_cyl = nullptr;
     std::vector<device_contact_property> body_cp;
     std::vector<SimMesh> meshes;
     device_plane_info* d_planes = nullptr;
@@ -109,5 +113,5 @@ struct xdem_sim {
     unsigned int* d_scene_plane_first = nullptr;  // [nscene + 1]
     double* d_scene_energy = nullptr;             // [2 * nscene]
     // capacities of the body tables
-    size_t plane_cap = 0, body_cap = 0, mp_cap = 0;
+    size_t plane_cap = 0, body_cap = 0, mp_cap = 0, cyl_cap = 0;
 };

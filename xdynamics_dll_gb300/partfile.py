@@ -4,8 +4,9 @@ into and written from dicts of numpy arrays.
 
     time (f64); np, ns (u32); mass[ns]; pos[np*4]; vel, acc[ns*3];
     ep, ev, ea[ns*4]; cpos[ns*4] (clusters only); then for each contact kind
-    present: count[np] (u32), id[np*cap] (u32), tsd[np*cap*2] (f64), with cap
-    12 (particle pairs), 3 (planes), 5 (triangles).
+    present, in the order particle pairs, planes, cylinders, triangles:
+    count[np] (u32), id[np*cap] (u32), tsd[np*cap*2] (f64), with cap 12
+    (particle pairs), 3 (planes), 3 (cylinders), 5 (triangles).
 
 A file does not say which pair blocks it holds: the reader takes them from
 the model (`kinds`), as the reference does, and checks that the sizes add
@@ -14,7 +15,15 @@ Handles write and read the same layout with xdem_sim_save_part / load_part.
 """
 import numpy as np
 
-CAPS = {"pp": 12, "pl": 3, "ms": 5}
+CAPS = {"pp": 12, "pl": 3, "cy": 3, "ms": 5}
+ORDER = ("pp", "pl", "cy", "ms")
+
+
+def _ordered(kinds):
+    bad = [k for k in kinds if k not in CAPS]
+    if bad:
+        raise ValueError(f"unknown pair blocks {bad}")
+    return [k for k in ORDER if k in kinds]
 
 
 def read(path, kinds=("pp", "pl")):
@@ -38,7 +47,7 @@ def read(path, kinds=("pp", "pl")):
     d["ea"] = take("<f8", ns * 4)
     if npart != ns:
         d["cpos"] = take("<f8", ns * 4)
-    for k in kinds:
+    for k in _ordered(kinds):
         cap = CAPS[k]
         d[k + "_count"] = take("<u4", npart)
         d[k + "_id"] = take("<u4", npart * cap)
@@ -61,7 +70,7 @@ def write(path, d, kinds=("pp", "pl")):
             f.write(a.tobytes())
         if npart != ns:
             f.write(np.asarray(d["cpos"], "<f8").ravel().tobytes())
-        for k in kinds:
+        for k in _ordered(kinds):
             cap = CAPS[k]
             f.write(np.asarray(d[k + "_count"], "<u4").ravel().tobytes())
             f.write(np.asarray(d[k + "_id"], "<u4").ravel().tobytes())

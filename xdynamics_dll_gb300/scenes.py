@@ -40,6 +40,7 @@ class Scene:
     plane_cp: list = field(default_factory=list)      # ContactProperty
     plane_body: list = field(default_factory=list)    # 15-double records
     meshes: list = field(default_factory=list)        # dicts: vlist_local, body, cp
+    cylinders: list = field(default_factory=list)     # dicts: cyl (CylinderInfo), body, cp
     cpos: np.ndarray = None    # clusters: [ns*4]
     xci: np.ndarray = None     # clusters: uint32 [nco*4]
     rloc: np.ndarray = None    # clusters: [neach*3]
@@ -52,7 +53,7 @@ class Scene:
                              origin=self.origin, gravity=self.gravity,
                              contact_model=self.contact_model,
                              ncluster=self.ns if self.ns != self.np_ else 0, nco=nco,
-                             nplane=len(self.planes))
+                             nplane=len(self.planes), ncylinder=len(self.cylinders))
 
     def copy(self):
         import copy

@@ -53,6 +53,12 @@ class Sim:
             _lib.check(self.L.xdem_sim_add_plane(h, C.byref(pl), _p(rec), C.byref(scene.plane_cp[k]), C.byref(b)),
                        "xdem_sim_add_plane")
             self.bodies.append(b.value)
+        for cy in getattr(scene, "cylinders", []):
+            b = C.c_int()
+            rec = np.ascontiguousarray(cy["body"], dtype=np.float64)
+            _lib.check(self.L.xdem_sim_add_cylinder(h, C.byref(cy["cyl"]), _p(rec), C.byref(cy["cp"]), C.byref(b)),
+                       "xdem_sim_add_cylinder")
+            self.bodies.append(b.value)
         for m in scene.meshes:
             b = C.c_int()
             vl = np.ascontiguousarray(m["vlist_local"], dtype=np.float64).reshape(-1)
@@ -93,7 +99,8 @@ class Sim:
         return out
 
     def pairs(self, kind):
-        cap = [T.MAX_P2P_COUNT, T.MAX_P2PL_COUNT, T.MAX_P2MS_COUNT][kind]
+        """kind 0 particle pairs, 1 planes, 2 triangles, 3 cylinders."""
+        cap = [T.MAX_P2P_COUNT, T.MAX_P2PL_COUNT, T.MAX_P2MS_COUNT, T.MAX_P2CY_COUNT][kind]
         n = self.scene.np_
         cnt = np.zeros(n, np.uint32)
         ids = np.zeros(n * cap, np.uint32)

@@ -139,7 +139,7 @@ def d3(v):
 
 
 def make_params(*, np_, dt, gravity=(0.0, -9.80665, 0.0), cell_size, grid=(128, 128, 128),
-                origin=(-1.0, -1.0, -1.0), contact_model=1, ncluster=0, nco=0, nplane=0):
+                origin=(-1.0, -1.0, -1.0), contact_model=1, ncluster=0, nco=0, nplane=0, ncylinder=0):
     p = DemParameters()
     p.rollingCondition = False
     p.contact_model = contact_model
@@ -147,6 +147,7 @@ def make_params(*, np_, dt, gravity=(0.0, -9.80665, 0.0), cell_size, grid=(128, 
     p.nCluster = ncluster
     p.nClusterObject = nco
     p.nplane = nplane
+    p.ncylinder = ncylinder
     p.ncell = grid[0] * grid[1] * grid[2]
     p.grid_size = UInt3(*grid)
     p.dt = dt
