@@ -175,6 +175,11 @@ XDEM_API int xdem_last_body_wrench(double out6[6]);
  * 0 (default) applies the velocity-Verlet trapezoid to it as the CPU path and
  * the cluster kernel do (xIntegratorVV.cpp:143-149, impl:279-284). */
 XDEM_API int xdem_set_velocity_compat(int reproduce_reference_gpu);
+/* Rolling resistance of free spheres (cu_decide_rolling_friction_moment):
+ * 0 (default) reads J = inertia[id] of the double3 inertia array as the
+ * reference kernel does (impl:2434), i.e. an entry of sphere id/3; 1 reads
+ * the sphere's own J = inertia[3 id]. */
+XDEM_API int xdem_set_rolling_inertia(int per_sphere);
 /* Library build string. */
 XDEM_API const char* xdem_version(void);
 
@@ -466,6 +471,8 @@ XDEM_API int xdem_sim_save_part(xdem_sim* sim, const char* path, double time);
 XDEM_API int xdem_sim_load_part(xdem_sim* sim, const char* path, double* time);
 /* Status bits accumulated since the last call. */
 XDEM_API int xdem_sim_status(xdem_sim* sim);
+/* The same switch as xdem_set_rolling_inertia, for this handle's steps. */
+XDEM_API int xdem_sim_set_rolling_inertia(xdem_sim* sim, int per_sphere);
 /* Stream the handle's kernels run on (cudaStream_t).  The stream stays the
  * caller's: keep it alive while the handle uses it; xdem_sim_destroy never
  * destroys it.  NULL returns to the handle's own stream. */

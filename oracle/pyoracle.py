@@ -87,9 +87,9 @@ class Oracle:
                          _p(cs), _p(ce), C.byref(cp), C.c_uint(np_), C.c_uint(ntri), C.byref(st))
         return st.value
 
-    def rolling(self, prm, tmax, rres, inertia, ep, ev, moment, np_):
-        self.lib.xo_rolling(C.byref(prm), _p(tmax), _p(rres), _p(inertia), _p(ep), _p(ev), _p(moment),
-                            C.c_uint(np_))
+    def rolling(self, prm, tmax, rres, inertia, ep, ev, moment, np_, per_sphere=0):
+        self.lib.xo_rolling_ex(C.byref(prm), _p(tmax), _p(rres), _p(inertia), _p(ep), _p(ev), _p(moment),
+                               C.c_uint(np_), C.c_int(per_sphere))
 
     def update_mesh(self, dbi, vlist, sphere, dlocal, dpi, ntri):
         self.lib.xo_update_mesh(_p(dbi), _p(vlist), _p(sphere), _p(dlocal), _p(dpi), C.c_uint(ntri))

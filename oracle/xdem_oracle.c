@@ -922,6 +922,14 @@ void xo_cluster_mesh(const device_dem_parameters* prm, const device_triangle_inf
 void xo_rolling(const device_dem_parameters* prm, double* tmax, double* rres, const double* inertia,
                 const double* ep, const double* ev, double* moment, unsigned int np)
 {
+    xo_rolling_ex(prm, tmax, rres, inertia, ep, ev, moment, np, 0);
+}
+
+/* per_sphere = 1 reads the sphere's own inertia, inertia[3 i] (the three
+ * entries are equal for a sphere), instead of the flat inertia[i]. */
+void xo_rolling_ex(const device_dem_parameters* prm, double* tmax, double* rres, const double* inertia,
+                   const double* ep, const double* ev, double* moment, unsigned int np, int per_sphere)
+{
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -929,7 +937,7 @@ void xo_rolling(const device_dem_parameters* prm, double* tmax, double* rres, co
         double Tr = rres[i];
         if (!Tr) continue;
         v3 Tmax = ld3(tmax, i);
-        double J = inertia[i];          /* scalar read of a double3 array, impl:2434 */
+        double J = per_sphere ? inertia[3 * i] : inertia[i];  /* impl:2434 reads the flat entry i */
         v3 om = ang_vel(ld4(ep, i), ld4(ev, i));
         v3 T = sub3(mul3(J * prm->dt, om), Tmax);
         double lT = len3(T);

@@ -88,6 +88,11 @@ void xo_mesh(const device_dem_parameters* prm, const device_triangle_info* dti,
 void xo_rolling(const device_dem_parameters* prm, double* tmax, double* rres,
                 const double* inertia, const double* ep, const double* ev,
                 double* moment, unsigned int np);
+/* xo_rolling with per_sphere = 1: J = inertia[3 i], the sphere's own entry
+ * (impl:2434 reads the flat entry i of the double3 array) */
+void xo_rolling_ex(const device_dem_parameters* prm, double* tmax, double* rres,
+                   const double* inertia, const double* ep, const double* ev,
+                   double* moment, unsigned int np, int per_sphere);
 /* impl:2544-2601 */
 void xo_update_mesh(const double* dbi, const double* vList, double* sphere,
                     const double* dlocal, device_triangle_info* dpi,

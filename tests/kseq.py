@@ -67,7 +67,8 @@ class OracleBackend:
                            g["sorted_index"], g["cstart"], g["cend"], cp, s["np"], ntri)
 
     def rolling(self, s):
-        self.o.rolling(self.prm, s["tmax"], s["rres"], s["inertia"], s["ep"], s["ev"], s["moment"], s["np"])
+        self.o.rolling(self.prm, s["tmax"], s["rres"], s["inertia"], s["ep"], s["ev"], s["moment"], s["np"],
+                       s.get("rolling_per_sphere", 0))
 
     def update_mesh(self, dbi, vlist, sphere, dlocal, dti, ntri):
         self.o.update_mesh(dbi, vlist, sphere, dlocal, dti, ntri)

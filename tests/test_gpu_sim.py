@@ -270,3 +270,28 @@ def test_cylinder_pairs_survive_a_part_file(simmod, tmp_path):
         assert np.array_equal(sa[k], sb[k]), k
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("launcher_path", [0, 1])
+def test_rolling_inertia_per_sphere_matches_oracle(simmod, oracle, launcher_path):
+    """xdem_sim_set_rolling_inertia(1): rolling resistance with each sphere's
+    own inertia (the reference reads the flat entry i of the double3 array,
+    impl:2434) against the oracle with the same switch; and the switch does
+    change the motion."""
+    sc = scene_with_mesh(seed=23, rfric=0.05)
+    sm = simmod.Sim(sc, precision=T.XDEM_FP64, launcher_path=launcher_path)
+    sm.set_rolling_inertia(1)
+    ref = simmod.Sim(sc, precision=T.XDEM_FP64, launcher_path=launcher_path)
+    meshes = oracle_meshes_from_sim(sm, sc)
+    s = kseq.state_arrays(sc)
+    s["rolling_per_sphere"] = 1
+    be = kseq.OracleBackend(oracle)
+    for step in range(5):
+        sm.step(1)
+        ref.step(1)
+        kseq.sphere_step(be, sc, s, meshes, compat=0)
+        compare(sm, s, sc, 1e-11, step)
+    assert sm.status() == 0
+    assert not np.array_equal(sm.state()["ev"], ref.state()["ev"])
+    sm.close()
+    ref.close()

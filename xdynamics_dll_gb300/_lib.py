@@ -29,6 +29,7 @@ _SIGS = {
     "xdem_get_body_force_buffers": ([vp], i32),
     "xdem_last_body_wrench": ([vp], i32),
     "xdem_set_velocity_compat": ([i32], i32),
+    "xdem_set_rolling_inertia": ([i32], i32),
     "setDEMSymbolicParameter": ([vp], i32),
     "vv_update_position": ([vp] * 6 + [u32], i32),
     "vv_update_velocity": ([vp] * 9 + [u32], i32),
@@ -69,6 +70,7 @@ _SIGS = {
     "xdem_sim_set_pairs": ([vp, i32, vp, vp, vp], i32),
     "xdem_sim_energy": ([vp, vp, vp], i32),
     "xdem_sim_status": ([vp], i32),
+    "xdem_sim_set_rolling_inertia": ([vp, i32], i32),
     "xdem_sim_set_stream": ([vp, vp], i32),
     "xdem_sim_set_profiling": ([vp, i32], i32),
     "xdem_sim_set_graph": ([vp, i32], i32),

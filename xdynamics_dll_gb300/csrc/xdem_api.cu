@@ -53,6 +53,7 @@ device_dem_parameters g_params;
 bool g_params_set = false;
 double* g_bf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 int g_vel_compat = 0;
+int g_roll_per_sphere = 0;
 thread_local cudaStream_t t_stream = 0;
 thread_local int t_status = XDEM_OK;
 
@@ -229,6 +230,12 @@ XDEM_API int xdem_last_body_wrench(double out6[6])
 XDEM_API int xdem_set_velocity_compat(int reproduce_reference_gpu)
 {
     g_vel_compat = reproduce_reference_gpu ? 1 : 0;
+    return set_status(XDEM_OK);
+}
+
+XDEM_API int xdem_set_rolling_inertia(int per_sphere)
+{
+    g_roll_per_sphere = per_sphere ? 1 : 0;
     return set_status(XDEM_OK);
 }
 
@@ -412,7 +419,8 @@ XDEM_API int cu_decide_rolling_friction_moment(double* tmax, double* rres, doubl
                                                double* moment, unsigned int np)
 {
     if (int s = need_params()) return set_status(s);
-    return set_status(cuda_status(launch_rolling(g_params, tmax, rres, inertia, ep, ev, moment, np, t_stream)));
+    return set_status(
+        cuda_status(launch_rolling(g_params, tmax, rres, inertia, ep, ev, moment, np, t_stream, g_roll_per_sphere)));
 }
 
 XDEM_API double reduction(double* in, unsigned int np)

@@ -504,7 +504,9 @@ k_fused_contact(const ContactLaunch c)
     // ------------------------------------------------ rolling resistance (impl:2420-2454)
     const double Tr = res;
     if (Tr) {
-        const double J = c.inertia[oid];  // scalar read of the double3 array, as impl:2434
+        // the flat entry oid of the double3 array as impl:2434 reads it, or
+        // the sphere's own (rolling_per_sphere)
+        const double J = c.rolling_per_sphere ? c.inertia[3 * (size_t)oid] : c.inertia[oid];
         const d3 om = mk3(io.x, io.y, io.z);
         const d3 T = (J * p.dt) * om - tma;
         const double lT = length(T);

@@ -185,6 +185,7 @@ struct FusedArgs {
     size_t ncell;
     int sort_bits;
     int vel_compat;
+    int rolling_per_sphere;    // rolling resistance reads inertia[3 i] (else the flat entry i)
     // state: pos/ep are swapped with the alternate buffers by fused_step
     double** pos;
     double** ep;
@@ -257,6 +258,7 @@ struct ContactLaunch {
     MixedTune tune;
     unsigned int np, nentry;
     int vel_compat;
+    int rolling_per_sphere;
     bool rolling;
     const double* snap_pos;
     const double* snap_vel;

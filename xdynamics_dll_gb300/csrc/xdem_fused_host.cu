@@ -727,6 +727,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.np = np;
     c.nentry = n;
     c.vel_compat = a.vel_compat;
+    c.rolling_per_sphere = a.rolling_per_sphere;
     c.rolling = a.rolling;
     c.snap_pos = fs.snap_pos; c.snap_vel = fs.snap_vel; c.snap_om = fs.snap_om; c.snap_f = fs.snap_f;
     c.margin = fs.frame_margin;

@@ -1291,7 +1291,8 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     if (acc.rs != 0.f) {
         need_bc();
         const V3<float> iom = v3<float>(Ci.x, Ci.y, Ci.z);
-        const float J = d2f_rn(c.inertia[oid]);  // scalar read of the double3 array, as impl:2434
+        // the flat entry oid as impl:2434 reads it, or the sphere's own
+        const float J = d2f_rn(c.rolling_per_sphere ? c.inertia[3 * (size_t)oid] : c.inertia[oid]);
         const V3<float> T = (J * c.dt_f) * iom - acc.tm;
         const float lT2 = tdot(T, T);
         const float lT = lT2 == 0.f ? 0.f : sqrtf(lT2);

@@ -668,15 +668,17 @@ k_mesh(device_dem_parameters p, const device_triangle_info* dti, unsigned int lo
 }
 
 // ---------------------------------------------------------------- rolling (impl:2420-2500)
+// per_sphere: J = inertia[3 i], the sphere's own entry, instead of the flat
+// entry i the reference reads (impl:2434)
 __global__ void k_rolling(device_dem_parameters p, double* tmax, double* rres, const double* inertia,
-                          const double* ep, const double* ev, double* moment, unsigned int n)
+                          const double* ep, const double* ev, double* moment, unsigned int n, int per_sphere)
 {
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double Tr = rres[i];
     if (!Tr) return;
     const d3 Tm = ld3(tmax, i);
-    const double J = inertia[i];  // scalar read of the double3 array (impl:2434)
+    const double J = per_sphere ? inertia[3 * (size_t)i] : inertia[i];
     const d3 om = ang_vel(ld4(ep, i), ld4(ev, i));
     const d3 T = (J * p.dt) * om - Tm;
     const double lT = length(T);
@@ -1030,9 +1032,10 @@ cudaError_t launch_mesh(const device_dem_parameters& p, const device_triangle_in
 }
 
 cudaError_t launch_rolling(const device_dem_parameters& p, double* tmax, double* rres, const double* inertia,
-                           const double* ep, const double* ev, double* moment, unsigned int n, cudaStream_t st)
+                           const double* ep, const double* ev, double* moment, unsigned int n, cudaStream_t st,
+                           int per_sphere)
 {
-    XDEM_LAUNCH(k_rolling, n, p, tmax, rres, inertia, ep, ev, moment, n);
+    XDEM_LAUNCH(k_rolling, n, p, tmax, rres, inertia, ep, ev, moment, n, per_sphere);
 }
 
 cudaError_t launch_cluster_rolling(const device_dem_parameters& p, double* tmax, double* rres, const double* inertia,

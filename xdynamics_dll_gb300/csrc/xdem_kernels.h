@@ -63,7 +63,8 @@ cudaError_t launch_mesh(const device_dem_parameters& p, const device_triangle_in
                         const xClusterInformation* xci, unsigned int n, unsigned int ntri, unsigned int* status,
                         cudaStream_t st);
 cudaError_t launch_rolling(const device_dem_parameters& p, double* tmax, double* rres, const double* inertia,
-                           const double* ep, const double* ev, double* moment, unsigned int n, cudaStream_t st);
+                           const double* ep, const double* ev, double* moment, unsigned int n, cudaStream_t st,
+                           int per_sphere = 0);
 cudaError_t launch_update_mesh(const double* dbi, const double* vlist, double* sphere, const double* dlocal,
                                device_triangle_info* dpi, unsigned int ntri, cudaStream_t st);
 cudaError_t launch_clusters_p2p(const device_dem_parameters& p, const double* pos, const double* cpos,

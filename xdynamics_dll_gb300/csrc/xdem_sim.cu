@@ -289,7 +289,7 @@ int step_launcher(xdem_sim* s, cudaEvent_t e0, cudaEvent_t e1)
     if (s->clusters)
         ok(launch_cluster_rolling(p, s->tmax, s->rres, s->inertia, s->ep, s->ev, s->moment, s->xci, n, st));
     else
-        ok(launch_rolling(p, s->tmax, s->rres, s->inertia, s->ep, s->ev, s->moment, n, st));
+        ok(launch_rolling(p, s->tmax, s->rres, s->inertia, s->ep, s->ev, s->moment, n, st, s->rolling_per_sphere));
     if (s->clusters)
         ok(launch_vv_cluster_velocity(p, s->vel, s->acc, s->ep, s->ev, s->ea, s->force, s->moment, s->mass,
                                       s->inertia, s->xci, s->ns, st));
@@ -365,6 +365,7 @@ FusedArgs fused_args(xdem_sim* s)
     a.ncell = s->ncell;
     a.sort_bits = bits_for(s->ncell);
     a.vel_compat = s->cfg.velocity_compat;
+    a.rolling_per_sphere = s->rolling_per_sphere;
     a.pos = &s->pos; a.vel = s->vel; a.acc = s->acc; a.ep = &s->ep; a.ev = s->ev; a.ea = s->ea;
     a.mass = s->mass; a.inertia = s->inertia; a.tmax = s->tmax; a.rres = s->rres;
     a.k0 = s->k0; a.v0 = s->v0; a.k1 = s->k1; a.v1 = s->v1; a.hist = s->hist;
@@ -588,6 +589,14 @@ XDEM_API int xdem_sim_destroy(xdem_sim* s)
     // a stream given by xdem_sim_set_stream belongs to the caller
     if (s->own_st) cudaStreamDestroy(s->own_st);
     delete s;
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_set_rolling_inertia(xdem_sim* s, int per_sphere)
+{
+    if (!s) return XDEM_ERR_ARG;
+    s->rolling_per_sphere = per_sphere ? 1 : 0;
+    s->dirty_bodies = true;  // captured step graphs bake the switch in
     return XDEM_OK;
 }
 

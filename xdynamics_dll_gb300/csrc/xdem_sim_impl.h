@@ -37,6 +37,7 @@ struct xdem_sim {
     cudaStream_t own_st = 0;   // created with the handle; the only stream destroy releases
     unsigned int np = 0, ns = 0, nco = 0, nrloc = 0;
     bool clusters = false;
+    int rolling_per_sphere = 0;  // xdem_sim_set_rolling_inertia
     unsigned int status_host = 0;
     // state (reference layout)
     double *pos = nullptr, *cpos = nullptr, *vel = nullptr, *acc = nullptr, *ep = nullptr, *ev = nullptr,

@@ -155,6 +155,11 @@ class Sim:
     def set_profiling(self, on):
         self.L.xdem_sim_set_profiling(self.h, int(on))
 
+    def set_rolling_inertia(self, per_sphere):
+        """1: rolling resistance reads each sphere's own inertia (inertia[3 i]);
+        0 (default): the flat entry i, as the reference kernel does."""
+        _lib.check(self.L.xdem_sim_set_rolling_inertia(self.h, int(per_sphere)), "xdem_sim_set_rolling_inertia")
+
     def set_graph(self, on):
         """Replay the step from a captured CUDA graph (identical results)."""
         _lib.check(self.L.xdem_sim_set_graph(self.h, int(on)), "xdem_sim_set_graph")
