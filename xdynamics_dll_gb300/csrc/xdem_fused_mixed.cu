@@ -468,11 +468,15 @@ __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oi
     cp_async_commit();
     const unsigned int n = c.vl_cnt[oid];
     const unsigned int* ids = c.vl_ids + (size_t)oid * kListCap;
+    // the first four candidates come with the count (a row is 96 bytes, so
+    // 16-byte aligned), not after it: their records' loads start a round
+    // trip earlier
+    const uint4 head = reinterpret_cast<const uint4*>(ids)[0];
     // (cell offset key, id) of the candidates inside this step's stencil
     unsigned long long key[kListCap];
     unsigned int nk = 0;
     for (unsigned int q = 0; q < n; ++q) {
-        const unsigned int k = ids[q];
+        const unsigned int k = q == 0 ? head.x : q == 1 ? head.y : q == 2 ? head.z : q == 3 ? head.w : ids[q];
         if (c.scene_of && c.scene_of[k] != scene) continue;  // another scene of the batch
         const unsigned int Tk = rec_cell(c.rec[4 * (size_t)k + kRecC]);
         const unsigned int xs = (Tk - ux + 1u) & 2047u;
