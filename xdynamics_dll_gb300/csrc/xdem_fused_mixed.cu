@@ -717,19 +717,51 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
                 // a cell's entries are in ascending id (stable sort of an
                 // id-ordered input): this mesh's spheres, ids lo .. lo + ntri
                 // - 1, follow every particle; later meshes follow them
+                // both scans take four entries a step, their loads issued
+                // together, so a sphere's walk is a quarter as many
+                // dependent loads long
                 unsigned int jm = end;
-                while (jm > start && c.sorted_index[jm - 1] >= lo) --jm;
-                for (unsigned int j = jm; j < end; ++j) {
-                    unsigned int tk = c.sorted_index[j];
-                    if (tk >= lo + ntri) break;
-                    tk -= lo;
-                    if (!mr.coh) {
-                        const double2 q0 = reinterpret_cast<const double2*>(sph)[2 * tk];
-                        const double2 q1 = reinterpret_cast<const double2*>(sph)[2 * tk + 1];
-                        const float dx = d2f_rn(q0.x) - xf, dy = d2f_rn(q0.y) - yf, dz = d2f_rn(q1.x) - zf;
-                        const float lim = d2f_rn(q1.y) + rf + 1e-5f;
-                        if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+                while (jm > start) {
+                    const unsigned int n4 = umin(4u, jm - start);
+                    unsigned int sk[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) sk[q] = (unsigned int)q < n4 ? c.sorted_index[jm - 1 - q] : 0u;
+                    unsigned int k = 0;
+                    while (k < n4 && sk[k] >= lo) ++k;
+                    jm -= k;
+                    if (k < n4) break;
+                }
+                for (unsigned int j0 = jm; j0 < end; j0 += 4) {
+                    unsigned int tks[4];
+                    unsigned int take4 = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        tks[q] = j0 + q < end ? c.sorted_index[j0 + q] - lo : 0xffffffffu;
+                        if (tks[q] < ntri) take4 |= 1u << q;
                     }
+                    // ids ascend within the cell: a later mesh's entry ends this one's
+                    const bool last = take4 != 0xfu;
+                    if (!mr.coh) {
+                        float4 fs[4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            fs[q] = make_float4(0.f, 0.f, 0.f, -1.f);
+                            if (take4 >> q & 1u) {
+                                const double2 q0 = reinterpret_cast<const double2*>(sph)[2 * tks[q]];
+                                const double2 q1 = reinterpret_cast<const double2*>(sph)[2 * tks[q] + 1];
+                                fs[q] = make_float4(d2f_rn(q0.x), d2f_rn(q0.y), d2f_rn(q1.x), d2f_rn(q1.y));
+                            }
+                        }
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float dx = fs[q].x - xf, dy = fs[q].y - yf, dz = fs[q].z - zf;
+                            const float lim = fs[q].w + rf + 1e-5f;
+                            if (dx * dx + dy * dy + dz * dz > lim * lim) take4 &= ~(1u << q);
+                        }
+                    }
+                    for (int q = 0; q < 4; ++q) {
+                    if (!(take4 >> q & 1u)) continue;
+                    const unsigned int tk = tks[q];
                     int t = -1;
                     const d3 cpt = closest_pt_triangle(c.tri[c.mesh_first[m] + tk], ipos, t);
                     const double cd = ir - length(ipos - cpt);
@@ -751,6 +783,8 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
                     if (t == 2) { if (nf < XDEM_MAX_TRI_CANDIDATES) hf[nf++] = hit; else bits |= XDEM_ERR_TRI_CANDIDATES; }
                     else if (t == 1) { if (nl < XDEM_MAX_TRI_CANDIDATES) hl[nl++] = hit; else bits |= XDEM_ERR_TRI_CANDIDATES; }
                     else if (t == 0) { if (npt < XDEM_MAX_TRI_CANDIDATES) hp[npt++] = hit; else bits |= XDEM_ERR_TRI_CANDIDATES; }
+                    }
+                    if (last) break;
                 }
             }
     const Hit* list = nf ? hf : (nl ? hl : hp);
