@@ -259,25 +259,25 @@ def bench_e2e(sm, scene, torch, steps):
     """Same metric through the C-ABI with host buffers: each step uploads
     every body's 15-double pose record and plane frame from pinned host memory
     (xParticlePlaneContact::update does two such copies per plane per step)
-    and reads back every body's 6-double wrench (the MBD exchange)."""
+    and reads back every body's 6-double wrench (the MBD exchange), all
+    bodies in one xdem_sim_set_bodies and one xdem_sim_body_wrenches call."""
     import ctypes as C
+    from xdynamics_dll_gb300 import _lib, types as T
     nb = len(sm.bodies)
     rec = torch.zeros((nb, 15), dtype=torch.float64).pin_memory()
     for b in range(nb):
         rec[b] = torch.from_numpy(np.asarray(scene.plane_body[b], dtype=np.float64))
     wr = torch.zeros((nb, 6), dtype=torch.float64).pin_memory()
-    planes = scene.planes
+    idx = (C.c_int * nb)(*sm.bodies)
+    planes = (T.PlaneInfo * nb)(*scene.planes[:nb])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        for b in range(nb):
-            sm.L.xdem_sim_set_body(sm.h, sm.bodies[b], C.c_void_p(rec[b].data_ptr()), C.byref(planes[b]))
+        _lib.check(sm.L.xdem_sim_set_bodies(sm.h, nb, idx, C.c_void_p(rec.data_ptr()), planes), "xdem_sim_set_bodies")
         sm.step(1)
-        for b in range(nb):
-            sm.L.xdem_sim_body_wrench(sm.h, sm.bodies[b], C.c_void_p(wr[b].data_ptr()))
+        _lib.check(sm.L.xdem_sim_body_wrenches(sm.h, nb, idx, C.c_void_p(wr.data_ptr())), "xdem_sim_body_wrenches")
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    from xdynamics_dll_gb300 import types as T
     h2d = nb * (15 * 8 + C.sizeof(T.PlaneInfo))
     return {"value": scene.np_ * steps / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": nb * 48,
             "steps": steps}
@@ -409,7 +409,7 @@ def bench_wheel(args, torch, local):
     triangles) and the planes from host records and reads every body's
     wrench back, the host moving the wheel from its wrench."""
     import ctypes as C
-    from xdynamics_dll_gb300 import scenes, sim as S, types as T
+    from xdynamics_dll_gb300 import _lib, scenes, sim as S, types as T
 
     def stage(msg):
         sys.stderr.write(f"[wheel] {msg}\n")
@@ -460,6 +460,10 @@ def bench_wheel(args, torch, local):
     for b in range(nb):
         rec[b] = torch.from_numpy(recs[b])
     wr = torch.zeros((nb, 6), dtype=torch.float64).pin_memory()
+    # every body's pose and frame in one call, every wrench in one call (the
+    # tyre's frame entry is not read)
+    idx = (C.c_int * nb)(*sm.bodies)
+    pl_arr = (T.PlaneInfo * nb)(*(list(sc.planes) + [T.PlaneInfo()] * (nb - len(sc.planes))))
     omega = -2.0 * float(recs[-1][14])
     m_w = float(recs[-1][0])
     # the held wheel's first contact pushed the top layer down: the exchange
@@ -474,12 +478,10 @@ def bench_wheel(args, torch, local):
         rec[nb - 1, 10] = float(np.sin(0.5 * th))
         rec[nb - 1, 2] = y_w
         rec[nb - 1, 5] = vy_w
-        for b in range(nb):
-            pl = C.byref(sc.planes[b]) if b < len(sc.planes) else None
-            sm.L.xdem_sim_set_body(sm.h, sm.bodies[b], C.c_void_p(rec[b].data_ptr()), pl)
+        _lib.check(sm.L.xdem_sim_set_bodies(sm.h, nb, idx, C.c_void_p(rec.data_ptr()), pl_arr),
+                   "xdem_sim_set_bodies")
         sm.step(1)
-        for b in range(nb):
-            sm.L.xdem_sim_body_wrench(sm.h, sm.bodies[b], C.c_void_p(wr[b].data_ptr()))
+        _lib.check(sm.L.xdem_sim_body_wrenches(sm.h, nb, idx, C.c_void_p(wr.data_ptr())), "xdem_sim_body_wrenches")
         fy = float(wr[nb - 1, 1])
         fy_sum += fy
         vy_w += sc.dt * (fy / m_w + sc.gravity[1])

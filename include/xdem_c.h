@@ -445,6 +445,23 @@ XDEM_API int xdem_sim_step(xdem_sim* sim, unsigned int nsteps);
 /* Wrench of the last step on a body: (fx,fy,fz,mx,my,mz).  Synchronises. */
 XDEM_API int xdem_sim_body_wrench(xdem_sim* sim, int body_index,
                                   double out6[6]);
+/* The same exchange for several bodies in one call each way.  The reference
+ * exchanges body by body: xParticlePlaneContact::update and
+ * xParticleMeshObjectContact::update copy each pose in
+ * (xParticlePlaneContact.cpp:96-131, xParticleMeshObjectContact.cpp:169-184)
+ * and `reduction` + xPointMass::addContactForce read each wrench back
+ * (decl:285-317, xPointMass.cpp:159-168).
+ * xdem_sim_set_bodies: bodies is count x 15 doubles, planes count entries
+ * (read for plane bodies; NULL keeps every frame).  Results equal count
+ * xdem_sim_set_body calls in list order; the body records and plane tables
+ * go up in one copy each from pinned staging, and the call does not wait
+ * for the copies.  xdem_sim_body_wrenches: out is count x 6 doubles, from one
+ * device-to-host copy of every body's wrench; synchronises. */
+XDEM_API int xdem_sim_set_bodies(xdem_sim* sim, int count,
+                                 const int* body_index, const double* bodies,
+                                 const device_plane_info* planes);
+XDEM_API int xdem_sim_body_wrenches(xdem_sim* sim, int count,
+                                    const int* body_index, double* out);
 /* Copies the state back to host arrays (reference layout); NULL skips. */
 XDEM_API int xdem_sim_get_state(xdem_sim* sim, double* pos, double* vel,
                                 double* acc, double* ep, double* ev,

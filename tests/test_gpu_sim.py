@@ -295,3 +295,58 @@ def test_rolling_inertia_per_sphere_matches_oracle(simmod, oracle, launcher_path
     assert not np.array_equal(sm.state()["ev"], ref.state()["ev"])
     sm.close()
     ref.close()
+
+
+@pytest.mark.parametrize("precision", [T.XDEM_FP64, T.XDEM_MIXED])
+def test_batched_body_exchange_matches_per_body_calls(simmod, precision):
+    """xdem_sim_set_bodies / xdem_sim_body_wrenches against one
+    xdem_sim_set_body / xdem_sim_body_wrench call per body: five planes (their
+    records given a sliding velocity, their frames re-sent) and a mesh pushed
+    through the bed, re-posed every step; states and wrenches bit for bit."""
+    sc = scene_with_mesh(seed=12)
+    nb = len(sc.planes) + 1
+    out = []
+    for batched in (False, True):
+        sm = simmod.Sim(sc, precision=precision)
+        assert len(sm.bodies) == nb
+        recs = np.array([np.asarray(r, dtype=np.float64) for r in sc.plane_body] +
+                        [np.asarray(sc.meshes[0]["body"], dtype=np.float64)])
+        walls = []
+        for step in range(12):
+            recs[:len(sc.planes), 4] = 0.01 * (step + 1)  # the planes slide along x
+            recs[-1, 2] += 0.02 * sc.dt                   # the mesh moves along y
+            if batched:
+                sm.set_bodies(sm.bodies, recs, list(sc.planes) + [T.PlaneInfo()])
+            else:
+                for b in range(nb):
+                    sm.set_body(sm.bodies[b], recs[b], sc.planes[b] if b < len(sc.planes) else None)
+            sm.step(1)
+            if batched:
+                w = sm.wrenches(sm.bodies)
+            else:
+                w = np.array([sm.wrench(sm.bodies[b]) for b in range(nb)])
+            walls.append(w)
+        assert sm.status() == 0
+        out.append((sm.state(), np.array(walls), [sm.pairs(k) for k in (0, 1, 2)]))
+        sm.close()
+    (sa, wa, pa), (sb, wb, pb) = out
+    for k in ("pos", "vel", "acc", "ep", "ev", "ea"):
+        assert np.array_equal(sa[k], sb[k]), k
+    assert np.array_equal(wa, wb)
+    assert np.abs(wa).max() > 0
+    for x, y in zip(pa, pb):
+        for u, v in zip(x, y):
+            assert np.array_equal(u, v)
+
+
+def test_batched_body_exchange_checks_its_arguments(simmod):
+    sc = scene_with_mesh(n=500, seed=3)
+    sm = simmod.Sim(sc, precision=T.XDEM_MIXED)
+    with pytest.raises(Exception):
+        sm.set_bodies([len(sm.bodies)], np.zeros((1, 15)))
+    sm.step(1)
+    assert sm.wrenches([]).shape == (0, 6)
+    w = sm.wrenches([sm.bodies[-1], sm.bodies[0]])
+    assert np.array_equal(w[0], sm.wrench(sm.bodies[-1]))
+    assert np.array_equal(w[1], sm.wrench(sm.bodies[0]))
+    sm.close()

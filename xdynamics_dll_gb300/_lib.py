@@ -65,6 +65,8 @@ _SIGS = {
     "xdem_sim_set_body": ([vp, i32, vp, vp], i32),
     "xdem_sim_step": ([vp, u32], i32),
     "xdem_sim_body_wrench": ([vp, i32, vp], i32),
+    "xdem_sim_set_bodies": ([vp, i32, vp, vp, vp], i32),
+    "xdem_sim_body_wrenches": ([vp, i32, vp, vp], i32),
     "xdem_sim_get_state": ([vp] * 8, i32),
     "xdem_sim_get_pairs": ([vp, i32, vp, vp, vp], i32),
     "xdem_sim_set_pairs": ([vp, i32, vp, vp, vp], i32),

@@ -235,6 +235,10 @@ int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& 
                        cudaStream_t st);
 // Bounding sphere of mesh m (centre relative to the grid origin, radius;
 // a radius of 1e18 searches every sphere): refreshed on the stream.
+// Host copies of plane k's FP32 and float-pair tables (fs.h_planef,
+// fs.h_planedf) from its frame, without the upload; false when the tables
+// do not exist yet.
+bool fused_plane_tables_host(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh);
 int fused_set_mesh_bounds(FusedState& fs, unsigned int m, float4 b, cudaStream_t st);
 // The next step sorts the cell table even when the candidate lists hold
 // (a mesh moved: its spheres' cells changed).

@@ -548,6 +548,13 @@ int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned i
     return e == cudaSuccess ? XDEM_OK : XDEM_ERR_CUDA;
 }
 
+bool fused_plane_tables_host(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh)
+{
+    if (k >= fs.nplane || !fs.d_planef || !fs.d_planedf) return false;
+    plane_tables(host_plane, fs.origin, coh, fs.h_planef[k], fs.h_planedf[k]);
+    return true;
+}
+
 int fused_update_plane(FusedState& fs, unsigned int k, const device_plane_info& host_plane, bool coh,
                        cudaStream_t st)
 {

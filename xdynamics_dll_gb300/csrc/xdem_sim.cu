@@ -582,6 +582,8 @@ XDEM_API int xdem_sim_destroy(xdem_sim* s)
     if (s->d_tri) cudaFree(s->d_tri);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->pin_ev) cudaEventDestroy(s->pin_ev);
+    if (s->h_pin) cudaFreeHost(s->h_pin);
     for (int i = 0; i < xdem_sim::kProfEvents; ++i) {
         if (s->pe0[i]) cudaEventDestroy(s->pe0[i]);
         if (s->pe1[i]) cudaEventDestroy(s->pe1[i]);
@@ -866,6 +868,107 @@ XDEM_API int xdem_sim_set_body(xdem_sim* s, int body_index, const double body[15
     // the pinned-free host record must stay valid until the copy ran
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     return cerr(e);
+}
+
+// Pinned staging of at least `bytes`, with the last upload from it finished.
+static int pin_stage(xdem_sim* s, size_t bytes, char** out)
+{
+    if (!s->pin_ev) {
+        if (cudaEventCreateWithFlags(&s->pin_ev, cudaEventDisableTiming) != cudaSuccess) return XDEM_ERR_CUDA;
+    } else if (cudaEventSynchronize(s->pin_ev) != cudaSuccess) {
+        return XDEM_ERR_CUDA;
+    }
+    if (bytes > s->h_pin_cap) {
+        if (s->h_pin) cudaFreeHost(s->h_pin);
+        s->h_pin = nullptr;
+        s->h_pin_cap = 0;
+        if (cudaHostAlloc(&s->h_pin, bytes, cudaHostAllocDefault) != cudaSuccess) return XDEM_ERR_ALLOC;
+        s->h_pin_cap = bytes;
+    }
+    *out = static_cast<char*>(s->h_pin);
+    return XDEM_OK;
+}
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+XDEM_API int xdem_sim_set_bodies(xdem_sim* s, int count, const int* body_index, const double* bodies,
+                                 const device_plane_info* planes)
+{
+    if (!s || count < 0 || (count > 0 && (!body_index || !bodies))) return XDEM_ERR_ARG;
+    const int nb = (int)s->bodies.size();
+    for (int q = 0; q < count; ++q)
+        if (body_index[q] < 0 || body_index[q] >= nb) return XDEM_ERR_ARG;
+    if (count == 0) return XDEM_OK;
+    if (int r = upload_bodies(s)) return r;
+    // the host mirrors in list order (a body listed twice keeps its last entry)
+    bool moved_plane = false, tables = false;
+    for (int q = 0; q < count; ++q) {
+        SimBody& b = s->bodies[body_index[q]];
+        std::memcpy(b.rec, bodies + 15 * (size_t)q, sizeof(b.rec));
+        if (b.kind == 0 && planes) {
+            device_plane_info pl = planes[q];
+            pl.id = s->planes[b.index].id;
+            s->planes[b.index] = pl;
+            moved_plane = true;
+            tables |= fused_plane_tables_host(s->fs, (unsigned int)b.index, pl, s->body_cp[body_index[q]].coh != 0.0);
+        }
+    }
+    // then every record, and every plane's frame and tables if one moved,
+    // in one copy per array
+    const size_t npl = s->planes.size(), nft = tables ? s->fs.nplane : 0;
+    const size_t ob = 0, op = align16(ob + (size_t)nb * 15 * sizeof(double));
+    const size_t of = align16(op + (moved_plane ? npl * sizeof(device_plane_info) : 0));
+    const size_t od = align16(of + nft * sizeof(PlaneF));
+    const size_t end = od + nft * sizeof(PlaneDF);
+    char* h = nullptr;
+    if (int r = pin_stage(s, end, &h)) return r;
+    for (int i = 0; i < nb; ++i) std::memcpy(h + ob + (size_t)i * 15 * sizeof(double), s->bodies[i].rec, 15 * sizeof(double));
+    cudaError_t e = cudaMemcpyAsync(s->d_body, h + ob, (size_t)nb * 15 * sizeof(double), cudaMemcpyHostToDevice, s->st);
+    if (moved_plane && npl) {
+        std::memcpy(h + op, s->planes.data(), npl * sizeof(device_plane_info));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d_planes, h + op, npl * sizeof(device_plane_info), cudaMemcpyHostToDevice, s->st);
+    }
+    if (nft) {
+        std::memcpy(h + of, s->fs.h_planef.data(), nft * sizeof(PlaneF));
+        std::memcpy(h + od, s->fs.h_planedf.data(), nft * sizeof(PlaneDF));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->fs.d_planef, h + of, nft * sizeof(PlaneF), cudaMemcpyHostToDevice, s->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->fs.d_planedf, h + od, nft * sizeof(PlaneDF), cudaMemcpyHostToDevice, s->st);
+    }
+    // meshes follow their records as in xdem_sim_set_body
+    for (int q = 0; q < count && e == cudaSuccess; ++q) {
+        const int bi = body_index[q];
+        const SimBody& b = s->bodies[bi];
+        if (b.kind != 1) continue;
+        const SimMesh& m = s->meshes[b.index];
+        e = launch_update_mesh(s->d_body + 15 * bi, s->d_vlist + 9 * (size_t)m.first, s->d_sphere + 4 * (size_t)m.first,
+                               s->d_dlocal + 3 * (size_t)m.first, s->d_tri + m.first, m.ntri, s->st);
+        if (e == cudaSuccess && fused_force_sort(s->fs, s->st) != XDEM_OK) e = cudaErrorUnknown;
+        if (e == cudaSuccess && push_mesh_bounds(s, b.index) != XDEM_OK) e = cudaErrorUnknown;
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(s->pin_ev, s->st);
+    return cerr(e);
+}
+
+XDEM_API int xdem_sim_body_wrenches(xdem_sim* s, int count, const int* body_index, double* out)
+{
+    if (!s || count < 0 || (count > 0 && (!body_index || !out))) return XDEM_ERR_ARG;
+    if (s->nscene > 1) return XDEM_ERR_ARG;  // batched handles keep no body wrenches
+    const int nb = (int)s->bodies.size();
+    for (int q = 0; q < count; ++q)
+        if (body_index[q] < 0 || body_index[q] >= nb) return XDEM_ERR_ARG;
+    if (count == 0) return XDEM_OK;
+    if (!s->wrench || s->dirty_alloc) return XDEM_ERR_ARG;  // no step has run on this body set
+    char* h = nullptr;
+    if (int r = pin_stage(s, (size_t)nb * 6 * sizeof(double), &h)) return r;
+    cudaError_t e = cudaMemcpyAsync(h, s->wrench, (size_t)nb * 6 * sizeof(double), cudaMemcpyDeviceToHost, s->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return cerr(e);
+    for (int q = 0; q < count; ++q)
+        std::memcpy(out + 6 * (size_t)q, h + (size_t)body_index[q] * 6 * sizeof(double), 6 * sizeof(double));
+    return XDEM_OK;
 }
 
 XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)

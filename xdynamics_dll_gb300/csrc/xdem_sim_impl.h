@@ -80,6 +80,9 @@ struct xdem_sim {
     double *d_vlist = nullptr, *d_dlocal = nullptr, *d_sphere = nullptr;
     double* bsums = nullptr;       // per body: nblocks * 6
     double* wrench = nullptr;      // per body: 6
+    void* h_pin = nullptr;         // pinned staging of the batched body exchange
+    size_t h_pin_cap = 0;
+    cudaEvent_t pin_ev = nullptr;  // the last upload from h_pin
     unsigned int* d_status = nullptr;
     bool dirty_bodies = true;      // device body tables need upload
     bool dirty_alloc = true;       // contact tables need (re)allocation

@@ -132,6 +132,27 @@ class Sim:
         _lib.check(self.L.xdem_sim_set_body(self.h, body, _p(rec), C.byref(plane) if plane is not None else None),
                    "xdem_sim_set_body")
 
+    def set_bodies(self, bodies, recs, planes=None):
+        """Several poses in one call (xdem_sim_set_bodies): recs is
+        len(bodies) x 15; planes a sequence of PlaneInfo, one per entry (read
+        for plane bodies), or None."""
+        idx = np.ascontiguousarray(bodies, dtype=np.int32)
+        recs = np.ascontiguousarray(recs, dtype=np.float64).reshape(len(idx), 15)
+        pl = None
+        if planes is not None:
+            pl = (T.PlaneInfo * len(idx))(*planes)
+        _lib.check(self.L.xdem_sim_set_bodies(self.h, len(idx), idx.ctypes.data_as(C.c_void_p), _p(recs),
+                                              C.cast(pl, C.c_void_p) if pl is not None else None),
+                   "xdem_sim_set_bodies")
+
+    def wrenches(self, bodies):
+        """Wrenches of several bodies from one copy (xdem_sim_body_wrenches)."""
+        idx = np.ascontiguousarray(bodies, dtype=np.int32)
+        out = np.zeros((len(idx), 6))
+        _lib.check(self.L.xdem_sim_body_wrenches(self.h, len(idx), idx.ctypes.data_as(C.c_void_p), _p(out)),
+                   "xdem_sim_body_wrenches")
+        return out
+
     def energy(self):
         ke = C.c_double()
         nc = C.c_uint()
