@@ -77,3 +77,10 @@ def test_argument_checks_need_no_gpu(L):
         cfg.grid_size[i] = 16
     h = C.c_void_p()
     assert L.xdem_sim_create(C.byref(cfg), C.byref(h)) == T.XDEM_ERR_ARG
+    # an empty scene is refused the same way
+    cfg.np, cfg.ns, cfg.precision = 0, 0, T.XDEM_FP64
+    assert L.xdem_sim_create(C.byref(cfg), C.byref(h)) == T.XDEM_ERR_ARG
+    # the batched body exchange checks its handle and lists first
+    idx = (C.c_int * 1)(0)
+    assert L.xdem_sim_set_bodies(None, 1, idx, None, None) == T.XDEM_ERR_ARG
+    assert L.xdem_sim_body_wrenches(None, 1, idx, None) == T.XDEM_ERR_ARG
