@@ -183,16 +183,18 @@ def new_sim(scene, precision):
     return sm
 
 
-def run_cpu_baseline(scene, budget_s=15.0, max_steps=400):
+def run_cpu_baseline(scene, budget_s=15.0, max_steps=400, warmup=1):
     """The CPU oracle (plain C restatement of the reference kernels, OpenMP
     over particles) on a bounded sample of the same workload: the full scene
-    for as many steps as fit in `budget_s` seconds after one warm-up step."""
+    for as many steps as fit in `budget_s` seconds after `warmup` untimed
+    steps."""
     import kseq
     import pyoracle
     o = pyoracle.Oracle()
     be = kseq.OracleBackend(o)
     s = kseq.state_arrays(scene)
-    kseq.sphere_step(be, scene, s, (), compat=0)
+    for _ in range(warmup):
+        kseq.sphere_step(be, scene, s, (), compat=0)
     t0 = time.perf_counter()
     steps = 0
     while steps < max_steps:
@@ -202,7 +204,7 @@ def run_cpu_baseline(scene, budget_s=15.0, max_steps=400):
             break
     dt = time.perf_counter() - t0
     return {"value": scene.np_ * steps / dt, "unit": UNIT, "cores": o.threads(), "kind": "port",
-            "sample": f"{steps} steps of the full {scene.np_}-sphere scene after 1 warm-up step "
+            "sample": f"{steps} steps of the full {scene.np_}-sphere scene after {warmup} warm-up step(s) "
                       f"({dt:.1f} s, oracle/xdem_oracle.c, OpenMP)"}
 
 
@@ -614,13 +616,15 @@ def main():
         # the reference's own CPU DEM path does not work (plane detection is
         # stubbed, every pair is applied to every particle); its GPU kernels
         # restated in C (the oracle) run on the host cores instead
-        cb = run_cpu_baseline(scene, budget_s=min(60.0, 5.0 + 0.5 * args.steps), max_steps=max(args.steps, 1))
+        cb = run_cpu_baseline(scene, budget_s=min(60.0, 5.0 + 0.5 * args.steps), max_steps=max(args.steps, 1),
+                              warmup=warmup)
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0,
-            "steps": args.steps, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * scene.np_ / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"dam break, {scene.np_} polydisperse spheres r~U[1,2] mm, dt=5e-6 s",
-                       "precision": "f64", "grid": list(scene.grid)},
+            "config": {"workload": f"dam break, {scene.np_} polydisperse spheres r~U[1,2] mm, dt=5e-6 s, 5 planes",
+                       "precision": "f64", "grid": list(scene.grid), "cell_size": scene.cell_size},
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}))
         return
