@@ -2,8 +2,12 @@
 
 Workload (the dam-break configuration): 1,000,000 spheres, radii U[1, 2] mm,
 rho 2500, E 1e7, nu 0.3, restitution 0.3, friction 0.4, Hertz-Mindlin,
-dt 5e-6 s, a block at one end of a 1 x 0.4 m box (floor + 4 walls; the gate
-plane is removed at t = 0), seeded jittered-lattice packing (synthetic data).
+dt 5e-6 s.  A seeded random packing fills x in [0, 0.2] m of a 1 x 0.4 x 0.4 m
+box (floor + 4 walls); the gate plane at x = 0.2 m is removed at t = 0.  The
+packing is made by an untimed, seeded settling pre-run on the GPU (an FCC
+fill of the same spheres falls and comes to rest behind the gate, 40,000
+steps of 1e-5 s) and kept as a part file; both arms load that file
+(synthetic data).
 
 A step is one pass of the whole DEM step over all spheres (position update,
 hash, sort, contact, velocity update).  `value` is the mixed-precision path
@@ -55,21 +59,21 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_dambreak_1M.json")
+
+
 def profile_traffic():
-    """DRAM bytes per sphere of the contact kernel from the committed ncu
-    summary (profiles/*contact*.md, line 'dram_bytes_per_sphere_mixed: X')."""
-    pdir = os.path.join(ROOT, "profiles")
-    if not os.path.isdir(pdir):
+    """DRAM bytes (read + write) per sphere of the mixed contact stage on a
+    list step, from the machine-readable summary of ncu captures
+    (profiles/traffic_dambreak_1M.json: per kernel dram__bytes_read.sum +
+    dram__bytes_write.sum of one launch, the sphere count captured, and the
+    command).  Returns (bytes per sphere, source description) or
+    (None, None) when no capture summary is present."""
+    if not os.path.exists(TRAFFIC_FILE):
         return None, None
-    for f in sorted(os.listdir(pdir)):
-        if "contact" in f and f.endswith(".md"):
-            for line in open(os.path.join(pdir, f)):
-                if line.strip().startswith("dram_bytes_per_sphere_mixed:"):
-                    try:
-                        return float(line.split(":")[1].split()[0]), f
-                    except ValueError:
-                        pass
-    return None, None
+    d = json.load(open(TRAFFIC_FILE))
+    per = sum(k["dram_bytes"] for k in d["kernels"]) / float(d["spheres"])
+    return per, f"{os.path.basename(TRAFFIC_FILE)} ({d.get('capture', '')})"
 
 
 class ClockSampler:
@@ -144,35 +148,28 @@ def replica_totals(secs64, secsx, secs_e2e_per_unit, ws, n, steps, device):
     return (ws * n * steps / secsx, ws * n * steps / secs64, ws / secs_e2e_per_unit, secs64, secsx)
 
 
+def log(msg):
+    sys.stderr.write(f"[bench] {msg}\n")
+    sys.stderr.flush()
+
+
 def make_scene(n):
+    """The dam break from the settled random packing (the settling pre-run
+    runs once per box and is cached as a part file)."""
     from xdynamics_dll_gb300 import scenes
-    return scenes.dam_break(n_target=n)
+    t0 = time.perf_counter()
+    sc = scenes.dam_break_packed(n=n, log=log)
+    log(f"scene ready in {time.perf_counter() - t0:.1f} s: {sc.note}")
+    return sc
 
 
-def settle(scene, steps, torch):
-    """Untimed, deterministic pre-run: the block settles under gravity behind
-    a gate plane at x = 0.2 m (the dam), then the gate is removed (t = 0 of
-    the dam break).  Returns the scene with the settled state and the pair
-    lists (tangential history) to carry over."""
-    from xdynamics_dll_gb300 import scenes, sim as S, types as T
-    sc = scene.copy()
-    p = sc.pos.reshape(-1, 4)
-    gate_x = float(p[:, 0].max() + p[:, 3].max() + 1e-4)
-    top = float(p[:, 1].max() + 0.01)
-    gate = T.plane_from_points(len(sc.planes), (gate_x, 0.0, 0.0), (gate_x, 0.0, 0.4), (gate_x, top, 0.0))
-    sc.planes = list(sc.planes) + [gate]
-    sc.plane_cp = list(sc.plane_cp) + [sc.plane_cp[0]]
-    sc.plane_body = list(sc.plane_body) + [T.body_record()]
-    sm = S.Sim(sc, precision=T.XDEM_MIXED)
-    sm.step(steps)
-    st = sm.state()
-    pairs = [sm.pairs(k) for k in range(3)]
-    sm.close()
-    out = scene.copy()
-    for k in ("pos", "vel", "acc", "ep", "ev", "ea"):
-        setattr(out, k, st[k])
-    out.pairs = pairs
-    return out
+def workload_config(scene):
+    """The `config` object both arms print (same keys, same values)."""
+    return {"workload": f"dam break, {scene.np_} polydisperse spheres r~U[1,2] mm, seeded random packing "
+                        f"settled behind the gate, gate removed at t=0, dt=5e-6 s, 5 planes",
+            "grid": list(scene.grid), "cell_size": scene.cell_size,
+            "packing": "FCC fill settled 40,000 x 1e-5 s on the GPU (untimed), part file loaded by both arms",
+            "l2": "inputs larger than L2 (about 0.5 GB of state), no flush"}
 
 
 def new_sim(scene, precision):
@@ -193,6 +190,12 @@ def run_cpu_baseline(scene, budget_s=15.0, max_steps=400, warmup=1):
     o = pyoracle.Oracle()
     be = kseq.OracleBackend(o)
     s = kseq.state_arrays(scene)
+    # the packing's pair lists with their tangential history, as the GPU
+    # handles load them
+    for (cnt, ids, tsd), key in zip(getattr(scene, "pairs", []) or [], ("pp", "pl")):
+        s[key + "_count"][:] = cnt
+        s[key + "_id"][:] = ids
+        s[key + "_tsd"][:] = tsd
     for _ in range(warmup):
         kseq.sphere_step(be, scene, s, (), compat=0)
     t0 = time.perf_counter()
@@ -283,6 +286,86 @@ def bench_e2e(sm, scene, torch, steps):
     h2d = nb * (15 * 8 + C.sizeof(T.PlaneInfo))
     return {"value": scene.np_ * steps / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": nb * 48,
             "steps": steps}
+
+
+def pair_capacity(scene):
+    """Spheres of the packing whose particle-pair list is full: the
+    reference keeps MAX_P2P_COUNT = 12 partners per sphere (decl:13); a
+    sphere that touches more raises XDEM_ERR_P2P_OVERFLOW and its extra
+    contacts are dropped (the reference writes them into the next
+    particle's slots)."""
+    from xdynamics_dll_gb300 import types as T
+    cnt = np.asarray(scene.pairs[0][0]) if getattr(scene, "pairs", None) else None
+    if cnt is None:
+        return None
+    return {"slots": T.MAX_P2P_COUNT, "spheres_at_capacity": int((cnt >= T.MAX_P2P_COUNT).sum()),
+            "fraction_at_capacity": float((cnt >= T.MAX_P2P_COUNT).mean())}
+
+
+def precision_check(scene, steps, torch, shapes):
+    """Mixed against plain FP64 on the same input, untimed: both forms step
+    the packing `steps` steps; kinetic energy and stored contacts are read
+    every steps/10 steps.  Returns the final and the largest relative KE
+    difference, the contact-count difference, and the list rebuilds of the
+    mixed form per 1000 steps."""
+    from xdynamics_dll_gb300 import types as T
+    out = {}
+    for prec in (T.XDEM_MIXED, T.XDEM_FP64):
+        sm = new_sim(scene, prec)
+        if prec == T.XDEM_MIXED and shapes:
+            sm.set_tune(**{k: int(shapes[k]) for k in T.Tune.SHAPE})
+        sm.set_graph(True)
+        trace = []
+        t0 = time.perf_counter()
+        for _ in range(10):
+            sm.step(steps // 10)
+            trace.append(sm.energy())
+        torch.cuda.synchronize()
+        out[prec] = dict(trace=trace, status=sm.status(), rebuilds=sm.list_rebuilds(),
+                         secs=time.perf_counter() - t0)
+        sm.close()
+        log(f"precision check {'mixed' if prec == T.XDEM_MIXED else 'fp64'}: {out[prec]['secs']:.1f} s")
+    mx, fp = out[T.XDEM_MIXED], out[T.XDEM_FP64]
+    rel = [abs(a[0] - b[0]) / b[0] for a, b in zip(mx["trace"], fp["trace"])]
+    return {"steps": steps, "ke_fp64": fp["trace"][-1][0], "ke_mixed": mx["trace"][-1][0],
+            "ke_rel_err_vs_fp64": rel[-1], "ke_rel_err_max_over_trace": max(rel),
+            "contacts_fp64": fp["trace"][-1][1], "contacts_mixed": mx["trace"][-1][1],
+            "contact_count_diff_vs_fp64": int(mx["trace"][-1][1]) - int(fp["trace"][-1][1]),
+            "contact_count_rel_diff_max_over_trace": max(abs(int(a[1]) - int(b[1])) / b[1]
+                                                         for a, b in zip(mx["trace"], fp["trace"])),
+            "list_rebuilds_per_1000_steps": 1000.0 * mx["rebuilds"] / steps,
+            "status": {"mixed": mx["status"], "fp64": fp["status"]},
+            "trace_every": steps // 10,
+            "ke_trace_fp64": [t[0] for t in fp["trace"]], "ke_trace_mixed": [t[0] for t in mx["trace"]]}
+
+
+def rebuild_timing(sm, torch, stream, steps=16):
+    """Eager step times (CUDA events on the handle's stream) of a step that
+    rebuilds the candidate lists and of steps that reuse them: re-uploading
+    the particle-pair list unchanged makes the next step rebuild (a state or
+    list change always does), and the following steps run from the lists."""
+    cnt, ids, tsd = sm.pairs(0)
+    sm.set_graph(False)
+
+    def one():
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        sm.step(1)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    rebuild = []
+    plain = []
+    for _ in range(3):
+        sm.set_pairs(0, cnt, ids, tsd)
+        rebuild.append(one())
+        plain += [one() for _ in range(steps // 3)]
+        cnt, ids, tsd = sm.pairs(0)
+    return {"rebuild_step_ms": statistics.median(rebuild), "list_step_ms": statistics.median(plain),
+            "timing": "eager launches, CUDA events per step, median of 3 rebuild steps and "
+                      f"{len(plain)} list steps"}
 
 
 def bench_sweep(args, torch, local):
@@ -596,9 +679,8 @@ def main():
     ap.add_argument("--shapes", default=None,
                     help='mixed-stage shapes as JSON (e.g. the "autotune" field of an earlier line) instead of '
                          'autotuning')
-    ap.add_argument("--settle", type=int, default=0,
-                    help="untimed GPU settling steps behind a gate before timing (0: time the deterministic "
-                         "initial packing, the same input the reference arm times)")
+    ap.add_argument("--check-steps", type=int, default=1000,
+                    help="steps of the untimed mixed-vs-FP64 comparison on the same packing (0 skips it)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     warmup = max(3, args.warmup)
@@ -612,6 +694,11 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        # the packing is made by the GPU library's settling pre-run (once per
+        # box, cached as a part file) and read back here; the timed steps
+        # below run on the host cores only
+        from xdynamics_dll_gb300 import build
+        build.build()
         scene = make_scene(args.n)
         # the reference's own CPU DEM path does not work (plane detection is
         # stubbed, every pair is applied to every particle); its GPU kernels
@@ -622,9 +709,7 @@ def main():
             "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": warmup, "ms_per_step": 1e3 * scene.np_ / cb["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"dam break, {scene.np_} polydisperse spheres r~U[1,2] mm, dt=5e-6 s, 5 planes",
-                       "precision": "f64", "grid": list(scene.grid), "cell_size": scene.cell_size},
+            "dtype": "f64", "data": "synthetic", "config": workload_config(scene),
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}))
         return
@@ -649,8 +734,6 @@ def main():
             bench_wheel(args, torch, local)
         return
     scene = make_scene(args.n)
-    if args.settle:
-        scene = settle(scene, args.settle, torch)
 
     # plain FP64 path, then mixed (the headline), same scene
     sm64, _, r64 = bench_precision(scene, T.XDEM_FP64, args.steps, warmup, torch, local, advance=args.advance)
@@ -663,7 +746,9 @@ def main():
                                        advance=args.advance)
     clocks = sampler.summary()
     e2e = bench_e2e(smx, scene, torch, min(args.steps, 200))
+    rbt = rebuild_timing(smx, torch, stream)
     smx.close()
+    check = precision_check(scene, args.check_steps, torch, rmx["tune"]) if args.check_steps else None
 
     n = scene.np_
     value, value64, e2e["value"], secs64, secsx = replica_totals(
@@ -687,11 +772,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": warmup,
         "ms_per_step": 1e3 * secsx / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 contact / f64 state (mixed)", "data": "synthetic",
-        "config": {"workload": f"dam break, {n} polydisperse spheres r~U[1,2] mm, dt=5e-6 s, 5 planes",
-                   "precision": "mixed", "grid": list(scene.grid), "cell_size": scene.cell_size,
-                   "l2": "inputs larger than L2 (about 0.5 GB of state), no flush", "replicas": ws,
-                   "advance_steps": args.advance,
-                   "parallelism": f"replicas{ws}"},
+        "config": workload_config(scene),
+        "replicas": ws, "advance_steps": args.advance,
         "fp64": {"value": value64, "ms_per_step": 1e3 * secs64 / args.steps, "contact_kernel_ms": r64["contact_ms"],
                  "mixed_over_fp64": value / value64},
         "contacts_per_sphere": cbar,
@@ -703,6 +785,12 @@ def main():
         "gpu_launches": rmx["launches"],
         "autotune": rmx["tune"],
         "list_rebuilds": rmx["list_rebuilds"],
+        "list_rebuilds_per_1000_steps": 1000.0 * rmx["list_rebuilds"] / args.steps,
+        "rebuild_step": rbt,
+        "precision_check": check,
+        "ke_rel_err_vs_fp64": check["ke_rel_err_vs_fp64"] if check else None,
+        "contact_count_diff_vs_fp64": check["contact_count_diff_vs_fp64"] if check else None,
+        "pair_capacity": pair_capacity(scene),
         "status": {"fp64": r64["status"], "mixed": rmx["status"]},
     }
     if not args.no_cpu:

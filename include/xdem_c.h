@@ -220,8 +220,9 @@ XDEM_API int cu_reorderDataAndFindCellStart(unsigned int* hash,
  * cu_reorderDataAndFindCellStart, but it allocates no device memory: the sort
  * scratch is a fixed array inside the library (about 2.2 MB on every GPU that
  * loads the library, kept until the process exits), for callers that may not
- * call cudaMalloc -- a step being recorded into a CUDA graph, a real-time
- * loop, a host whose device memory belongs to an external pool.
+ * call cudaMalloc -- a real-time loop that cannot risk an allocation's
+ * latency or an out-of-memory failure mid-run, a host whose device memory
+ * belongs to an external pool.
  * np (particles + mesh spheres) must not exceed 262144; larger calls return
  * XDEM_ERR_ARG without touching the arrays.  The first call on a device looks
  * up the array's device address; make that first call before any stream
@@ -378,7 +379,8 @@ XDEM_API int xdem_sim_create(const xdem_sim_config* cfg, xdem_sim** out);
 XDEM_API int xdem_sim_destroy(xdem_sim* sim);
 /* Host arrays, reference layout: pos[np*4], vel/acc[ns*3], ep/ev/ea[ns*4],
  * mass[ns], inertia[ns*3].  Any pointer but pos/mass/inertia may be NULL
- * (zero; ep defaults to (1,0,0,0)). */
+ * (zero; ep defaults to (1,0,0,0)).  A NaN or infinite entry returns
+ * XDEM_ERR_NONFINITE | XDEM_ERR_ARG before anything is uploaded. */
 XDEM_API int xdem_sim_set_state(xdem_sim* sim, const double* pos,
                                 const double* vel, const double* acc,
                                 const double* ep, const double* ev,
@@ -467,7 +469,11 @@ XDEM_API int xdem_sim_get_state(xdem_sim* sim, double* pos, double* vel,
                                 double* acc, double* ep, double* ev,
                                 double* ea, double* cpos);
 /* kind: 0 particle-particle, 1 particle-plane, 2 particle-triangle,
- * 3 particle-cylinder (MAX_P2CY_COUNT slots). */
+ * 3 particle-cylinder (MAX_P2CY_COUNT slots).  set_pairs (and load_part, for
+ * the lists of a file) returns XDEM_ERR_ARG, uploading nothing, when a count
+ * exceeds the kind's slots or a stored id names no particle (kind 0), plane
+ * (1), triangle (2) or cylinder (3: id, or id + 1000 for an inner cap) of the
+ * handle. */
 XDEM_API int xdem_sim_get_pairs(xdem_sim* sim, int kind, unsigned int* count,
                                 unsigned int* ids, double* tsd);
 XDEM_API int xdem_sim_set_pairs(xdem_sim* sim, int kind,

@@ -31,7 +31,8 @@ import pyoracle  # noqa: E402
 import kseq  # noqa: E402
 from xdynamics_dll_gb300 import scenes, types as T  # noqa: E402
 
-REF_ROOT = os.environ.get("XDEM_REFERENCE_ROOT", "/root/reference")
+# the reference checkout sits beside this repository unless XDEM_REFERENCE_ROOT says otherwise
+REF_ROOT = os.environ.get("XDEM_REFERENCE_ROOT") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def read_part_file(path):

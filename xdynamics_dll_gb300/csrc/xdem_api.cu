@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -31,7 +32,9 @@ namespace {
 constexpr int kMaxDevices = 64;
 
 struct DevCtx {
-    bool init = false;
+    // set (release) once every pointer below is allocated; read (acquire)
+    // outside the lock by the fast path of ctx()
+    std::atomic<bool> init{false};
     unsigned int* status = nullptr;
     double* red_tmp = nullptr;     // 1024 partials + 1 result
     mat_pair* mp = nullptr;        // scratch material constants
@@ -94,9 +97,9 @@ DevCtx* ctx(int* err)
         return nullptr;
     }
     DevCtx& c = g_dev[dev];
-    if (!c.init) {
+    if (!c.init.load(std::memory_order_acquire)) {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!c.init) {
+        if (!c.init.load(std::memory_order_relaxed)) {
             e = cudaMalloc(&c.status, sizeof(unsigned int));
             if (e == cudaSuccess) e = cudaMemset(c.status, 0, sizeof(unsigned int));
             if (e == cudaSuccess) e = cudaMalloc(&c.red_tmp, 1025 * sizeof(double));
@@ -107,7 +110,7 @@ DevCtx* ctx(int* err)
                 *err = XDEM_ERR_ALLOC;
                 return nullptr;
             }
-            c.init = true;
+            c.init.store(true, std::memory_order_release);
         }
     }
     return &c;

@@ -123,6 +123,11 @@ XDEM_API int xdem_sim_load_part(xdem_sim* s, const char* path, double* time)
     }
     char extra;
     if (std::fread(&extra, 1, 1, in.f) != 0) return XDEM_ERR_ARG;  // blocks this handle has no contacts for
+    // every list is checked before anything of the file reaches the handle,
+    // so a corrupt file leaves the handle as it was
+    for (int b = 0; b < kBlocks; ++b)
+        if (want[b])
+            if (int r = sim_check_pairs(s, kBlockKind[b], cnt[b].data(), ids[b].data())) return r;
     // the inertia is not in the file: the handle keeps its own
     std::vector<double> iner(ns * 3);
     if (cudaMemcpy(iner.data(), s->inertia, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)

@@ -2,13 +2,13 @@
 // allocation.
 //
 // The regular launcher sorts with scratch the library allocates (and grows)
-// on first use with cudaMalloc.  Some callers cannot allow that: code that
-// records its step into a CUDA graph while capturing (cudaMalloc is not
-// permitted inside a capture), real-time loops where an allocation's latency
-// or a possible out-of-memory failure in mid-run is unacceptable, and hosts
-// whose device memory is owned by an external pool that forbids allocations
-// behind its back.  This variant takes its sort scratch from a fixed array
-// compiled into the library instead.
+// on first use with cudaMalloc.  Some callers cannot allow that: real-time
+// loops where an allocation's latency or a possible out-of-memory failure in
+// mid-run is unacceptable, and hosts whose device memory is owned by an
+// external pool that forbids allocations behind its back.  This variant takes
+// its sort scratch from a fixed array compiled into the library instead.
+// Its first call on a device looks the array's address up
+// (cudaGetSymbolAddress); make that first call before any stream capture.
 //
 // The array lives in device memory of every GPU that loads the library and
 // stays there until the process exits; its size is fixed at build time

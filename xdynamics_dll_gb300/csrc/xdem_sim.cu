@@ -617,6 +617,18 @@ XDEM_API int xdem_sim_set_state(xdem_sim* s, const double* pos, const double* ve
 {
     if (!s || !pos || !mass || !inertia) return XDEM_ERR_ARG;
     const size_t n = s->np, ns = s->ns;
+    // a state with a NaN or infinite entry is refused before any upload (the
+    // handle keeps its previous state); the step's own hash check raises
+    // XDEM_ERR_NONFINITE for values that turn non-finite on the device
+    auto finite = [](const double* h, size_t cnt) {
+        if (!h) return true;
+        for (size_t i = 0; i < cnt; ++i)
+            if (!std::isfinite(h[i])) return false;
+        return true;
+    };
+    if (!(finite(pos, n * 4) && finite(vel, ns * 3) && finite(acc, ns * 3) && finite(ep, ns * 4) &&
+          finite(ev, ns * 4) && finite(ea, ns * 4) && finite(mass, ns) && finite(inertia, ns * 3)))
+        return XDEM_ERR_NONFINITE | XDEM_ERR_ARG;
     cudaError_t e = cudaSuccess;
     auto H = [&](double* d, const double* h, size_t cnt, double fill, int every, int off) {
         if (e != cudaSuccess) return;
@@ -1117,6 +1129,34 @@ XDEM_API int xdem_sim_get_pairs(xdem_sim* s, int kind, unsigned int* count, unsi
     return cerr(e);
 }
 
+// Lists from a file or a caller are checked before anything reaches the
+// device: no count above the slot capacity, and every stored id names
+// something the handle has -- a particle (kind 0), a plane (1), a triangle
+// (2), a cylinder or its inner cap, id + 1000 (3).  Kernels that look a
+// partner up by its id (the adjoint's gather) then never index out of range.
+int sim_check_pairs(const xdem_sim* s, int kind, const unsigned int* count, const unsigned int* ids)
+{
+    if (!s || kind < 0 || kind > 3 || !count || !ids) return XDEM_ERR_ARG;
+    const unsigned int cap = kind == 0 ? MAX_P2P_COUNT : kind == 1 ? MAX_P2PL_COUNT
+                           : kind == 2 ? MAX_P2MS_COUNT : MAX_P2CY_COUNT;
+    const unsigned int ncyl = (unsigned int)s->cylinders.size();
+    for (size_t i = 0; i < s->np; ++i) {
+        if (count[i] > cap) return XDEM_ERR_ARG;
+        for (unsigned int k = 0; k < count[i]; ++k) {
+            const unsigned int id = ids[i * cap + k];
+            bool ok;
+            switch (kind) {
+            case 0: ok = id < s->np; break;
+            case 1: ok = id < s->planes.size(); break;
+            case 2: ok = id < s->ntri_total; break;
+            default: ok = id < ncyl || (id >= 1000u && id - 1000u < ncyl); break;
+            }
+            if (!ok) return XDEM_ERR_ARG;
+        }
+    }
+    return XDEM_OK;
+}
+
 XDEM_API int xdem_sim_set_pairs(xdem_sim* s, int kind, const unsigned int* count, const unsigned int* ids,
                                 const double* tsd)
 {
@@ -1124,6 +1164,7 @@ XDEM_API int xdem_sim_set_pairs(xdem_sim* s, int kind, const unsigned int* count
     const size_t n = s->np;
     const PairTables t = pair_tables(s, kind);
     const unsigned int cap = t.cap;
+    if (int r = sim_check_pairs(s, kind, count, ids)) return r;
     unsigned int* dc = t.count;
     unsigned int* di = t.id;
     double* dt = t.tsd;

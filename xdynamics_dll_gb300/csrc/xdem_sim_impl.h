@@ -119,3 +119,9 @@ struct xdem_sim {
     // capacities of the body tables
     size_t plane_cap = 0, body_cap = 0, mp_cap = 0, cyl_cap = 0;
 };
+
+// XDEM_OK when every count of a host pair list (kind as xdem_sim_get_pairs)
+// is within its slot capacity and every stored id names a particle, plane,
+// triangle or cylinder of the handle; XDEM_ERR_ARG otherwise.
+extern "C" int sim_check_pairs(const xdem_sim* s, int kind, const unsigned int* count,
+                                const unsigned int* ids);

@@ -8,6 +8,7 @@ Initialize (source/xdynamics_simulation/xDiscreteElementMethodSimulation.cpp:
 63-80): zero velocities, identity Euler parameters, acceleration (0, g_y, 0).
 All randomness is seeded.
 """
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -230,6 +231,148 @@ def dam_break(n_target=1_000_000, r_min=1e-3, r_max=2e-3, rho=2500.0, E=1e7, nu=
                  plane_body=[T.body_record() for _ in planes], name="dam_break",
                  note=f"{N} spheres r~U[{r_min},{r_max}] lattice {nx}x{ny}x{nz} spacing {sp:.5g} "
                       f"block height {pts[:, 1].max():.3f} m")
+
+
+def fcc_block(n, d, x_range, z_range, y0, jitter, rng):
+    """n sites of a face-centred cubic lattice with nearest-neighbour
+    distance d filling x_range x z_range layer by layer from y0 upward:
+    points of the cubic lattice of pitch h = d / sqrt(2) whose index sum is
+    even.  Ordered by layer (y), then z, then x, as the reference's cube
+    fills number their particles.  Each coordinate is jittered by
+    U[-jitter, jitter]."""
+    h = d / np.sqrt(2.0)
+    nx = int(np.floor((x_range[1] - x_range[0]) / h)) + 1
+    nz = int(np.floor((z_range[1] - z_range[0]) / h)) + 1
+    per_two = nx * nz  # sites in two consecutive layers
+    ny = int(np.ceil(2 * n / per_two)) + 1
+    j, k, i = np.meshgrid(np.arange(ny), np.arange(nz), np.arange(nx), indexing="ij")
+    keep = ((i + j + k) & 1) == 0
+    pts = np.stack([x_range[0] + i[keep] * h, y0 + j[keep] * h, z_range[0] + k[keep] * h], axis=1)[:n]
+    if pts.shape[0] < n:
+        raise ValueError("fcc_block: lattice too small")
+    return pts + rng.uniform(-jitter, jitter, size=pts.shape)
+
+
+def dam_break_fill(n=1_000_000, r_min=1e-3, r_max=2e-3, rho=2500.0, E=1e7, nu=0.3, rest=0.3, fric=0.4,
+                   dt=1e-5, seed=2025, block_x=0.2, box=(1.0, 0.4, 0.4)):
+    """The dam-break block before it settles: n spheres with radii
+    U[r_min, r_max] (seeded) on a jittered FCC lattice of nearest-neighbour
+    distance 2 r_max + 0.1 mm (no two spheres touch) filling x in
+    [0, block_x] and the box's depth, in a box of floor, four walls and the
+    gate plane at x = block_x, walls as tall as the lattice.  The settling
+    pre-run (settle_dam_break) turns it into the random packing the dam
+    break starts from."""
+    rng = np.random.default_rng(seed)
+    d = 2.0 * r_max + 1e-4
+    m = r_max + 5e-5
+    pts = fcc_block(n, d, (m, block_x - m), (m, box[2] - m), m, 2e-5, rng)
+    radii = rng.uniform(r_min, r_max, size=n)
+    pos = np.zeros((n, 4))
+    pos[:, :3] = pts
+    pos[:, 3] = radii
+    mass, J = sphere_mass_inertia(radii, rho)
+    vel, acc, ep, ev, ea = _init_state(n)
+    top = float(pts[:, 1].max()) + 2.0 * r_max
+    cp = default_material(E, nu, rest, fric)
+    planes = open_box_planes(0.0, box[0], 0.0, top, 0.0, box[2])
+    gate = T.plane_from_points(len(planes), (block_x, 0.0, 0.0), (block_x, 0.0, box[2]), (block_x, top, 0.0))
+    planes.append(gate)
+    cs = 2.0 * r_max
+    o = -1.25 * cs
+    grid_dims = (pow2_at_least(int(np.ceil((box[0] - o) / cs)) + 1),
+                 pow2_at_least(int(np.ceil((top - o) / cs)) + 1),
+                 pow2_at_least(int(np.ceil((box[2] - o) / cs)) + 1))
+    return Scene(np_=n, ns=n, pos=pos.ravel(), vel=vel, acc=acc, ep=ep, ev=ev, ea=ea, mass=mass,
+                 inertia=J.ravel(), dt=dt, cell_size=cs, grid=grid_dims, origin=(o, o, o), pp_cp=cp,
+                 planes=planes, plane_cp=[cp] * len(planes), plane_body=[T.body_record() for _ in planes],
+                 name="dam_break_fill", note=f"{n} spheres r~U[{r_min},{r_max}] FCC fill, top {top:.3f} m")
+
+
+# Settling pre-run of the dam-break packing: block shapes of the mixed step
+# (they do not change results) and the number of settling steps of 1e-5 s.
+SETTLE_SHAPES = dict(nt_pairs=128, stage=8, nt_bodies=128, occ_pairs=1024, occ_bodies=768, skin_div=32)
+SETTLE_STEPS = 40000
+
+
+def cache_dir():
+    d = os.environ.get("XDEM_CACHE") or os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                                     ".xdem_cache")
+    os.makedirs(d, exist_ok=True)
+    return d
+
+
+def settle_dam_break(fill, steps, path, log=None):
+    """Untimed, seeded settling pre-run on the GPU: the FCC fill falls under
+    gravity behind the gate and comes to rest as a random packing (mixed
+    step, dt of the fill).  Writes the final state and the particle-pair and
+    plane pair lists with their tangential history to a part file (the
+    reference's version-2 layout) at `path`.  Deterministic: the step sums
+    every contact in a fixed order, so the same build on the same GPU model
+    writes the same file."""
+    from . import sim as S
+    sm = S.Sim(fill, precision=T.XDEM_MIXED)
+    sm.set_tune(**SETTLE_SHAPES)
+    sm.set_graph(True)
+    done = 0
+    chunk = 5000
+    while done < steps:
+        k = min(chunk, steps - done)
+        sm.step(k)
+        done += k
+        if log:
+            ke, nc = sm.energy()
+            log(f"settle {done}/{steps}: ke {ke:.4e} J, {nc / fill.np_:.3f} contacts/sphere, "
+                f"status {sm.status()}")
+    tmp = path + ".tmp"
+    sm.save_part(tmp, 0.0)
+    sm.close()
+    os.replace(tmp, path)
+
+
+def dam_break_packed(n=1_000_000, seed=2025, settle_steps=SETTLE_STEPS, dt=5e-6, box=(1.0, 0.4, 0.4),
+                     log=None, path=None):
+    """The dam-break configuration from a settled random packing: the FCC
+    fill of dam_break_fill settled behind the gate for `settle_steps` steps
+    of 1e-5 s (settle_dam_break, cached as a part file keyed by n, seed and
+    steps), then the gate removed (t = 0).  The box is 1 x 0.4 x 0.4 m
+    (floor, four walls 0.4 m tall); dt 5e-6 s.  The scene carries the
+    settled state and, in `pairs`, the particle-pair and plane lists with
+    their tangential history (kinds 0 and 1; the gate's slots are dropped
+    by the first step, whose plane 0 restarts every plane list)."""
+    from . import partfile
+    fill = dam_break_fill(n=n, seed=seed, box=box)
+    if path is None:
+        path = os.path.join(cache_dir(), f"dam_break_n{n}_s{seed}_k{settle_steps}.part")
+    if not os.path.exists(path):
+        settle_dam_break(fill, settle_steps, path, log=log)
+    d = partfile.read(path, ("pp", "pl"))
+    if d["np"] != n:
+        raise ValueError(f"{path}: {d['np']} spheres, {n} expected")
+    sc = fill.copy()
+    sc.pos, sc.vel, sc.acc = d["pos"], d["vel"], d["acc"]
+    sc.ep, sc.ev, sc.ea = d["ep"], d["ev"], d["ea"]
+    sc.dt = dt
+    sc.planes = open_box_planes(0.0, box[0], 0.0, box[1], 0.0, box[2])
+    sc.plane_cp = [sc.pp_cp] * len(sc.planes)
+    sc.plane_body = [T.body_record() for _ in sc.planes]
+    cap_pp, cap_pl = T.MAX_P2P_COUNT, T.MAX_P2PL_COUNT
+    # the gate is gone: its plane slots are dropped, the other planes' slots
+    # keep their order and history
+    nb = len(sc.planes)
+    plc, pli, plt = d["pl_count"], d["pl_id"].reshape(n, cap_pl), d["pl_tsd"].reshape(n, cap_pl, 2)
+    keep = (np.arange(cap_pl)[None, :] < plc[:, None]) & (pli < nb)
+    order = np.argsort(~keep, axis=1, kind="stable")
+    pli = np.where(np.take_along_axis(keep, order, 1), np.take_along_axis(pli, order, 1), 0)
+    plt = np.where(np.take_along_axis(keep, order, 1)[:, :, None], np.take_along_axis(plt, order[:, :, None], 1), 0.0)
+    plc = keep.sum(1).astype(np.uint32)
+    sc.pairs = [(d["pp_count"], d["pp_id"], d["pp_tsd"]), (plc, pli.ravel(), plt.ravel())]
+    assert d["pp_id"].size == n * cap_pp and d["pl_id"].size == n * cap_pl
+    p = sc.pos.reshape(-1, 4)
+    sc.name = "dam_break_packed"
+    sc.note = (f"{n} spheres r~U[1,2] mm, random packing settled {settle_steps} x 1e-5 s behind the gate "
+               f"(bed top {float((p[:, 1] + p[:, 3]).max()):.3f} m), gate removed at t = 0")
+    sc.part_path = path
+    return sc
 
 
 def random_packed(n, r_min, r_max, box, seed, overlap=0.05, vel_scale=0.05, omega_scale=5.0,
