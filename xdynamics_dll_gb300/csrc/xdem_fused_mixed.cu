@@ -437,7 +437,18 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
     }
     c.pp_count_new[oid] = cnt;
     if (build) {
-        if (nlist > kListCap) atomicOr(c.vl_flag + kVlOverflow, 1u);
+        if (nlist > kListCap) {
+            atomicOr(c.vl_flag + kVlOverflow, 1u);
+        } else {
+            // the row ascends by id, so that a list step's (stencil cell,
+            // slot) keys order the contacts by (cell, id) as the walk does
+            for (unsigned int a = 1; a < nlist; ++a) {
+                const unsigned int v = vl[a];
+                unsigned int b = a;
+                for (; b > 0 && vl[b - 1] > v; --b) vl[b] = vl[b - 1];
+                vl[b] = v;
+            }
+        }
         c.vl_cnt[oid] = nlist;
         reinterpret_cast<float4*>(c.vl_xb)[oid] =
             make_float4((float)ux * cs + Ai.x, (float)uy * cs + Ai.y, (float)uz * cs + Ai.z, 0.f);
@@ -453,13 +464,17 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
 // Ft a zero-slip contact keeps and every sum come out the same.  The list
 // holds every sphere within r_i + r_j + skin at its build, so while no
 // sphere has moved half the skin it holds every contact.
+static_assert(kListCap <= 32, "a list sort key keeps the slot in 5 bits");
+
 template <unsigned int NT>
 __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oid, float4 Ai, float4 Li,
-                                         unsigned int Ti, float4 Bi, float4 Ci, unsigned int* old_id, Acc& acc,
-                                         unsigned int& bits)
+                                         unsigned int Ti, float4 Bi, float4 Ci, unsigned int* old_id,
+                                         unsigned int* keys, Acc& acc, unsigned int& bits)
 {
     const unsigned int scene = scene_index(c, oid);
     const bool coh = false;  // lists are only kept without cohesion
+    const float cs = c.cs_f;
+    const float screen = 1.0f + 0x1p-11f;
     const unsigned int ux = Ti & 2047u, uy = (Ti >> 11) & 2047u, uz = Ti >> 22;
     const unsigned int sid = oid * MAX_P2P_COUNT;
     unsigned int old_count = c.pp_count_old[oid];
@@ -472,30 +487,43 @@ __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oi
     // 16-byte aligned), not after it: their records' loads start a round
     // trip earlier
     const uint4 head = reinterpret_cast<const uint4*>(ids)[0];
-    // (cell offset key, id) of the candidates inside this step's stencil
-    unsigned long long key[kListCap];
+    // Key phase: each candidate's position (A) and cell (C) records; those
+    // inside this step's stencil that pass the walk's FP32 screen (squared
+    // distance within 1 + 2^-11 of the squared contact distance, so no
+    // contact is ever dropped: the float-pair test below decides) get a key
+    // (stencil cell << 5 | slot).  The row is sorted by id when it is built,
+    // so ascending keys visit the contacts in the walk's (cell, id) order.
+    // Keys are sorted in shared memory, [slot][thread] with stride NT.
     unsigned int nk = 0;
+#pragma unroll 2
     for (unsigned int q = 0; q < n; ++q) {
         const unsigned int k = q == 0 ? head.x : q == 1 ? head.y : q == 2 ? head.z : q == 3 ? head.w : ids[q];
         if (c.scene_of && c.scene_of[k] != scene) continue;  // another scene of the batch
-        const unsigned int Tk = rec_cell(c.rec[4 * (size_t)k + kRecC]);
+        const float4* r = c.rec + 4 * (size_t)k;
+        const float4 Aj = r[kRecA];
+        const unsigned int Tk = rec_cell(r[kRecC]);
         const unsigned int xs = (Tk - ux + 1u) & 2047u;
         const unsigned int ys = ((Tk >> 11) - uy + 1u) & 2047u;
         const unsigned int zs = ((Tk >> 22) - uz + 1u) & 1023u;
         if (xs > 2u || ys > 2u || zs > 2u) continue;
-        const unsigned long long kk = ((unsigned long long)((zs * 3u + ys) * 3u + xs) << 32) | k;
+        const float dx = Aj.x + ((xs == 0u ? -cs : (xs == 2u ? cs : 0.f)) - Ai.x);
+        const float dy = Aj.y + ((ys == 0u ? -cs : (ys == 2u ? cs : 0.f)) - Ai.y);
+        const float dz = Aj.z + ((zs == 0u ? -cs : (zs == 2u ? cs : 0.f)) - Ai.z);
+        const float rr = Ai.w + Aj.w;
+        if (!(dx * dx + dy * dy + dz * dz < rr * rr * screen)) continue;
+        const unsigned int key = (((zs * 3u + ys) * 3u + xs) << 5) | q;
         unsigned int p = nk++;
-        while (p > 0 && key[p - 1] > kk) {
-            key[p] = key[p - 1];
+        while (p > 0 && keys[(p - 1) * NT] > key) {
+            keys[p * NT] = keys[(p - 1) * NT];
             --p;
         }
-        key[p] = kk;
+        keys[p * NT] = key;
     }
     cp_async_wait_all();
     V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
     unsigned int cnt = 0;
     for (unsigned int q = 0; q < nk; ++q) {
-        const unsigned int k = (unsigned int)key[q];
+        const unsigned int k = ids[keys[q * NT] & 31u];
         const float4* r = c.rec + 4 * (size_t)k;
         const float4 Aj = r[kRecA], Lj = r[kRecL], Bj = r[kRecB], Cj = r[kRecC];
         p2p_pair_rec<NT>(c, k, rec_cell(Cj), Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
@@ -1173,7 +1201,8 @@ template <bool MESH, unsigned int NT, unsigned int OCC>
 __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
 {
     __shared__ float smf[MESH ? (NT / 32) * 6 * 2 : 1];
-    __shared__ unsigned int stage[16 * NT];                   // walk fallback candidates, [slot][thread]
+    // walk fallback candidates or the list's sort keys, [slot][thread]
+    __shared__ unsigned int stage[kListCap * NT];
     __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
     const bool rebuild = c.vl_flag[kVlRebuild] != 0u;
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1194,7 +1223,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_
     unsigned int bits = 0;
     if (live) {
         if (!rebuild && c.vl_cnt[oid] <= kListCap)
-            p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, acc, bits);
+            p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, stage + threadIdx.x, acc, bits);
         else
             p2p_mixed<NT, 16>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
                               bits, rebuild);
@@ -1284,21 +1313,36 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
         const unsigned int scene = live ? scene_index(c, oid) : 0u;
         const unsigned int kbeg = batched ? c.scene_plane_first[scene] : 0u;
         const unsigned int kend = batched ? (live ? c.scene_plane_first[scene + 1] : kbeg) : c.nplane;
-        for (unsigned int k = kbeg; k < kend; ++k) {
+        // conservative FP32 test: every region of the plane test needs the
+        // centre within r of the plane and of the rectangle's extent
+        auto near_plane = [&](unsigned int k) {
+            if (c.planedf[k].coh) return true;
+            const PlaneF& pf = c.planef[k];
+            const float dx = ipf.x - pf.v[0], dy = ipf.y - pf.v[1], dz = ipf.z - pf.v[2];
+            const float wx = dx * pf.v[3] + dy * pf.v[4] + dz * pf.v[5];
+            const float wy = dx * pf.v[6] + dy * pf.v[7] + dz * pf.v[8];
+            const float wz = dx * pf.v[9] + dy * pf.v[10] + dz * pf.v[11];
+            const float lim = ipf.w + c.margin;
+            return fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
+        };
+        // one block-wide vote first: a block none of whose spheres is near
+        // any plane (almost every block of a large bed) writes zero wrench
+        // partials for every plane and skips the plane loop with its
+        // per-plane barriers -- what the loop would have written
+        bool run_planes = true;
+        if (!batched) {
+            bool any_near = false;
+            if (live)
+                for (unsigned int k = kbeg; k < kend && !any_near; ++k) any_near = near_plane(k);
+            run_planes = __syncthreads_or(any_near ? 1 : 0) != 0;
+            if (!run_planes)
+                for (unsigned int w = threadIdx.x; w < 6u * c.nplane; w += NT)
+                    c.bsums[((size_t)(w / 6u) * c.nblocks + blockIdx.x) * 6 + w % 6u] = 0.0;
+        }
+        for (unsigned int k = kbeg; run_planes && k < kend; ++k) {
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             bool touched = false;
-            // conservative FP32 test: every region of the plane test needs the
-            // centre within r of the plane and of the rectangle's extent
-            bool near = true;
-            if (live && !c.planedf[k].coh) {
-                const PlaneF& pf = c.planef[k];
-                const float dx = ipf.x - pf.v[0], dy = ipf.y - pf.v[1], dz = ipf.z - pf.v[2];
-                const float wx = dx * pf.v[3] + dy * pf.v[4] + dz * pf.v[5];
-                const float wy = dx * pf.v[6] + dy * pf.v[7] + dz * pf.v[8];
-                const float wz = dx * pf.v[9] + dy * pf.v[10] + dz * pf.v[11];
-                const float lim = ipf.w + c.margin;
-                near = fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
-            }
+            const bool near = !live || near_plane(k);
             if (live && near) {
                 need_bc();
                 const PlaneOut o = plane_call(&c, k, kbeg, oid, ip, Bi, Ci, pl_cnt);
