@@ -534,10 +534,14 @@ def bench_wheel(args, torch, local):
     st_mx = sm.status()
     stage(f"mixed timed: {1e3 * secs / args.steps:.3f} ms/step")
     # e2e: the multibody exchange of every step -- host pose records in,
-    # wrenches out.  The host side moves the wheel: spin at omega about -z
-    # (prescribed drive) and vertical motion from the wrench and its weight
-    # (semi-implicit Euler), the pose of the next step re-placing its
-    # triangles; the planes stay where they are
+    # wrenches out.  The host side is the HHT-alpha multibody integrator
+    # (xdem_mbd_*): a 10 kg carriage sliding vertically on the ground, the
+    # tyre on a revolute joint to it about z, its spin driven at the
+    # configuration's 2 rad/s; each step the tyre's pose goes to the DEM
+    # step, the bed's wrench on the tyre comes back into the HHT force
+    # vector and the HHT step advances the rig.  The planes stay where they
+    # are
+    from xdynamics_dll_gb300 import mbd
     k_e2e = max(1, min(args.steps, 100))
     nb = len(sm.bodies)
     recs = [np.asarray(b, dtype=np.float64) for b in sc.plane_body] + [np.asarray(sc.meshes[0]["body"])]
@@ -549,33 +553,42 @@ def bench_wheel(args, torch, local):
     # tyre's frame entry is not read)
     idx = (C.c_int * nb)(*sm.bodies)
     pl_arr = (T.PlaneInfo * nb)(*(list(sc.planes) + [T.PlaneInfo()] * (nb - len(sc.planes))))
-    omega = -2.0 * float(recs[-1][14])
-    m_w = float(recs[-1][0])
+    w_rec = recs[-1].copy()
     # the held wheel's first contact pushed the top layer down: the exchange
     # starts with the wheel lowered 0.1 mm, pressing on the bed again
-    y_w, vy_w = float(recs[-1][2]) - 1e-4, 0.0
+    w_rec[2] -= 1e-4
+    m_w = float(w_rec[0])
+    omega_z = 2.0 * float(w_rec[14])  # w = 2 E(p) p_dot about z for the identity pose
+    r_t, w_t = 0.15, 0.1  # tyre radius and width: a thin ring about z
+    J_w = (m_w * (3 * r_t * r_t + w_t * w_t) / 12.0, m_w * (3 * r_t * r_t + w_t * w_t) / 12.0, m_w * r_t * r_t)
+    w_rec[3:7] = 0.0  # the rig starts at rest; the driver brings the spin
+    w_rec[11:15] = 0.0
+    rig, wb = mbd.wheel_rig(sc.dt, w_rec, J_w, omega_z, carriage_mass=10.0)
+    y_start = float(w_rec[2])
     fy_sum = 0.0
+    iters = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(k_e2e):
-        th = -omega * sc.dt * (i + 1)  # rolling toward +x: rotation about -z
-        rec[nb - 1, 7] = float(np.cos(0.5 * th))
-        rec[nb - 1, 10] = float(np.sin(0.5 * th))
-        rec[nb - 1, 2] = y_w
-        rec[nb - 1, 5] = vy_w
+        rec[nb - 1] = torch.from_numpy(rig.record(wb))
         _lib.check(sm.L.xdem_sim_set_bodies(sm.h, nb, idx, C.c_void_p(rec.data_ptr()), pl_arr),
                    "xdem_sim_set_bodies")
         sm.step(1)
         _lib.check(sm.L.xdem_sim_body_wrenches(sm.h, nb, idx, C.c_void_p(wr.data_ptr())), "xdem_sim_body_wrenches")
-        fy = float(wr[nb - 1, 1])
-        fy_sum += fy
-        vy_w += sc.dt * (fy / m_w + sc.gravity[1])
-        y_w += sc.dt * vy_w
+        fy_sum += float(wr[nb - 1, 1])
+        rig.set_contact_wrench(wb, wr[nb - 1].numpy())
+        iters.append(rig.step())
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     wheel_wrench = wr[nb - 1].tolist()
+    qw, qdw, _ = rig.body(wb)
     wheel = {"wrench_last": wheel_wrench, "mean_contact_force_y": fy_sum / k_e2e,
-             "sink_m": float(recs[-1][2]) - y_w, "mass_kg": m_w}
+             "sink_m": y_start - float(qw[1]), "mass_kg": m_w, "carriage_mass_kg": 10.0,
+             "host_integrator": "HHT-alpha (alpha -0.3), carriage on a vertical slider, tyre on a revolute "
+                                "joint driven at 2 rad/s",
+             "hht_newton_iterations": {"min": min(iters), "max": max(iters), "mean": float(np.mean(iters))},
+             "spin_angle_rad": float(2.0 * np.arctan2(qw[6], qw[3]))}
+    rig.close()
     sm.close()
     stage("e2e timed")
     # FP64 cluster step on the same scene

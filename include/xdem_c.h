@@ -576,6 +576,55 @@ XDEM_API int xdem_adj_backward(xdem_adj* adj, const double* dl_dpos, const doubl
 /* Properties (1 + planes), steps of the last forward, device bytes held. */
 XDEM_API int xdem_adj_info(xdem_adj* adj, unsigned int* nprop, unsigned int* nsteps, unsigned long long* bytes);
 
+/* ------------------------------------------------------------------------ */
+/* Host multibody side of the coupling: HHT-alpha over rigid bodies         */
+/* ------------------------------------------------------------------------ */
+/* The rigid bodies the DEM bed pushes on (a wheel on its carriage) advanced
+ * on the host by the HHT-alpha integrator of xIntegratorHHT
+ * (source/xdynamics_simulation/xIntegratorHHT.cpp:51-183): Euler-parameter
+ * coordinates, revolute and translational joints, a rotation driver on a
+ * revolute joint, a Newton loop with a dense solve, the DEM wrench in the
+ * force vector as xMultiBodySimulation::ConstructForceVector adds the
+ * contact force and moment (xMultiBodySimulation.cpp:341-360).  Body 0 is
+ * the ground.  Joints and the driver are defined at the bodies' poses when
+ * they are added; xdem_mbd_initialize then solves the consistent
+ * accelerations.  Host only: these calls touch no GPU.  Returns XDEM_OK or
+ * XDEM_ERR_ARG (bad argument, singular system, or a step whose Newton loop
+ * did not converge in 100 iterations). */
+typedef struct xdem_mbd xdem_mbd;
+/* alpha in [-1/3, 0] (the reference uses -0.3); gravity may be NULL. */
+XDEM_API int xdem_mbd_create(double dt, double alpha, const double gravity[3], xdem_mbd** out);
+XDEM_API int xdem_mbd_destroy(xdem_mbd* mbd);
+/* Newton tolerance on the residual norm (default 1e-5, the reference's). */
+XDEM_API int xdem_mbd_set_tolerance(xdem_mbd* mbd, double eps);
+/* Rigid body: mass, principal inertia (body frame), centre, Euler
+ * parameters; vel and ed (Euler-parameter rates) may be NULL. */
+XDEM_API int xdem_mbd_add_body(xdem_mbd* mbd, double mass, const double inertia[3], const double pos[3],
+                               const double ep[4], const double vel[3], const double ed[4], int* body);
+/* Revolute joint between bodies i and j at global point loc about the
+ * global axis (5 equations); translational joint letting j slide along the
+ * axis relative to i (5 equations). */
+XDEM_API int xdem_mbd_add_revolute(xdem_mbd* mbd, int body_i, int body_j, const double loc[3],
+                                   const double axis[3], int* joint);
+XDEM_API int xdem_mbd_add_translational(xdem_mbd* mbd, int body_i, int body_j, const double loc[3],
+                                        const double axis[3], int* joint);
+/* Drives the rotation of a revolute joint's body j relative to body i about
+ * the joint axis at omega rad/s from its present angle. */
+XDEM_API int xdem_mbd_add_rotation_driver(xdem_mbd* mbd, int revolute_joint, double omega);
+XDEM_API int xdem_mbd_initialize(xdem_mbd* mbd);
+/* Contact force and moment (global frame, fx fy fz mx my mz) on a body,
+ * held until replaced: the out6 of xdem_sim_body_wrench for that body. */
+XDEM_API int xdem_mbd_set_contact_wrench(xdem_mbd* mbd, int body, const double w6[6]);
+/* One HHT-alpha step of dt (prediction + Newton correction). */
+XDEM_API int xdem_mbd_step(xdem_mbd* mbd, int* iterations);
+/* Coordinates (r, p), their rates and accelerations; NULL skips. */
+XDEM_API int xdem_mbd_get_body(xdem_mbd* mbd, int body, double q[7], double qd[7], double qdd[7]);
+/* The body's 15-double record (decl:20) for xdem_sim_set_body(ies). */
+XDEM_API int xdem_mbd_body_record(xdem_mbd* mbd, int body, double rec[15]);
+XDEM_API int xdem_mbd_info(xdem_mbd* mbd, double* time, int* iterations, int* nconstraint);
+/* Lagrange multipliers (joints 5 each, drivers, normalisations). */
+XDEM_API int xdem_mbd_multipliers(xdem_mbd* mbd, double* lambda, int cap);
+
 #ifdef __cplusplus
 }
 #endif

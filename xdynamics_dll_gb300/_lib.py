@@ -88,6 +88,20 @@ _SIGS = {
     "xdem_adj_forward": ([vp, u32], i32),
     "xdem_adj_backward": ([vp] * 6, i32),
     "xdem_adj_info": ([vp, vp, vp, vp], i32),
+    "xdem_mbd_create": ([f64, f64, vp, vp], i32),
+    "xdem_mbd_destroy": ([vp], i32),
+    "xdem_mbd_set_tolerance": ([vp, f64], i32),
+    "xdem_mbd_add_body": ([vp, f64, vp, vp, vp, vp, vp, vp], i32),
+    "xdem_mbd_add_revolute": ([vp, i32, i32, vp, vp, vp], i32),
+    "xdem_mbd_add_translational": ([vp, i32, i32, vp, vp, vp], i32),
+    "xdem_mbd_add_rotation_driver": ([vp, i32, f64], i32),
+    "xdem_mbd_initialize": ([vp], i32),
+    "xdem_mbd_set_contact_wrench": ([vp, i32, vp], i32),
+    "xdem_mbd_step": ([vp, vp], i32),
+    "xdem_mbd_get_body": ([vp, i32, vp, vp, vp], i32),
+    "xdem_mbd_body_record": ([vp, i32, vp], i32),
+    "xdem_mbd_info": ([vp, vp, vp, vp], i32),
+    "xdem_mbd_multipliers": ([vp, vp, i32], i32),
 }
 
 

@@ -33,6 +33,7 @@ UNITS = {
     "xdem_adjoint.cu": ["-fmad=false"],
     "xdem_tune.cu": [],
     "xdem_io.cu": [],
+    "xdem_hht.cu": ["-fmad=false"],
 }
 
 

@@ -284,7 +284,11 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
     }
     model_f(c.prm.contact_model, fc, c.dt_f, cdist, sd0, sd1, rv, unit, Ft, Fn, fca);
     const V3<float> fsum = Fn + Ft;
-    const V3<float> mm = tcross(dcpr, fsum);
+    // moment dcpr x (Fn + Ft) with dcpr = r n and Fn parallel to n: only the
+    // tangential force turns the sphere.  Forming r (n x Ft) leaves out the
+    // FP32 residue of crossing two parallel vectors (~1e-7 of r |Fn|), which
+    // would otherwise be the whole moment of a contact without friction
+    const V3<float> mm = ir * tcross(unit, Ft);
     acc.f[0].add(fsum.x); acc.f[1].add(fsum.y); acc.f[2].add(fsum.z);
     acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
     if (c.rolling) {
@@ -676,7 +680,9 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
         V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
         model_f(p.contact_model, fc, c.dt_f, cd, sd0, sd1, dv, un, Ft, Fn, fca);
         mf = Fn + Ft;
-        const V3<float> mm = tcross(dcpr, mf);
+        // dcpr = r un is parallel to Fn: only Ft turns the sphere (no FP32
+        // residue of crossing parallel vectors)
+        const V3<float> mm = r * tcross(un, Ft);
         acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
         if (c.rolling) {
             acc.tm = acc.tm + mm;

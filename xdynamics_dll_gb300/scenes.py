@@ -416,6 +416,27 @@ def random_packed(n, r_min, r_max, box, seed, overlap=0.05, vel_scale=0.05, omeg
                  plane_body=[T.body_record() for _ in planes], name="random_packed")
 
 
+def cluster_mass_inertia(rloc, sub_r, rho):
+    """Mass and principal inertia of a clump of equal spheres at body-frame
+    offsets rloc [neach, 3], as xParticleManager::SetClusterMassAndInertia
+    (source/xdynamics_manager/xParticleManager.cpp:1071-1084) sets them:
+    m = neach rho 4/3 pi r^3 and J = sum over members of m_s (parallel-axis
+    terms of rloc) -- the members' own 2/5 m_s r^2 is computed there but not
+    added.  On an axis where that sum is zero (members in a row along it,
+    the clumps of the wheel testbed) the reference's value would leave the
+    Euler-parameter update dividing by zero; there, and only there, the
+    members' own 2/5 m_s r^2 is added.  Returns (mass, J3, axes that got the
+    members' own term)."""
+    rloc = np.asarray(rloc, float).reshape(-1, 3)
+    neach = rloc.shape[0]
+    m1 = rho * (4.0 / 3.0) * np.pi * sub_r ** 3
+    J3 = np.array([m1 * np.sum(rloc[:, 1] ** 2 + rloc[:, 2] ** 2), m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 2] ** 2),
+                   m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 1] ** 2)])
+    own = J3 == 0.0
+    J3 = np.where(own, (2.0 / 5.0) * m1 * sub_r ** 2 * neach, J3)
+    return m1 * neach, J3, own
+
+
 def cluster_bed(ncluster, neach=3, sub_r=2e-3, seed=7, rho=2500.0, E=1e7, nu=0.3, rest=0.5, fric=0.3,
                 dt=1e-5, spacing_factor=1.0, trough=(1.0, 0.3, 0.15), vel_scale=0.0, grid=(128, 128, 128),
                 origin=(-1.0, -1.0, -1.0), cell_size=None):
@@ -450,13 +471,8 @@ def cluster_bed(ncluster, neach=3, sub_r=2e-3, seed=7, rho=2500.0, E=1e7, nu=0.3
     pos = np.zeros((N, 4))
     pos[:, :3] = mem.reshape(-1, 3)
     pos[:, 3] = sub_r
-    m1 = rho * (4.0 / 3.0) * np.pi * sub_r ** 3
-    mass = np.full(ns, m1 * neach)
-    J3 = np.array([m1 * np.sum(rloc[:, 1] ** 2 + rloc[:, 2] ** 2), m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 2] ** 2),
-                   m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 1] ** 2)])
-    # a clump of spheres in a row has no inertia about its axis in this
-    # parallel-axis-only model; give that axis the spheres' own 2/5 m r^2
-    J3 = J3 + (2.0 / 5.0) * m1 * sub_r ** 2 * neach
+    m_c, J3, _ = cluster_mass_inertia(rloc, sub_r, rho)
+    mass = np.full(ns, m_c)
     inertia = np.tile(J3, ns)
     vel, acc, ep, ev, ea = _init_state(ns)
     ep = q.ravel().copy()
@@ -606,11 +622,8 @@ def wheel_testbed(ncluster=2_000_000, neach=3, sub_r=2e-3, rho=2500.0, E=1e7, nu
     cpos = np.zeros((ns, 4))
     cpos[:, :3] = cent
     cpos[:, 3] = sub_r
-    m1 = rho * (4.0 / 3.0) * np.pi * sub_r ** 3
-    mass = np.full(ns, m1 * neach)
-    J3 = np.array([m1 * np.sum(rloc[:, 1] ** 2 + rloc[:, 2] ** 2), m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 2] ** 2),
-                   m1 * np.sum(rloc[:, 0] ** 2 + rloc[:, 1] ** 2)])
-    J3 = J3 + (2.0 / 5.0) * m1 * sub_r ** 2 * neach  # as cluster_bed: a row of spheres gets its own spin inertia
+    m_c, J3, _ = cluster_mass_inertia(rloc, sub_r, rho)
+    mass = np.full(ns, m_c)
     inertia = np.tile(J3, ns)
     vel, acc, ep, ev, ea = _init_state(ns)
     ep = q.ravel().copy()
