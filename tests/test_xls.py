@@ -133,13 +133,16 @@ def test_workbook_scene_steps_as_the_oracle(oracle):
     sm = sim.Sim(sc, precision=0)
     s = kseq.state_arrays(sc)
     be = kseq.OracleBackend(oracle)
+    touched = 0
     for k in range(300):
         sm.step(1)
         kseq.sphere_step(be, sc, s, (), compat=0)
+        if k % 30 == 0:
+            cnt, ids, _ = sm.pairs(1)
+            assert kseq.pairs_equal(cnt, ids, s["pl_count"], s["pl_id"], 3) == sc.np_, k
+            touched += int(s["pl_count"].sum())
     st = sm.state()
     for key in ("pos", "vel", "ep", "ev"):
         scale = max(np.abs(s[key]).max(), 1e-300)
         assert np.abs(st[key] - s[key]).max() <= 1e-11 * scale, key
-    cnt, ids, _ = sm.pairs(1)
-    assert kseq.pairs_equal(cnt, ids, s["pl_count"], s["pl_id"], 3) == sc.np_
-    assert s["pl_count"].sum() > 0 and sm.status() == 0
+    assert touched > 0 and sm.status() == 0

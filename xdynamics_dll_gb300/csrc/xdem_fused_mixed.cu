@@ -253,7 +253,7 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
         acc.f[0].add(-cf * unit.x); acc.f[1].add(-cf * unit.y); acc.f[2].add(-cf * unit.z);
         if (cnt < MAX_P2P_COUNT) {
             c.pp_id_new[slot] = k;
-            reinterpret_cast<double2*>(c.pp_tsd_new)[slot] = make_double2(0.0, 0.0);
+            reinterpret_cast<float2*>(c.pp_tsd_new)[slot] = make_float2(0.f, 0.f);
             cnt++;
         } else {
             bits |= XDEM_ERR_P2P_OVERFLOW;
@@ -265,8 +265,9 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
     float sd0 = 0.f, sd1 = 0.f;
     for (unsigned int q = 0; q < old_count; ++q)
         if (old_id[q * NT] == k) {
-            const double2 t = reinterpret_cast<const double2*>(c.pp_tsd_old)[sid + q];
-            sd0 = d2f_rn(t.x); sd1 = d2f_rn(t.y);
+            // FP32 history (float2 slots in the double2 buffer)
+            const float2 t = reinterpret_cast<const float2*>(c.pp_tsd_old)[sid + q];
+            sd0 = t.x; sd1 = t.y;
             break;
         }
     const MatR<float> mr = matr(c.mpf[scene]);
@@ -298,7 +299,7 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
     }
     if (cnt < MAX_P2P_COUNT) {
         c.pp_id_new[slot] = k;
-        reinterpret_cast<double2*>(c.pp_tsd_new)[slot] = make_double2(f2d(sd0), f2d(sd1));
+        reinterpret_cast<float2*>(c.pp_tsd_new)[slot] = make_float2(sd0, sd1);
         cnt++;
     } else {
         bits |= XDEM_ERR_P2P_OVERFLOW;
@@ -1331,21 +1332,31 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
             const float lim = ipf.w + c.margin;
             return fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
         };
-        // one block-wide vote first: a block none of whose spheres is near
-        // any plane (almost every block of a large bed) writes zero wrench
-        // partials for every plane and skips the plane loop with its
-        // per-plane barriers -- what the loop would have written
-        bool run_planes = true;
+        // one block-wide vote first: which of the first 32 planes is any
+        // sphere of the block near?  A plane none is near gets zero wrench
+        // partials from this block with no barrier (what its reduction would
+        // write); only the others pay the reduction's barriers.  (In a bed
+        // numbered row by row every block reaches a side wall, so voting on
+        // "any plane" alone would skip nothing.)
+        __shared__ unsigned int near_mask_s;
+        unsigned int block_near = 0xffffffffu;
         if (!batched) {
-            bool any_near = false;
+            unsigned int mine = 0;
             if (live)
-                for (unsigned int k = kbeg; k < kend && !any_near; ++k) any_near = near_plane(k);
-            run_planes = __syncthreads_or(any_near ? 1 : 0) != 0;
-            if (!run_planes)
-                for (unsigned int w = threadIdx.x; w < 6u * c.nplane; w += NT)
-                    c.bsums[((size_t)(w / 6u) * c.nblocks + blockIdx.x) * 6 + w % 6u] = 0.0;
+                for (unsigned int k = kbeg; k < kend && k < 32u; ++k)
+                    if (near_plane(k)) mine |= 1u << k;
+            if (threadIdx.x == 0) near_mask_s = 0u;
+            __syncthreads();
+            mine = __reduce_or_sync(0xffffffffu, mine);
+            if ((threadIdx.x & 31u) == 0 && mine) atomicOr(&near_mask_s, mine);
+            __syncthreads();
+            block_near = near_mask_s;
         }
-        for (unsigned int k = kbeg; run_planes && k < kend; ++k) {
+        for (unsigned int k = kbeg; k < kend; ++k) {
+            if (!batched && k < 32u && !((block_near >> k) & 1u)) {
+                if (threadIdx.x < 6) c.bsums[((size_t)k * c.nblocks + blockIdx.x) * 6 + threadIdx.x] = 0.0;
+                continue;
+            }
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             bool touched = false;
             const bool near = !live || near_plane(k);

@@ -356,6 +356,12 @@ bool fused_path(const xdem_sim* s)
     return !s->cfg.launcher_path && s->cylinders.empty() && (!s->clusters || s->precision_mixed());
 }
 
+// The particle-pair tangential history of a mixed handle on the fused step
+// is stored as float2 (ds, previous s_dot) in the first half of its double2
+// buffer: the mixed kernels compute it in FP32, so the FP32 copy is exact
+// and halves its traffic.  The pair-list calls convert at the boundary.
+bool pp_history_f32(const xdem_sim* s) { return s->precision_mixed() && fused_path(s); }
+
 FusedArgs fused_args(xdem_sim* s)
 {
     FusedArgs a{};
@@ -1125,7 +1131,15 @@ XDEM_API int xdem_sim_get_pairs(xdem_sim* s, int kind, unsigned int* count, unsi
     cudaError_t e = cudaStreamSynchronize(s->st);
     if (e == cudaSuccess && count) e = cudaMemcpy(count, dc, n * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && ids) e = cudaMemcpy(ids, di, n * 4 * cap, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && tsd) e = cudaMemcpy(tsd, dt, n * 16 * cap, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && tsd) {
+        if (kind == 0 && pp_history_f32(s)) {
+            std::vector<float> f(n * cap * 2);
+            e = cudaMemcpy(f.data(), dt, f.size() * sizeof(float), cudaMemcpyDeviceToHost);
+            for (size_t i = 0; i < f.size(); ++i) tsd[i] = (double)f[i];
+        } else {
+            e = cudaMemcpy(tsd, dt, n * 16 * cap, cudaMemcpyDeviceToHost);
+        }
+    }
     return cerr(e);
 }
 
@@ -1171,7 +1185,16 @@ XDEM_API int xdem_sim_set_pairs(xdem_sim* s, int kind, const unsigned int* count
     cudaError_t e = cudaStreamSynchronize(s->st);
     if (e == cudaSuccess) e = cudaMemcpy(dc, count, n * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(di, ids, n * 4 * cap, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(dt, tsd, n * 16 * cap, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        if (kind == 0 && pp_history_f32(s)) {
+            // rounded to nearest, as the mixed kernels round a double history
+            std::vector<float> f(n * cap * 2);
+            for (size_t i = 0; i < f.size(); ++i) f[i] = (float)tsd[i];
+            e = cudaMemcpy(dt, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+        } else {
+            e = cudaMemcpy(dt, tsd, n * 16 * cap, cudaMemcpyHostToDevice);
+        }
+    }
     fused_invalidate(s->fs);
     return cerr(e);
 }
