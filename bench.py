@@ -42,13 +42,17 @@ UNIT = "particle-steps/s"
 # state array read once (pos 32, vel 24, acc 24, ep 32, ev 32, ea 32, mass 8,
 # inertia 24 = 208) and written once (pos 32, vel 24, acc 24, ep 32, ev 32,
 # ea 32 = 176), the next cell hash + index (8), the pair count (read + write
-# 8) and 40 bytes per stored contact (id 4 + history 16, read + write).  The
-# whole step adds the grid's 28 bytes (sort pass 16, sorted index 4, cell
-# ranges 8): 428 + 40 c.  The force hand-off between the two kernels
-# (32 B written, 32 B read) is an implementation cost, not counted.
+# 8) and, per stored contact, its id (4) and tangential history read and
+# written: 16-byte FP64 history in the FP64 form (40 per contact), 8-byte
+# FP32 history in the mixed form, which computes the history in FP32 and
+# keeps it so (24 per contact).  The whole step adds the grid's 28 bytes
+# (sort pass 16, sorted index 4, cell ranges 8): 428 + 24 c for the mixed
+# form.  The force hand-off between the two kernels (32 B written, 32 B
+# read) is an implementation cost, not counted.
 B_CONTACT_FIXED = 400.0
 B_STEP_FIXED = 428.0
-B_PER_CONTACT = 40.0
+B_PER_CONTACT = 24.0        # mixed form (FP32 history)
+B_PER_CONTACT_FP64 = 40.0   # FP64 form
 
 
 def load_peaks():
@@ -779,6 +783,7 @@ def main():
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
             "traffic": traffic_per_sphere * n if traffic_per_sphere else None,
             "algorithmic_bytes_per_launch": b_contact,
+            "bytes_model": "400 + 24 c per sphere (mixed form: 8-byte FP32 tangential history per contact)",
             "contact_kernel_ms": rmx["contact_ms"], "traffic_source": tfile}
     step_bw = (B_STEP_FIXED + B_PER_CONTACT * cbar) * n / (secsx / args.steps) / 1e9
     out = {
@@ -788,7 +793,10 @@ def main():
         "config": workload_config(scene),
         "replicas": ws, "advance_steps": args.advance,
         "fp64": {"value": value64, "ms_per_step": 1e3 * secs64 / args.steps, "contact_kernel_ms": r64["contact_ms"],
-                 "mixed_over_fp64": value / value64},
+                 "mixed_over_fp64": value / value64,
+                 "contact_hbm_frac": (B_CONTACT_FIXED + B_PER_CONTACT_FP64 * r64["ncontact"] / n) * n /
+                                     (r64["contact_ms"] * 1e-3) / 1e9 / peak,
+                 "bytes_model": "400 + 40 c per sphere (16-byte FP64 history)"},
         "contacts_per_sphere": cbar,
         "step_hbm": {"achieved": step_bw, "peak": peak, "frac": step_bw / peak, "unit": "GB/s",
                      "bytes_per_sphere": B_STEP_FIXED + B_PER_CONTACT * cbar},

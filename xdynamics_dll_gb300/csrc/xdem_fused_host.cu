@@ -791,8 +791,10 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
         // body's contacts -- planes: the body kernel (sorted entries, or
         // clusters); meshes: the pair kernel (sorted entries on the walk,
         // spheres with candidate lists); the row stride covers both
+        // (the sphere body kernel writes one row per warp, the cluster body
+        // kernel one per block)
         const unsigned int nt_b = fs.tune.nt_bodies, nt_p = fs.tune.nt_pairs;
-        rows_plane = clusters ? (a.cl.ns + nt_b - 1) / nt_b : (n + nt_b - 1) / nt_b;
+        rows_plane = clusters ? (a.cl.ns + nt_b - 1) / nt_b : (n + 31) / 32;
         rows_mesh = use_list ? (np + nt_p - 1) / nt_p : (n + nt_p - 1) / nt_p;
         c.nblocks = std::max(rows_plane, rows_mesh);
     }

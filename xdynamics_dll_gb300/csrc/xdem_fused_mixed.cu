@@ -187,6 +187,31 @@ __device__ __forceinline__ void emit_body_f(const float f6[6], bool any, double*
     }
 }
 
+// Warp sum of six per-thread FP32 values into out[0..5] (FP64), written by
+// lane 0: the compensated butterflies of emit_body_f without its combine
+// across warps, so no block barrier.  Every lane of the warp calls it.
+__device__ __forceinline__ void emit_warp_f(const float f6[6], bool any, double* out)
+{
+    const int lane = threadIdx.x & 31;
+    if (!__any_sync(0xffffffffu, any)) {
+        if (lane < 6) out[lane] = 0.0;
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        float hi = f6[c], lo = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+            const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+            const df t = two_sum(hi, oh);
+            hi = t.hi;
+            lo = (lo + ol) + t.lo;
+        }
+        if (lane == 0) out[c] = f2d(hi) + f2d(lo);
+    }
+}
+
 // Per-sphere accumulators of the mixed kernel.
 struct Acc {
     CSum f[3], m[3];
@@ -1273,7 +1298,6 @@ __global__ void k_vl_roll(unsigned int* flag)
 template <unsigned int NT, unsigned int OCC>
 __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
 {
-    __shared__ float smf[(NT / 32) * 6 * 2];
     const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = oid < c.np;
     // the record's velocity + mass (B) and spin (C) are read only by a sphere
@@ -1332,31 +1356,9 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
             const float lim = ipf.w + c.margin;
             return fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
         };
-        // one block-wide vote first: which of the first 32 planes is any
-        // sphere of the block near?  A plane none is near gets zero wrench
-        // partials from this block with no barrier (what its reduction would
-        // write); only the others pay the reduction's barriers.  (In a bed
-        // numbered row by row every block reaches a side wall, so voting on
-        // "any plane" alone would skip nothing.)
-        __shared__ unsigned int near_mask_s;
-        unsigned int block_near = 0xffffffffu;
-        if (!batched) {
-            unsigned int mine = 0;
-            if (live)
-                for (unsigned int k = kbeg; k < kend && k < 32u; ++k)
-                    if (near_plane(k)) mine |= 1u << k;
-            if (threadIdx.x == 0) near_mask_s = 0u;
-            __syncthreads();
-            mine = __reduce_or_sync(0xffffffffu, mine);
-            if ((threadIdx.x & 31u) == 0 && mine) atomicOr(&near_mask_s, mine);
-            __syncthreads();
-            block_near = near_mask_s;
-        }
+        // wrench partials: one row per warp (no block barrier in the loop)
+        const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
         for (unsigned int k = kbeg; k < kend; ++k) {
-            if (!batched && k < 32u && !((block_near >> k) & 1u)) {
-                if (threadIdx.x < 6) c.bsums[((size_t)k * c.nblocks + blockIdx.x) * 6 + threadIdx.x] = 0.0;
-                continue;
-            }
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             bool touched = false;
             const bool near = !live || near_plane(k);
@@ -1378,7 +1380,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
                     acc.rs += o.rs;
                 }
             }
-            if (!batched) emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
+            if (!batched) emit_warp_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + wrow) * 6);
         }
         if (live) c.pl_count[oid] = pl_cnt;
     }

@@ -120,8 +120,9 @@ int ensure_tables(xdem_sim* s)
     A(s->k0, s->nentry); A(s->v0, s->nentry); A(s->k1, s->nentry); A(s->v1, s->nentry);
     A(s->hist, radix_hist_size(s->nentry));
     A(s->sorted_index, s->nentry);
-    // partial rows sized for the smallest block shape the tuner may pick
-    const unsigned int nb = blocks_for(s->nentry, 64);
+    // partial rows: one per warp (the mixed sphere body kernel writes one
+    // row per warp; every other emitter writes one per block of at least 64)
+    const unsigned int nb = blocks_for(s->nentry, 32);
     const size_t nbody = std::max<size_t>(s->bodies.size(), 1);
     // batched handles keep no body wrenches: no per-block partials
     A(s->bsums, (size_t)nb * 6 * (s->nscene > 1 ? 1 : nbody));
