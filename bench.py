@@ -372,6 +372,35 @@ def rebuild_timing(sm, torch, stream, steps=16):
                       f"{len(plain)} list steps"}
 
 
+def bench_stage(args, torch, local):
+    """Profiling aid for ncu: the dam break from the settled packing, one
+    handle (mixed, or FP64 with --stage-fp64) with the shapes of --shapes,
+    args.steps steps launched eagerly with the contact stage bracketed by
+    CUDA events; prints the mean stage time of the second half of the
+    steps.  A capture's -s / -k pick the launches to profile."""
+    from xdynamics_dll_gb300 import sim as S, types as T
+    scene = make_scene(args.n)
+    prec = T.XDEM_FP64 if args.stage_fp64 else T.XDEM_MIXED
+    sm = S.Sim(scene, precision=prec)
+    for k, pr in enumerate(scene.pairs):
+        sm.set_pairs(k, *pr)
+    if prec == T.XDEM_MIXED and args.shapes:
+        sm.set_tune(**{k: int(v) for k, v in json.loads(args.shapes).items() if k in T.Tune.SHAPE})
+    sm.set_profiling(True)
+    tot, half = 0.0, args.steps // 2
+    for i in range(args.steps):
+        sm.step(1)
+        _, ms, _ = sm.profile()
+        if i >= half:
+            tot += ms
+    torch.cuda.synchronize()
+    ke, nc = sm.energy()
+    print(json.dumps({"workload": "stage", "n": scene.np_, "precision": "fp64" if args.stage_fp64 else "mixed",
+                      "contact_stage_ms": tot / max(args.steps - half, 1), "contacts_per_sphere": nc / scene.np_,
+                      "status": sm.status(), "tune": sm.get_tune()}))
+    sm.close()
+
+
 def bench_sweep(args, torch, local):
     """The batched parameter sweep: 256 sphere drops with particle counts
     U{2000..60000}, radii U[1, 3] mm, friction U[0.1, 0.6], restitution
@@ -684,10 +713,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--workload", default="dambreak", choices=["dambreak", "sweep", "calibration", "wheel"],
+    ap.add_argument("--stage-fp64", action="store_true", help="stage workload: the FP64 handle")
+    ap.add_argument("--workload", default="dambreak", choices=["dambreak", "sweep", "calibration", "wheel", "stage"],
                     help="dambreak: the headline line; sweep: the batched 256-scene parameter sweep; "
                          "calibration: forward + adjoint of the column collapse; wheel: the wheel testbed "
-                         "of rigid clumps (mixed cluster step)")
+                         "of rigid clumps (mixed cluster step); stage: eager contact-stage steps of the dam "
+                         "break for profiling")
     ap.add_argument("--clusters", type=int, default=2_000_000, help="clumps of the wheel workload")
     ap.add_argument("--scenes", type=int, default=256, help="scenes of the sweep workload")
     ap.add_argument("--advance", type=int, default=0,
@@ -749,6 +780,10 @@ def main():
     if args.workload == "wheel":
         if rank == 0:
             bench_wheel(args, torch, local)
+        return
+    if args.workload == "stage":
+        if rank == 0:
+            bench_stage(args, torch, local)
         return
     scene = make_scene(args.n)
 
