@@ -141,7 +141,7 @@ struct FusedState {
     float* fA = nullptr;        // [np*4] particle-particle force, rolling resistance (original order)
     float* fB = nullptr;        // [np*4] particle-particle moment
     float* fC = nullptr;        // [np*4] rolling: sum of contact moments
-    // candidate lists (skin_div > 0): ids in any order, count (> kListCap:
+    // candidate lists (skin_div > 0): ids ascending, count (> kListCap:
     // overflowed, walk), FP32 centre at the build, rebuild flags [in, out]
     unsigned int* vl_ids = nullptr;  // [np * kListCap]
     unsigned int* vl_cnt = nullptr;  // [np]
