@@ -590,7 +590,8 @@ XDEM_API int xdem_adj_info(xdem_adj* adj, unsigned int* nprop, unsigned int* nst
  * they are added; xdem_mbd_initialize then solves the consistent
  * accelerations.  Host only: these calls touch no GPU.  Returns XDEM_OK or
  * XDEM_ERR_ARG (bad argument, singular system, or a step whose Newton loop
- * did not converge in 100 iterations). */
+ * did not converge in 100 iterations; a failed step leaves the bodies, the
+ * time and the multipliers as they were before it). */
 typedef struct xdem_mbd xdem_mbd;
 /* alpha in [-1/3, 0] (the reference uses -0.3); gravity may be NULL. */
 XDEM_API int xdem_mbd_create(double dt, double alpha, const double gravity[3], xdem_mbd** out);

@@ -151,3 +151,30 @@ def test_argument_checks(mbd):
         sys.add_revolute(0, 5, (0, 0, 0), (0, 0, 1))
     with pytest.raises(_lib.XdemError):
         sys.add_revolute(0, b, (0, 0, 0), (0, 0, 0))
+
+
+def test_failed_step_leaves_the_system_as_it_was(mbd):
+    """A Newton loop that cannot meet its tolerance (1e-300 sits below the
+    residual's rounding) fails after 100 iterations; the bodies, the time
+    and the multipliers stay at the last completed step, and the system
+    steps on once the tolerance is reachable again."""
+    dt = 1e-3
+    sys = mbd.Multibody(dt)
+    b = sys.add_body(2.0, (0.01, 0.01, 0.01), (0.3, -0.4, 0.0))
+    sys.add_revolute(0, b, (0.0, 0.0, 0.0), (0.0, 0.0, 1.0))
+    sys.initialize()
+    for _ in range(5):
+        sys.step()
+    before = [a.copy() for a in sys.body(b)]
+    t0, _, _ = sys.info()
+    lam0 = sys.multipliers().copy()
+    sys.set_tolerance(1e-300)
+    with pytest.raises(_lib.XdemError):
+        sys.step()
+    after = sys.body(b)
+    assert all(np.array_equal(x, y) for x, y in zip(before, after))
+    t1, _, _ = sys.info()
+    assert t1 == t0 and np.array_equal(sys.multipliers(), lam0)
+    sys.set_tolerance(1e-5)
+    sys.step()
+    assert sys.info()[0] == pytest.approx(t0 + dt)

@@ -581,6 +581,13 @@ XDEM_API int xdem_mbd_step(xdem_mbd* m, int* iterations)
     }
     for (int r = 0; r < nc; ++r) x[nd + r] = m->lambda[r];
     const double tn = m->t + dt;
+    // a step that fails leaves the system as it was before the call
+    const std::vector<Body> saved = m->bodies;
+    auto fail = [&](int its) {
+        m->bodies = saved;
+        if (iterations) *iterations = its;
+        return (int)XDEM_ERR_ARG;
+    };
     auto place = [&]() {
         for (size_t bb = 1; bb < m->bodies.size(); ++bb) {
             Body& B = m->bodies[bb];
@@ -596,10 +603,7 @@ XDEM_API int xdem_mbd_step(xdem_mbd* m, int* iterations)
     // ---- correction (xIntegratorHHT::CorrectionStep)
     int it = 0;
     while (true) {
-        if (++it > 100) {
-            if (iterations) *iterations = it - 1;
-            return XDEM_ERR_ARG;  // no convergence: the step is not taken further
-        }
+        if (++it > 100) return fail(it - 1);  // no convergence
         constraints(m, tn, Phi, &Jq);
         force_vector(m, f);
         // ee = F - Phi_q^T lambda - M q_dd / (1 + alpha) - pre; -Phi / (beta dt^2)
@@ -621,10 +625,7 @@ XDEM_API int xdem_mbd_step(xdem_mbd* m, int* iterations)
         for (int k = 0; k < n; ++k) e2 += ee[k] * ee[k];
         const double enorm = std::sqrt(e2);
         system_matrix(m, divalpha, x.data(), divalpha * b * dt * dt, Jq, L);
-        if (!solve(L, ee, n)) {
-            if (iterations) *iterations = it;
-            return XDEM_ERR_ARG;
-        }
+        if (!solve(L, ee, n)) return fail(it);
         for (int k = 0; k < n; ++k) x[k] += ee[k];
         place();
         if (enorm <= m->eps) break;
