@@ -1229,6 +1229,29 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
 // otherwise its contacts come from the list (a sphere whose list overflowed
 // walks; the cell sort is kept up to date for it).  Writes the same sums as
 // k_mixed_pairs for kernel 2.
+// The stencil walk of the list kernel (rebuild steps, and spheres whose list
+// overflowed) behind a call boundary: inlined, its staged-row loads set the
+// register allocation of the whole kernel and the list path spilled inside
+// its per-contact loop.  Apart, the list path keeps its own allocation and
+// the walk pays the call on the steps that need it.  Starts from empty sums
+// and returns them by value, like plane_call.
+struct WalkOut {
+    Acc acc;
+    unsigned int bits;
+};
+template <unsigned int NT>
+__device__ __noinline__ WalkOut walk_call(const ContactLaunch* cp, unsigned int oid, unsigned int gx, unsigned int gy,
+                                          unsigned int gz, float4 Ai, float4 Li, unsigned int Ti, float4 Bi, float4 Ci,
+                                          unsigned int* stage, unsigned int* old_id, bool rebuild)
+{
+    WalkOut o;
+    o.acc.tm = v3<float>(0.f, 0.f, 0.f);
+    o.acc.rs = 0.f;
+    o.bits = 0;
+    p2p_mixed<NT, 16>(*cp, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage, old_id, o.acc, o.bits, rebuild);
+    return o;
+}
+
 template <bool MESH, unsigned int NT, unsigned int OCC>
 __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
 {
@@ -1254,11 +1277,15 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_
     acc.rs = 0.f;
     unsigned int bits = 0;
     if (live) {
-        if (!rebuild && c.vl_cnt[oid] <= kListCap)
+        if (!rebuild && c.vl_cnt[oid] <= kListCap) {
             p2p_list<NT>(c, oid, Ai, Li, Ti, Bi, Ci, old_id + threadIdx.x, stage + threadIdx.x, acc, bits);
-        else
-            p2p_mixed<NT, 16>(c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x, old_id + threadIdx.x, acc,
-                              bits, rebuild);
+        } else {
+            // acc is still empty here: the walk's sums are the sphere's
+            const WalkOut w = walk_call<NT>(&c, oid, gx, gy, gz, Ai, Li, Ti, Bi, Ci, stage + threadIdx.x,
+                                            old_id + threadIdx.x, rebuild);
+            acc = w.acc;
+            bits |= w.bits;
+        }
     }
     // triangle meshes (impl:1930-2109): the cell table holds the mesh
     // spheres as of the last sort, and a moved mesh forces a sort
