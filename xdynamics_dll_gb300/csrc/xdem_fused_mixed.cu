@@ -38,6 +38,37 @@ __device__ __forceinline__ V3<float> qdiv(V3<float> a, float b)
 {
     return v3<float>(qdiv(a.x, b), qdiv(a.y, b), qdiv(a.z, b));
 }
+// Square root and quotient at the hardware approximation (sqrt.approx.f32,
+// __fdividef: relative error of a few 2^-23): for the contact constants,
+// the magnitudes of the contact model and the seed of the float-pair square
+// root, where an error of 1e-7 of the value is below the FP32 rounding the
+// contact force carries anyway; each saves the IEEE sequence's Newton steps
+// and special-case check in the per-contact loop.  The unit normal keeps
+// the IEEE quotient (qdiv above).
+__device__ __forceinline__ float sqrt_fast(float x)
+{
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float div_fast(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float len_fast(V3<float> a) { return sqrt_fast(tdot(a, a)); }
+
+// Contact constants of a pair (fconst_r of the FP64 form) with the fast
+// quotient and square root.
+__device__ __forceinline__ FC<float> fconst_f(const MatR<float>& m, int model, float ir, float jr, float im, float jm)
+{
+    FC<float> c;
+    c.eq_m = jm != 0.f ? div_fast(im * jm, im + jm) : im;
+    c.eq_r = jr != 0.f ? div_fast(ir * jr, ir + jr) : ir;
+    c.kn = (4.f / 3.f) * m.Eeq * sqrt_fast(c.eq_r);
+    c.vn = m.beta;
+    c.ks = model == 1 ? m.Seq8 : c.kn * m.sratio;
+    c.vs = m.vs1;
+    c.mu = m.fric;
+    return c;
+}
+
 __device__ __forceinline__ unsigned int umax(unsigned int a, unsigned int b) { return a > b ? a : b; }
 __device__ __forceinline__ unsigned int umin(unsigned int a, unsigned int b) { return a < b ? a : b; }
 
@@ -58,13 +89,16 @@ __device__ __forceinline__ df df_sqr(df a)
     const df p = two_prod(a.hi, a.hi);
     return fast_two_sum(p.hi, p.lo + 2.f * a.hi * a.lo);
 }
+// The seed s may be a few ulp off: the remainder a - s^2 is exact (two_prod,
+// Sterbenz) and the correction step r / 2s brings the pair to the float-pair
+// square root all the same.
 __device__ __forceinline__ df df_sqrt(df a)
 {
-    const float s = sqrtf(a.hi);
+    const float s = sqrt_fast(a.hi);
     if (!(s > 0.f)) return df{s, 0.f};
     const df p = two_prod(s, s);
     const float r = ((a.hi - p.hi) - p.lo) + a.lo;
-    return fast_two_sum(s, r * (0.5f / s));
+    return fast_two_sum(s, r * div_fast(0.5f, s));
 }
 // One component of the relative position of neighbour j from sphere i as a
 // float pair: (A_j + L_j) - (A_i + L_i) + step, with step = +-cell size or 0
@@ -121,28 +155,29 @@ __device__ __forceinline__ void model_f(int model, const FC<float>& c, float dt,
                                         float& dots_io, V3<float> dv, V3<float> unit, V3<float>& Ft, V3<float>& Fn,
                                         float fca)
 {
-    const float fsn = -c.kn * (cdist * sqrtf(cdist));
+    const float fsn = -c.kn * (cdist * sqrt_fast(cdist));
     const float dvn = tdot(dv, unit);
     Fn = (fsn + fca + c.vn * dvn) * unit;
     const V3<float> e = dv - dvn * unit;
     // an exactly zero tangential velocity is common (stacked spheres); skip
     // the square root's special-case path for it
     const float me2 = tdot(e, e);
-    const float mag_e = me2 == 0.f ? 0.f : sqrtf(me2);
+    const float mag_e = me2 == 0.f ? 0.f : sqrt_fast(me2);
     if (mag_e != 0.f) {
-        const V3<float> s_hat = qdiv(e, mag_e);
+        const float inv_e = div_fast(1.f, mag_e);
+        const V3<float> s_hat = v3<float>(e.x * inv_e, e.y * inv_e, e.z * inv_e);
         const float s_dot = tdot(dv, s_hat);
         const float ds = ds_io + dt * (s_dot + dots_io);
         ds_io = ds;
         dots_io = s_dot;
         float a;
         if (model == 1) {
-            const float S_t = c.ks * sqrtf(c.eq_r * cdist);
-            a = S_t * ds + c.vs * sqrtf(S_t * c.eq_m);
+            const float S_t = c.ks * sqrt_fast(c.eq_r * cdist);
+            a = S_t * ds + c.vs * sqrt_fast(S_t * c.eq_m);
         } else {
             a = c.ks * ds + c.vs * s_dot;
         }
-        const float b = c.mu * tlen(Fn);
+        const float b = c.mu * len_fast(Fn);
         Ft = (a < b ? a : b) * s_hat;
     }
 }
@@ -301,7 +336,7 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
     const V3<float> dcpr_j = dcpr - rp;
     const V3<float> rv = (v3<float>(Bj.x, Bj.y, Bj.z) + tcross(v3<float>(Cj.x, Cj.y, Cj.z), dcpr_j)) -
                          (v3<float>(Bi.x, Bi.y, Bi.z) + tcross(v3<float>(Ci.x, Ci.y, Ci.z), dcpr));
-    const FC<float> fc = fconst_r<float>(mr, c.prm.contact_model, ir, Aj.w, Bi.w, Bj.w);
+    const FC<float> fc = fconst_f(mr, c.prm.contact_model, ir, Aj.w, Bi.w, Bj.w);
     float fca = 0.f;
     if (coh) {
         const double fsn = -(double)fc.kn * ((double)cdist * sqrt((double)cdist));
@@ -696,7 +731,7 @@ __device__ __forceinline__ bool plane_mixed(const ContactLaunch& c, unsigned int
                 break;
             }
         const V3<float> dv = (b.v + tcross(b.om, dcpr_j)) - (ivel + tcross(iom, dcpr));
-        const FC<float> fc = fconst_r<float>(mr, p.contact_model, r, 0.f, im, member ? b.m : 0.f);
+        const FC<float> fc = fconst_f(mr, p.contact_model, r, 0.f, im, member ? b.m : 0.f);
         float fca = 0.f;
         if (mr.coh) {
             const double fsn = -(double)fc.kn * (cdd * sqrt(cdd));
@@ -870,7 +905,7 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
                 if (o_id[r] == hit.id) { sd0 = o_a[r]; sd1 = o_b[r]; break; }
             const V3<float> rc = cvt<float>(rpd);
             const V3<float> dv = (b.v + tcross(b.om, po2cp)) - (ivel + tcross(iom, rc));
-            const FC<float> fc = fconst_r<float>(mr, p.contact_model, (float)ir, 0.f, im, b.m);
+            const FC<float> fc = fconst_f(mr, p.contact_model, (float)ir, 0.f, im, b.m);
             float fca = 0.f;
             if (mr.coh) {
                 const double fsn = -(double)fc.kn * (cd * sqrt(cd));
@@ -1234,7 +1269,9 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs(const __grid_const
 // register allocation of the whole kernel and the list path spilled inside
 // its per-contact loop.  Apart, the list path keeps its own allocation and
 // the walk pays the call on the steps that need it.  Starts from empty sums
-// and returns them by value, like plane_call.
+// and returns them by value, like plane_call.  The unit is compiled without
+// implicit FMA contraction, so the call computes the same bits as the walk
+// inlined in k_mixed_pairs.
 struct WalkOut {
     Acc acc;
     unsigned int bits;
