@@ -311,11 +311,20 @@ def precision_check(scene, steps, torch, shapes):
     the packing `steps` steps; kinetic energy and stored contacts are read
     every steps/10 steps.  Returns the final and the largest relative KE
     difference, the contact-count difference, and the list rebuilds of the
-    mixed form per 1000 steps."""
+    mixed form per 1000 steps.  A third run, FP64 with one sphere's centre
+    moved by 1e-12 m, gives the floor any difference reaches over the same
+    steps in this chaotic flow (`ke_rel_diff_fp64_perturbed_*`)."""
     from xdynamics_dll_gb300 import types as T
     out = {}
-    for prec in (T.XDEM_MIXED, T.XDEM_FP64):
-        sm = new_sim(scene, prec)
+    for name, prec in (("mixed", T.XDEM_MIXED), ("fp64", T.XDEM_FP64), ("fp64_perturbed", T.XDEM_FP64)):
+        pos0 = scene.pos
+        if name == "fp64_perturbed":
+            scene.pos = pos0.copy()
+            scene.pos[4 * (scene.np_ // 2)] += 1e-12
+        try:
+            sm = new_sim(scene, prec)
+        finally:
+            scene.pos = pos0
         if prec == T.XDEM_MIXED and shapes:
             sm.set_tune(**{k: int(shapes[k]) for k in T.Tune.SHAPE})
         sm.set_graph(True)
@@ -325,14 +334,16 @@ def precision_check(scene, steps, torch, shapes):
             sm.step(steps // 10)
             trace.append(sm.energy())
         torch.cuda.synchronize()
-        out[prec] = dict(trace=trace, status=sm.status(), rebuilds=sm.list_rebuilds(),
+        out[name] = dict(trace=trace, status=sm.status(), rebuilds=sm.list_rebuilds(),
                          secs=time.perf_counter() - t0)
         sm.close()
-        log(f"precision check {'mixed' if prec == T.XDEM_MIXED else 'fp64'}: {out[prec]['secs']:.1f} s")
-    mx, fp = out[T.XDEM_MIXED], out[T.XDEM_FP64]
+        log(f"precision check {name}: {out[name]['secs']:.1f} s")
+    mx, fp, fq = out["mixed"], out["fp64"], out["fp64_perturbed"]
     rel = [abs(a[0] - b[0]) / b[0] for a, b in zip(mx["trace"], fp["trace"])]
+    floor = [abs(a[0] - b[0]) / b[0] for a, b in zip(fq["trace"], fp["trace"])]
     return {"steps": steps, "ke_fp64": fp["trace"][-1][0], "ke_mixed": mx["trace"][-1][0],
             "ke_rel_err_vs_fp64": rel[-1], "ke_rel_err_max_over_trace": max(rel),
+            "ke_rel_diff_fp64_perturbed_final": floor[-1], "ke_rel_diff_fp64_perturbed_max": max(floor),
             "contacts_fp64": fp["trace"][-1][1], "contacts_mixed": mx["trace"][-1][1],
             "contact_count_diff_vs_fp64": int(mx["trace"][-1][1]) - int(fp["trace"][-1][1]),
             "contact_count_rel_diff_max_over_trace": max(abs(int(a[1]) - int(b[1])) / b[1]
