@@ -573,6 +573,17 @@ XDEM_API int xdem_adj_forward(xdem_adj* adj, unsigned int nsteps);
  * at the end of the first segment's re-run. */
 XDEM_API int xdem_adj_backward(xdem_adj* adj, const double* dl_dpos, const double* dl_dvel, double* grad,
                                double* dl_dpos0, double* dl_dvel0);
+/* Forward mode of the same linearisation (an independent check of the
+ * adjoint): re-runs the trajectory of the last xdem_adj_forward from its
+ * first checkpoint and carries the derivative of the state along it in
+ * ndir <= 3 parameter directions at once.  dparam: HOST array [ndir][nprop]
+ * [4] of d(fric, rest, Ei, Ej) per contact property.  tpos, tvel: optional
+ * DEVICE arrays [ndir][np*3] receiving the derivative of the final
+ * positions and velocities in each direction.  For a loss L of the final
+ * state, dL/dx . tpos[k] equals grad . dparam[k] of xdem_adj_backward.
+ * Leaves the handle at the end of the trajectory; returns the re-run's
+ * status bits. */
+XDEM_API int xdem_adj_tangent(xdem_adj* adj, unsigned int ndir, const double* dparam, double* tpos, double* tvel);
 /* Properties (1 + planes), steps of the last forward, device bytes held. */
 XDEM_API int xdem_adj_info(xdem_adj* adj, unsigned int* nprop, unsigned int* nsteps, unsigned long long* bytes);
 

@@ -2,6 +2,9 @@
 // function f and a random cotangent ly, the directional derivative of
 // ly . f(x) along random directions d by central differences against
 // (VJP ly) . d.  Prints one line "name max_relative_error" per check.
+// The same forward pieces evaluated on dual numbers (the forward mode that
+// xdem_adj_tangent runs) give ly . (J d) directly: "name_jvp" lines compare
+// it with (VJP ly) . d and with the central differences.
 // Built and run by tests/test_adjoint_math.py (g++, no GPU).
 #include <cmath>
 #include <cstdio>
@@ -57,6 +60,66 @@ static double check(const char* name, const Vec& x, const Vec& scale, int nout, 
     return worst;
 }
 
+// Dual-number counterpart of check: for each random direction d the
+// tangent ly . (J d) of fd (the forward on Dual<1> inputs x + eps d) against
+// (VJP ly) . d and against central differences of f.
+using D1 = Dual<1>;
+using DVec = std::vector<D1>;
+using FwdD = std::function<void(const DVec&, DVec&)>;
+static double jvp_check(const char* name, const Vec& x, const Vec& scale, int nout, Fwd f, FwdD fd, Vjp vjp,
+                        int ndir = 12)
+{
+    Vec ly(nout);
+    for (int i = 0; i < nout; ++i) ly[i] = nrm();
+    Vec lx(x.size(), 0.0);
+    vjp(x, ly, lx);
+    double worst = 0.0;
+    for (int k = 0; k < ndir; ++k) {
+        Vec d(x.size());
+        for (size_t i = 0; i < x.size(); ++i) d[i] = scale[i] * nrm();
+        DVec xd(x.size()), yd(nout);
+        for (size_t i = 0; i < x.size(); ++i) {
+            xd[i] = D1(x[i]);
+            xd[i].d[0] = d[i];
+        }
+        fd(xd, yd);
+        double jv = 0.0, jmag = 0.0, vj = 0.0, vmag = 0.0;
+        for (int i = 0; i < nout; ++i) {
+            jv += ly[i] * yd[i].d[0];
+            jmag += std::fabs(ly[i] * yd[i].d[0]);
+        }
+        for (size_t i = 0; i < x.size(); ++i) {
+            vj += lx[i] * d[i];
+            vmag += std::fabs(lx[i] * d[i]);
+        }
+        const double h = 1e-6;
+        Vec xp = x, xm = x, yp(nout), ym(nout);
+        for (size_t i = 0; i < x.size(); ++i) {
+            xp[i] += h * d[i];
+            xm[i] -= h * d[i];
+        }
+        f(xp, yp);
+        f(xm, ym);
+        double fdd = 0.0;
+        for (int i = 0; i < nout; ++i) fdd += ly[i] * (yp[i] - ym[i]) / (2.0 * h);
+        // a cancelling directional derivative is judged against its terms
+        const double mag = std::max(std::max(jmag, vmag), 1e-300);
+        const double e1 = std::fabs(jv - vj) / mag;
+        const double e2 = std::min(std::fabs(jv - fdd) / std::max(std::fabs(jv), 1e-300),
+                                   10.0 * std::fabs(jv - fdd) / mag);
+        worst = std::max(worst, std::max(e1, e2));
+    }
+    std::printf("%s_jvp %.3e\n", name, worst);
+    return worst;
+}
+template <class T> static VT<T> gv(const std::vector<T>& x, int o) { return VT<T>{x[o], x[o + 1], x[o + 2]}; }
+template <class T> static QT<T> gq(const std::vector<T>& x, int o) { return QT<T>{x[o], x[o + 1], x[o + 2], x[o + 3]}; }
+template <class T> static void pv(std::vector<T>& y, int o, VT<T> v) { y[o] = v.x; y[o + 1] = v.y; y[o + 2] = v.z; }
+template <class T> static void pq(std::vector<T>& y, int o, QT<T> q)
+{
+    y[o] = q.x; y[o + 1] = q.y; y[o + 2] = q.z; y[o + 3] = q.w;
+}
+
 static Q getq(const Vec& x, int o) { return mkq(x[o], x[o + 1], x[o + 2], x[o + 3]); }
 static V getv(const Vec& x, int o) { return mkv(x[o], x[o + 1], x[o + 2]); }
 static void putq(Vec& y, int o, Q q) { y[o] = q.x; y[o + 1] = q.y; y[o + 2] = q.z; y[o + 3] = q.w; }
@@ -85,6 +148,15 @@ static void euler_checks()
                   addq_to(lx, 0, le);
                   addq_to(lx, 4, ld);
               });
+        jvp_check("ang_vel", x, Vec(8, 1.0), 3,
+                  [](const Vec& x, Vec& y) { putv(y, 0, ang_vel(getq(x, 0), getq(x, 4))); },
+                  [](const DVec& x, DVec& y) { pv(y, 0, ang_vel(gq(x, 0), gq(x, 4))); },
+                  [](const Vec& x, const Vec& ly, Vec& lx) {
+                      Q le = mkq(0, 0, 0, 0), ld = mkq(0, 0, 0, 0);
+                      ang_vel_vjp(getq(x, 0), getq(x, 4), getv(ly, 0), le, ld);
+                      addq_to(lx, 0, le);
+                      addq_to(lx, 4, ld);
+                  });
     }
     {
         Vec x(7);
@@ -99,6 +171,16 @@ static void euler_checks()
                   addv_to(lx, 0, lm);
                   addq_to(lx, 3, le);
               });
+        jvp_check("to_local", x, Vec(7, 1.0), 3,
+                  [](const Vec& x, Vec& y) { putv(y, 0, to_local(getv(x, 0), getq(x, 3))); },
+                  [](const DVec& x, DVec& y) { pv(y, 0, to_local(gv(x, 0), gq(x, 3))); },
+                  [](const Vec& x, const Vec& ly, Vec& lx) {
+                      V lm = mkv(0, 0, 0);
+                      Q le = mkq(0, 0, 0, 0);
+                      to_local_vjp(getv(x, 0), getq(x, 3), getv(ly, 0), lm, le);
+                      addv_to(lx, 0, lm);
+                      addq_to(lx, 3, le);
+                  });
     }
     for (int iso = 0; iso < 2; ++iso) {
         const V J = iso ? mkv(2.5e-9, 2.5e-9, 2.5e-9) : mkv(2.0e-9, 3.0e-9, 4.5e-9);
@@ -119,6 +201,17 @@ static void euler_checks()
                   addq_to(lx, 4, ld);
                   addv_to(lx, 8, ln);
               });
+        jvp_check(iso ? "uceom_isotropic" : "uceom", x, sc, 4,
+                  [J](const Vec& x, Vec& y) { putq(y, 0, uceom(J, getq(x, 0), getq(x, 4), getv(x, 8))); },
+                  [J](const DVec& x, DVec& y) { pq(y, 0, uceom(J, gq(x, 0), gq(x, 4), gv(x, 8))); },
+                  [J](const Vec& x, const Vec& ly, Vec& lx) {
+                      Q le = mkq(0, 0, 0, 0), ld = mkq(0, 0, 0, 0);
+                      V ln = mkv(0, 0, 0);
+                      uceom_vjp(J, getq(x, 0), getq(x, 4), getv(x, 8), getq(ly, 0), le, ld, ln);
+                      addq_to(lx, 0, le);
+                      addq_to(lx, 4, ld);
+                      addv_to(lx, 8, ln);
+                  });
         // the torque recovered from q
         const Q e = getq(x, 0), d = getq(x, 4);
         const V n = getv(x, 8);
@@ -135,6 +228,13 @@ static void euler_checks()
                   normalize_vjp(getq(x, 0), getq(ly, 0), le);
                   addq_to(lx, 0, le);
               });
+        jvp_check("normalize", x, Vec(4, 1.0), 4, [](const Vec& x, Vec& y) { putq(y, 0, normalize(getq(x, 0))); },
+                  [](const DVec& x, DVec& y) { pq(y, 0, normalize(gq(x, 0))); },
+                  [](const Vec& x, const Vec& ly, Vec& lx) {
+                      Q le = mkq(0, 0, 0, 0);
+                      normalize_vjp(getq(x, 0), getq(ly, 0), le);
+                      addq_to(lx, 0, le);
+                  });
     }
 }
 
@@ -186,6 +286,30 @@ static void pp_unpack(const PPCase& pc, const Vec& x, Body& bi, Body* nb, double
         nb[s].r = pc.rj[s]; nb[s].m = sphere_mass(pc.rj[s]);
         ds0[s] = x[o + 9]; dots0[s] = x[o + 10];
     }
+}
+
+// pp_sphere_fwd on x in the scalar type T (the layout of pp_unpack).
+template <class T>
+static void pp_eval(const PPCase& pc, int model, double dt, const std::vector<T>& x, std::vector<T>& y)
+{
+    BodyT<T> bi, nb[kMaxPairs];
+    T ds0[kMaxPairs], dots0[kMaxPairs], ds1[kMaxPairs], dots1[kMaxPairs];
+    bi.x = gv(x, 0); bi.v = gv(x, 3); bi.w = gv(x, 6);
+    bi.r = pc.ri; bi.m = sphere_mass(pc.ri);
+    for (int s = 0; s < pc.n; ++s) {
+        const int o = 9 + 11 * s;
+        nb[s].x = gv(x, o); nb[s].v = gv(x, o + 3); nb[s].w = gv(x, o + 6);
+        nb[s].r = pc.rj[s]; nb[s].m = sphere_mass(pc.rj[s]);
+        ds0[s] = x[o + 9]; dots0[s] = x[o + 10];
+    }
+    const int k = 9 + 11 * pc.n;
+    MatT<T> m;
+    m.Eeq = x[k]; m.Seq8 = x[k + 1]; m.beta = x[k + 2]; m.vs1 = x[k + 3]; m.fric = x[k + 4]; m.sratio = T(0.3);
+    VT<T> F = vzero<T>(), M = vzero<T>();
+    pp_sphere_fwd(model, dt, m, bi, nb, ds0, dots0, pc.n, F, M, ds1, dots1);
+    pv(y, 0, F);
+    pv(y, 3, M);
+    for (int s = 0; s < pc.n; ++s) { y[6 + s] = ds1[s]; y[6 + pc.n + s] = dots1[s]; }
 }
 
 static void pp_check(const char* name, int model, bool carry)
@@ -285,6 +409,24 @@ static void pp_check(const char* name, int model, bool carry)
         std::printf("# %s stick %d slip %d kept %d\n", name, stick, slip, kept);
     }
     check(name, x, sc, nout, f, vjp);
+    jvp_check(name, x, sc, nout, f, [pc, model, dt](const DVec& x, DVec& y) { pp_eval(pc, model, dt, x, y); }, vjp);
+}
+
+// plane_contact_fwd_t on x in the scalar type T (the layout of plane_check).
+template <class T>
+static void plane_eval(const PlaneContact& pc, int model, double r, double dt, const std::vector<T>& x,
+                       std::vector<T>& y)
+{
+    MatT<T> m;
+    m.Eeq = x[11]; m.Seq8 = x[12]; m.beta = x[13]; m.vs1 = x[14]; m.fric = x[15]; m.sratio = T(0.3);
+    BodyT<T> bi{gv(x, 0), gv(x, 3), gv(x, 6), r, sphere_mass(r)};
+    VT<T> F = vzero<T>(), M = vzero<T>();
+    T ds1, dots1;
+    plane_contact_fwd_t(model, dt, pc, m, bi, x[9], x[10], F, M, ds1, dots1);
+    pv(y, 0, F);
+    pv(y, 3, M);
+    y[6] = ds1;
+    y[7] = dots1;
 }
 
 static void plane_check(const char* name, int model, V pos)
@@ -344,6 +486,8 @@ static void plane_check(const char* name, int model, V pos)
         add_mat(lx, 11, g);
     };
     check(name, x, sc, 8, f, vjp);
+    jvp_check(name, x, sc, 8, f, [pc, model, r, dt](const DVec& x, DVec& y) { plane_eval(pc, model, r, dt, x, y); },
+              vjp);
 }
 
 int main()

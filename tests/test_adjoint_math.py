@@ -8,7 +8,8 @@ rotation, the Euler-parameter acceleration (anisotropic and isotropic
 inertia) and the torque recovered from it, normalisation, a sphere's
 particle-particle contacts (Hertz-Mindlin and DHS, stick and slip, a contact
 that keeps the previous tangential force) and plane contacts in the face,
-edge and corner regions.
+edge and corner regions.  The same forward pieces evaluated on dual numbers
+(forward mode) are checked against the VJPs and the differences too.
 """
 import os
 import shutil
@@ -42,6 +43,18 @@ def test_all_vjps_match_central_differences(results):
     errs, _ = results
     expected = {"ang_vel", "to_local", "uceom", "uceom_isotropic", "normalize", "pp_hm", "pp_dhs", "pp_hm_kept_ft",
                 "plane_face_hm", "plane_face_dhs", "plane_edge_hm", "plane_corner_hm"}
+    assert expected <= set(errs)
+    bad = {k: v for k, v in errs.items() if k in expected and not v < 1e-6}
+    assert not bad, bad
+
+
+def test_dual_number_tangents_match_vjps_and_differences(results):
+    """The forward pieces on dual numbers (the forward mode the tangent
+    kernels run): ly . (J d) against (VJP ly) . d and central differences."""
+    errs, _ = results
+    expected = {k + "_jvp" for k in ("ang_vel", "to_local", "uceom", "uceom_isotropic", "normalize", "pp_hm", "pp_dhs",
+                                     "pp_hm_kept_ft", "plane_face_hm", "plane_face_dhs", "plane_edge_hm",
+                                     "plane_corner_hm")}
     assert expected <= set(errs)
     bad = {k: v for k, v in errs.items() if k in expected and not v < 1e-6}
     assert not bad, bad

@@ -87,6 +87,7 @@ _SIGS = {
     "xdem_adj_destroy": ([vp], i32),
     "xdem_adj_forward": ([vp, u32], i32),
     "xdem_adj_backward": ([vp] * 6, i32),
+    "xdem_adj_tangent": ([vp, u32, vp, vp, vp], i32),
     "xdem_adj_info": ([vp, vp, vp, vp], i32),
     "xdem_mbd_create": ([f64, f64, vp, vp], i32),
     "xdem_mbd_destroy": ([vp], i32),

@@ -79,6 +79,22 @@ class Adjoint:
                    "xdem_adj_backward")
         return g.reshape(nprop, 4), out0[0], out0[1]
 
+    def tangent(self, dparam, velocities=False):
+        """Forward-mode derivative of the final state along the stored
+        trajectory (xdem_adj_tangent).  dparam: [ndir, nprop, 4] (ndir <= 3)
+        of d(fric, rest, Ei, Ej) per contact property.  Returns the
+        derivative of the final positions, a CUDA float64 tensor [ndir, np,
+        3] (and of the velocities with velocities=True)."""
+        n = self.sim.scene.np_
+        d = np.ascontiguousarray(dparam, dtype=np.float64)
+        if d.ndim != 3 or d.shape[1:] != (self.info()[0], 4) or not 1 <= d.shape[0] <= 3:
+            raise ValueError("dparam is [ndir <= 3, nprop, 4]")
+        tp = torch.empty((d.shape[0], n, 3), dtype=torch.float64, device="cuda")
+        tv = torch.empty_like(tp) if velocities else None
+        _lib.check(self.L.xdem_adj_tangent(self.h, d.shape[0], C.c_void_p(d.ctypes.data), _dptr(tp), _dptr(tv)),
+                   "xdem_adj_tangent")
+        return (tp, tv) if velocities else tp
+
 
 def with_parameters(scene, fric, rest, young):
     """A copy of `scene` whose contact properties all use friction `fric`,

@@ -20,6 +20,15 @@
 //                   (impl:32-41, 135-147).
 // The math and its VJPs are in xdem_adjoint.cuh.  Everything is FP64 and
 // deterministic: block sums have a fixed order and no atomics are used.
+//
+// xdem_adj_tangent is the forward mode of the same linearisation, as an
+// independent check of the adjoint: it re-runs the stored trajectory from
+// its first checkpoint and carries the derivative of the state along it in
+// up to kTanDirs parameter directions at once, with three kernels per step
+// (position half, contacts, velocity half) that evaluate the header's
+// forward pieces on dual numbers.  Its material derivatives come from
+// central differences of getConstant (make_mat_pair) on the host, not from
+// the chain rule the adjoint's gradients go through.
 // The unit is compiled with -fmad=false so the recomputed overlaps round
 // exactly as the forward step's did.
 #include <cuda_runtime.h>
@@ -378,6 +387,207 @@ __global__ void k_adj_gather(AdjArgs A, Slab S0, Slab S1)
     sq4(A.lea, j, lea0);
 }
 
+// ---------------------------------------------------------------- forward mode
+constexpr int kTanDirs = 3;
+using DT = adj::Dual<kTanDirs>;
+
+// Tangent arrays hold kTanDirs values per component: component c of sphere
+// i, direction k at [(i * ncomp + c) * kTanDirs + k].
+struct TanArgs {
+    unsigned int np, nplane;
+    int model, vel_compat;
+    double dt, h2;
+    const double *mass, *inertia;
+    const adj::Mat* mat;            // [nprop] values
+    const double* tmat;             // [nprop][5: Eeq, Seq8, beta, vs1, fric][kTanDirs]
+    const adj::PlaneContact* planes;
+    const unsigned int* plane_pid;
+    double *tx, *tv, *ta, *te, *ted, *tea;  // state tangents, n -> n+1 in place
+    double *tF, *tM, *Mv;                   // this step's force and moment tangents, moment values
+    const double* tpp_old;                  // [np * 12 * 2][kTanDirs] history tangents of lists n
+    double* tpp_new;                        // ... of lists n+1
+    const double* tpl_old;
+    double* tpl_new;
+};
+
+__device__ __forceinline__ DT dual_of(double v, const double* t)
+{
+    DT r(v);
+    for (int k = 0; k < kTanDirs; ++k) r.d[k] = t[k];
+    return r;
+}
+__device__ __forceinline__ void put_tan(double* t, const DT& x)
+{
+    for (int k = 0; k < kTanDirs; ++k) t[k] = x.d[k];
+}
+__device__ __forceinline__ adj::VT<DT> dv3(const double* val, size_t vi, const double* tan, size_t ti)
+{
+    return adj::VT<DT>{dual_of(val[vi], tan + ti * kTanDirs), dual_of(val[vi + 1], tan + (ti + 1) * kTanDirs),
+                       dual_of(val[vi + 2], tan + (ti + 2) * kTanDirs)};
+}
+__device__ __forceinline__ adj::QT<DT> dq4(const double* val, size_t vi, const double* tan, size_t ti)
+{
+    return adj::QT<DT>{dual_of(val[vi], tan + ti * kTanDirs), dual_of(val[vi + 1], tan + (ti + 1) * kTanDirs),
+                       dual_of(val[vi + 2], tan + (ti + 2) * kTanDirs),
+                       dual_of(val[vi + 3], tan + (ti + 3) * kTanDirs)};
+}
+__device__ __forceinline__ void put3(double* tan, size_t ti, const adj::VT<DT>& v)
+{
+    put_tan(tan + ti * kTanDirs, v.x);
+    put_tan(tan + (ti + 1) * kTanDirs, v.y);
+    put_tan(tan + (ti + 2) * kTanDirs, v.z);
+}
+__device__ __forceinline__ void put4(double* tan, size_t ti, const adj::QT<DT>& q)
+{
+    put_tan(tan + ti * kTanDirs, q.x);
+    put_tan(tan + (ti + 1) * kTanDirs, q.y);
+    put_tan(tan + (ti + 2) * kTanDirs, q.z);
+    put_tan(tan + (ti + 3) * kTanDirs, q.w);
+}
+__device__ __forceinline__ adj::MatT<DT> dual_mat(const TanArgs& T, unsigned int p)
+{
+    const adj::Mat& m = T.mat[p];
+    const double* t = T.tmat + (size_t)p * 5 * kTanDirs;
+    adj::MatT<DT> r;
+    r.Eeq = dual_of(m.Eeq, t);
+    r.Seq8 = dual_of(m.Seq8, t + kTanDirs);
+    r.beta = dual_of(m.beta, t + 2 * kTanDirs);
+    r.vs1 = dual_of(m.vs1, t + 3 * kTanDirs);
+    r.sratio = DT(m.sratio);
+    r.fric = dual_of(m.fric, t + 4 * kTanDirs);
+    return r;
+}
+
+// Position half of step n -> n+1: x1 = x0 + dt v0 + h a0, e1 = normalize(e0
+// + dt e_dot0 + h e_ddot0); tx and te become those of state n+1.
+__global__ void k_tan_position(TanArgs T, Slab S0)
+{
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= T.np) return;
+    using namespace adj;
+    const VT<DT> x0 = dv3(S0.pos, 4 * (size_t)j, T.tx, 3 * (size_t)j);
+    const VT<DT> v0 = dv3(S0.vel, 3 * (size_t)j, T.tv, 3 * (size_t)j);
+    const VT<DT> a0 = dv3(S0.acc, 3 * (size_t)j, T.ta, 3 * (size_t)j);
+    put3(T.tx, 3 * (size_t)j, (x0 + T.dt * v0) + T.h2 * a0);
+    const QT<DT> e0 = dq4(S0.ep, 4 * (size_t)j, T.te, 4 * (size_t)j);
+    const QT<DT> d0 = dq4(S0.ev, 4 * (size_t)j, T.ted, 4 * (size_t)j);
+    const QT<DT> q0 = dq4(S0.ea, 4 * (size_t)j, T.tea, 4 * (size_t)j);
+    put4(T.te, 4 * (size_t)j, normalize((e0 + T.dt * d0) + T.h2 * q0));
+}
+
+// Sphere i as the contacts of step n -> n+1 see it: centre and Euler
+// parameters of state n+1, velocities of state n.
+__device__ __forceinline__ adj::BodyT<DT> tan_body(const TanArgs& T, const Slab& S0, const Slab& S1, unsigned int i)
+{
+    adj::BodyT<DT> b;
+    b.x = dv3(S1.pos, 4 * (size_t)i, T.tx, 3 * (size_t)i);
+    b.r = S1.pos[4 * (size_t)i + 3];
+    b.v = dv3(S0.vel, 3 * (size_t)i, T.tv, 3 * (size_t)i);
+    b.w = adj::ang_vel(dq4(S1.ep, 4 * (size_t)i, T.te, 4 * (size_t)i),
+                       dq4(S0.ev, 4 * (size_t)i, T.ted, 4 * (size_t)i));
+    b.m = T.mass[i];
+    return b;
+}
+
+// Contacts of step n -> n+1 for sphere i on dual numbers: the particle pairs
+// of list n+1 in list order with the history each carried from list n, then
+// the planes with the in-place slot rule of the forward step.
+__global__ void __launch_bounds__(kAdjThreads) k_tan_contacts(TanArgs T, Slab S0, Slab S1)
+{
+    using namespace adj;
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T.np) return;
+    const BodyT<DT> bi = tan_body(T, S0, S1, i);
+    VT<DT> F = vzero<DT>(), M = vzero<DT>();
+    if (S1.ppc) {
+        const size_t sid = (size_t)i * MAX_P2P_COUNT;
+        const int n = (int)min(S1.ppc[i], (unsigned int)MAX_P2P_COUNT);
+        const int n_old = (int)min(S0.ppc[i], (unsigned int)MAX_P2P_COUNT);
+        BodyT<DT> nb[kMaxPairs];
+        DT ds0[kMaxPairs], dots0[kMaxPairs], ds1[kMaxPairs], dots1[kMaxPairs];
+        for (int s = 0; s < n; ++s) {
+            const unsigned int j = S1.ppi[sid + s];
+            nb[s] = tan_body(T, S0, S1, j);
+            ds0[s] = DT(0.0);
+            dots0[s] = DT(0.0);
+            for (int q = 0; q < n_old; ++q)
+                if (S0.ppi[sid + q] == j) {
+                    ds0[s] = dual_of(S0.ppt[2 * (sid + q)], T.tpp_old + 2 * (sid + q) * kTanDirs);
+                    dots0[s] = dual_of(S0.ppt[2 * (sid + q) + 1], T.tpp_old + (2 * (sid + q) + 1) * kTanDirs);
+                    break;
+                }
+        }
+        pp_sphere_fwd(T.model, T.dt, dual_mat(T, 0), bi, nb, ds0, dots0, n, F, M, ds1, dots1);
+        for (int s = 0; s < (int)MAX_P2P_COUNT; ++s) {
+            const DT a = s < n ? ds1[s] : DT(0.0), b = s < n ? dots1[s] : DT(0.0);
+            put_tan(T.tpp_new + 2 * (sid + s) * kTanDirs, a);
+            put_tan(T.tpp_new + (2 * (sid + s) + 1) * kTanDirs, b);
+        }
+    }
+    if (S1.plc) {
+        const size_t pid0 = (size_t)i * MAX_P2PL_COUNT;
+        const int cnt = (int)min(S1.plc[i], (unsigned int)MAX_P2PL_COUNT);
+        // slot contents as the step walks the planes: ids and histories of
+        // list n, overwritten slot by slot by this step's contacts
+        unsigned int cur_id[MAX_P2PL_COUNT];
+        DT cur_ds[MAX_P2PL_COUNT], cur_dots[MAX_P2PL_COUNT];
+        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q) {
+            cur_id[q] = S0.pli[pid0 + q];
+            cur_ds[q] = dual_of(S0.plt[2 * (pid0 + q)], T.tpl_old + 2 * (pid0 + q) * kTanDirs);
+            cur_dots[q] = dual_of(S0.plt[2 * (pid0 + q) + 1], T.tpl_old + (2 * (pid0 + q) + 1) * kTanDirs);
+        }
+        for (int s = 0; s < cnt; ++s) {
+            const unsigned int pid = S1.pli[pid0 + s];
+            int k = -1;
+            for (unsigned int p = 0; p < T.nplane; ++p)
+                if (T.plane_pid[p] == pid) { k = (int)p; break; }
+            DT ds0(0.0), dots0(0.0);
+            for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q)
+                if (cur_id[q] == pid) { ds0 = cur_ds[q]; dots0 = cur_dots[q]; break; }
+            DT ds1 = ds0, dots1 = dots0;
+            if (k >= 0)
+                plane_contact_fwd_t(T.model, T.dt, T.planes[k], dual_mat(T, 1 + k), bi, ds0, dots0, F, M, ds1, dots1);
+            cur_id[s] = pid;
+            cur_ds[s] = ds1;
+            cur_dots[s] = dots1;
+        }
+        for (int q = 0; q < (int)MAX_P2PL_COUNT; ++q) {
+            put_tan(T.tpl_new + 2 * (pid0 + q) * kTanDirs, cur_ds[q]);
+            put_tan(T.tpl_new + (2 * (pid0 + q) + 1) * kTanDirs, cur_dots[q]);
+        }
+    }
+    put3(T.tF, 3 * (size_t)i, F);
+    put3(T.tM, 3 * (size_t)i, M);
+    T.Mv[3 * (size_t)i] = M.x.v;
+    T.Mv[3 * (size_t)i + 1] = M.y.v;
+    T.Mv[3 * (size_t)i + 2] = M.z.v;
+}
+
+// Velocity half of step n -> n+1: a1 = F / m + g, v1 = v0 + dt/2 (a0 + a1)
+// (v1 = v0 in the velocity-compat mode), q = uceom(J, e1, e_dot0, A(e1)^T M),
+// e_dot1 = e_dot0 + dt/2 (e_ddot0 + q), e_ddot1 = q.
+__global__ void k_tan_velocity(TanArgs T, Slab S0, Slab S1)
+{
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= T.np) return;
+    using namespace adj;
+    const double hdt = 0.5 * T.dt, inv = 1.0 / T.mass[i];
+    const VT<DT> F = dv3(S1.acc, 3 * (size_t)i, T.tF, 3 * (size_t)i);  // value unused: only tangents flow
+    const VT<DT> a1 = inv * F;
+    const VT<DT> v0 = dv3(S0.vel, 3 * (size_t)i, T.tv, 3 * (size_t)i);
+    const VT<DT> a0 = dv3(S0.acc, 3 * (size_t)i, T.ta, 3 * (size_t)i);
+    put3(T.tv, 3 * (size_t)i, T.vel_compat ? v0 : v0 + hdt * (a0 + a1));
+    put3(T.ta, 3 * (size_t)i, a1);
+    const V J = mkv(T.inertia[3 * (size_t)i], T.inertia[3 * (size_t)i + 1], T.inertia[3 * (size_t)i + 2]);
+    const QT<DT> e1 = dq4(S1.ep, 4 * (size_t)i, T.te, 4 * (size_t)i);
+    const QT<DT> d0 = dq4(S0.ev, 4 * (size_t)i, T.ted, 4 * (size_t)i);
+    const QT<DT> q0 = dq4(S0.ea, 4 * (size_t)i, T.tea, 4 * (size_t)i);
+    const VT<DT> M = dv3(T.Mv, 3 * (size_t)i, T.tM, 3 * (size_t)i);
+    const QT<DT> q = uceom(J, e1, d0, to_local(M, e1));
+    put4(T.ted, 4 * (size_t)i, d0 + hdt * (q0 + q));
+    put4(T.tea, 4 * (size_t)i, q);
+}
+
 }  // namespace
 
 struct xdem_adj {
@@ -397,6 +607,10 @@ struct xdem_adj {
     adj::PlaneContact* d_planes = nullptr;
     unsigned int* d_pid = nullptr;
     std::vector<device_contact_property> cps;  // [nprop] properties the forward ran with
+    // forward mode (xdem_adj_tangent)
+    double *tx = nullptr, *tv = nullptr, *ta = nullptr, *te = nullptr, *ted = nullptr, *tea = nullptr;
+    double *tF = nullptr, *tM = nullptr, *Mv = nullptr, *tmat = nullptr;
+    double *tpp[2] = {nullptr, nullptr}, *tpl[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -615,7 +829,9 @@ XDEM_API int xdem_adj_destroy(xdem_adj* a)
 {
     if (!a) return XDEM_ERR_ARG;
     void* ps[] = {a->ckpt_mem, a->seg_mem, a->lx, a->lv, a->la, a->le, a->led, a->lea, a->lF, a->lM, a->lw,
-                  a->other, a->gpart, a->lpp[0], a->lpp[1], a->lpl[0], a->lpl[1], a->d_mat, a->d_planes, a->d_pid};
+                  a->other, a->gpart, a->lpp[0], a->lpp[1], a->lpl[0], a->lpl[1], a->d_mat, a->d_planes, a->d_pid,
+                  a->tx, a->tv, a->ta, a->te, a->ted, a->tea, a->tF, a->tM, a->Mv, a->tmat, a->tpp[0], a->tpp[1],
+                  a->tpl[0], a->tpl[1]};
     for (void* p : ps)
         if (p) cudaFree(p);
     delete a;
@@ -721,6 +937,125 @@ XDEM_API int xdem_adj_backward(xdem_adj* a, const double* dl_dpos, const double*
         }
     }
     return XDEM_OK;
+}
+
+namespace {
+
+// getConstant's terms (Eeq, Seq8, beta, vs1, fric) of property cp moved by
+// h * d, d = (fric, rest, Ei, Ej).
+void mat_terms(const device_contact_property& cp, int model, const double* d, double h, double out[5])
+{
+    device_contact_property c = cp;
+    c.fric += h * d[0];
+    c.rest += h * d[1];
+    c.Ei += h * d[2];
+    c.Ej += h * d[3];
+    const mat_pair m = make_mat_pair(c, model, false);
+    out[0] = m.Eeq; out[1] = m.Seq8; out[2] = m.beta; out[3] = m.vs1; out[4] = m.fric;
+}
+
+}  // namespace
+
+XDEM_API int xdem_adj_tangent(xdem_adj* a, unsigned int ndir, const double* dparam, double* tpos, double* tvel)
+{
+    if (!a || a->nsteps == 0 || ndir == 0 || ndir > (unsigned int)kTanDirs || !dparam) return XDEM_ERR_ARG;
+    xdem_sim* s = a->s;
+    cudaStream_t st = s->st;
+    const size_t np = a->np;
+    const int model = s->cfg.contact_model;
+    cudaError_t e = cudaSuccess;
+    auto need = [&](double*& p, size_t n) {
+        if (e == cudaSuccess && !p) e = cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * 8);
+    };
+    const size_t D = kTanDirs;
+    need(a->tx, np * 3 * D); need(a->tv, np * 3 * D); need(a->ta, np * 3 * D);
+    need(a->te, np * 4 * D); need(a->ted, np * 4 * D); need(a->tea, np * 4 * D);
+    need(a->tF, np * 3 * D); need(a->tM, np * 3 * D); need(a->Mv, np * 3);
+    need(a->tmat, (size_t)a->nprop * 5 * D);
+    need(a->tpp[0], np * MAX_P2P_COUNT * 2 * D); need(a->tpp[1], np * MAX_P2P_COUNT * 2 * D);
+    need(a->tpl[0], np * MAX_P2PL_COUNT * 2 * D); need(a->tpl[1], np * MAX_P2PL_COUNT * 2 * D);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return XDEM_ERR_ALLOC;
+    }
+    // material tangents by central differences of getConstant (smooth in
+    // the parameters): a relative step of 1e-6 in the largest component
+    std::vector<double> tm((size_t)a->nprop * 5 * D, 0.0);
+    for (unsigned int k = 0; k < ndir; ++k)
+        for (unsigned int p = 0; p < a->nprop; ++p) {
+            const double* d = dparam + ((size_t)k * a->nprop + p) * 4;
+            const device_contact_property& cp = a->cps[p];
+            const double base[4] = {cp.fric, cp.rest, cp.Ei, cp.Ej};
+            double rel = 0.0;
+            for (int c = 0; c < 4; ++c)
+                if (d[c] != 0.0) rel = std::max(rel, std::fabs(d[c]) / std::max(std::fabs(base[c]), 1e-300));
+            if (rel == 0.0) continue;
+            const double h = 1e-6 / rel;
+            double fp[5], fm[5];
+            mat_terms(cp, model, d, h, fp);
+            mat_terms(cp, model, d, -h, fm);
+            for (int f = 0; f < 5; ++f) tm[((size_t)p * 5 + f) * D + k] = (fp[f] - fm[f]) / (2.0 * h);
+        }
+    e = cudaMemcpyAsync(a->tmat, tm.data(), tm.size() * 8, cudaMemcpyHostToDevice, st);
+    for (double* p : {a->tx, a->tv, a->ta, a->tF, a->tM})
+        if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, np * 3 * D * 8, st);
+    for (double* p : {a->te, a->ted, a->tea})
+        if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, np * 4 * D * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a->tpp[0], 0, np * MAX_P2P_COUNT * 2 * D * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a->tpl[0], 0, np * MAX_P2PL_COUNT * 2 * D * 8, st);
+    if (e != cudaSuccess) return cerr(e);
+    // the stored trajectory again, from its first checkpoint
+    if ((e = restore_state(a, a->ckpt[0])) != cudaSuccess) return cerr(e);
+    if ((e = copy_slab(a, a->seg[0], a->ckpt[0])) != cudaSuccess) return cerr(e);
+    TanArgs T{};
+    T.np = a->np;
+    T.nplane = a->nplane;
+    T.model = model;
+    T.vel_compat = s->cfg.velocity_compat;
+    T.dt = s->prm.dt;
+    T.h2 = s->prm.half2dt;
+    T.mass = s->mass;
+    T.inertia = s->inertia;
+    T.mat = a->d_mat;
+    T.tmat = a->tmat;
+    T.planes = a->d_planes;
+    T.plane_pid = a->d_pid;
+    T.tx = a->tx; T.tv = a->tv; T.ta = a->ta; T.te = a->te; T.ted = a->ted; T.tea = a->tea;
+    T.tF = a->tF; T.tM = a->tM; T.Mv = a->Mv;
+    const unsigned int nb = a->nblocks;
+    int cur = 0;
+    for (unsigned int t = 0; t < a->nsteps; ++t) {
+        if (int r = xdem_sim_step(s, 1)) return r;
+        Slab s0 = a->seg[t & 1], s1 = a->seg[(t + 1) & 1];
+        if ((e = save_state(a, s1)) != cudaSuccess) return cerr(e);
+        if (!a->pp) { s0.ppc = s1.ppc = nullptr; }
+        if (!a->pl) { s0.plc = s1.plc = nullptr; }
+        T.tpp_old = a->tpp[cur]; T.tpp_new = a->tpp[cur ^ 1];
+        T.tpl_old = a->tpl[cur]; T.tpl_new = a->tpl[cur ^ 1];
+        k_tan_position<<<nb, kAdjThreads, 0, st>>>(T, s0);
+        k_tan_contacts<<<nb, kAdjThreads, 0, st>>>(T, s0, s1);
+        k_tan_velocity<<<nb, kAdjThreads, 0, st>>>(T, s0, s1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cerr(e);
+        cur ^= 1;
+    }
+    // direction-major outputs: out[k * np * 3 + 3 i + c]
+    std::vector<double> h(np * 3 * D);
+    auto out = [&](const double* src, double* dst) {
+        if (!dst || e != cudaSuccess) return;
+        e = cudaMemcpyAsync(h.data(), src, h.size() * 8, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return;
+        std::vector<double> o(np * 3 * ndir);
+        for (unsigned int k = 0; k < ndir; ++k)
+            for (size_t c = 0; c < np * 3; ++c) o[k * np * 3 + c] = h[c * D + k];
+        e = cudaMemcpyAsync(dst, o.data(), o.size() * 8, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    };
+    out(a->tx, tpos);
+    out(a->tv, tvel);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cerr(e);
+    return xdem_sim_status(s);  // the re-run's own overflow or non-finite bits, if any
 }
 
 XDEM_API int xdem_adj_info(xdem_adj* a, unsigned int* nprop, unsigned int* nsteps, unsigned long long* bytes)

@@ -35,40 +35,117 @@
 namespace xdem {
 namespace adj {
 
-struct V { double x, y, z; };
-struct Q { double x, y, z, w; };
+// The forward pieces are templates on the scalar type: double for the
+// forward restatement the VJPs differentiate, Dual (below) for the tangent
+// (forward mode) of the same arithmetic.  The VJPs take V = VT<double>.
+XA_HD double sqrt(double x) { return ::sqrt(x); }
+XA_HD double fabs(double x) { return ::fabs(x); }
+
+// Forward-mode dual number with N tangent directions: value v and
+// derivatives d[k].  Arithmetic follows the product, quotient and chain
+// rules; comparisons look at the value only, so a branch follows the
+// forward computation.
+template <int N>
+struct Dual {
+    double v;
+    double d[N];
+    XA_HD Dual() : v(0.0)
+    {
+        for (int k = 0; k < N; ++k) d[k] = 0.0;
+    }
+    XA_HD Dual(double x) : v(x)  // a constant
+    {
+        for (int k = 0; k < N; ++k) d[k] = 0.0;
+    }
+    friend XA_HD Dual operator+(const Dual& a, const Dual& b)
+    {
+        Dual r(a.v + b.v);
+        for (int k = 0; k < N; ++k) r.d[k] = a.d[k] + b.d[k];
+        return r;
+    }
+    friend XA_HD Dual operator-(const Dual& a, const Dual& b)
+    {
+        Dual r(a.v - b.v);
+        for (int k = 0; k < N; ++k) r.d[k] = a.d[k] - b.d[k];
+        return r;
+    }
+    friend XA_HD Dual operator-(const Dual& a)
+    {
+        Dual r(-a.v);
+        for (int k = 0; k < N; ++k) r.d[k] = -a.d[k];
+        return r;
+    }
+    friend XA_HD Dual operator*(const Dual& a, const Dual& b)
+    {
+        Dual r(a.v * b.v);
+        for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+        return r;
+    }
+    friend XA_HD Dual operator/(const Dual& a, const Dual& b)
+    {
+        Dual r(a.v / b.v);
+        for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
+        return r;
+    }
+    friend XA_HD Dual sqrt(const Dual& a)
+    {
+        Dual r(::sqrt(a.v));
+        for (int k = 0; k < N; ++k) r.d[k] = r.v > 0.0 ? a.d[k] / (2.0 * r.v) : 0.0;
+        return r;
+    }
+    friend XA_HD Dual fabs(const Dual& a) { return a.v < 0.0 ? -a : a; }
+    friend XA_HD bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+    friend XA_HD bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+    friend XA_HD bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+    friend XA_HD bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+    friend XA_HD bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
+    friend XA_HD bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
+};
+
+template <class T> struct VT { T x, y, z; };
+template <class T> struct QT { T x, y, z, w; };
+using V = VT<double>;
+using Q = QT<double>;
 
 XA_HD V mkv(double x, double y, double z) { return V{x, y, z}; }
 XA_HD Q mkq(double x, double y, double z, double w) { return Q{x, y, z, w}; }
-XA_HD V operator+(V a, V b) { return mkv(a.x + b.x, a.y + b.y, a.z + b.z); }
-XA_HD V operator-(V a, V b) { return mkv(a.x - b.x, a.y - b.y, a.z - b.z); }
-XA_HD V operator-(V a) { return mkv(-a.x, -a.y, -a.z); }
-XA_HD V operator*(double s, V a) { return mkv(s * a.x, s * a.y, s * a.z); }
-XA_HD V operator/(V a, double s) { return mkv(a.x / s, a.y / s, a.z / s); }
-XA_HD Q operator+(Q a, Q b) { return mkq(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-XA_HD Q operator-(Q a, Q b) { return mkq(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
-XA_HD Q operator*(double s, Q a) { return mkq(s * a.x, s * a.y, s * a.z, s * a.w); }
-XA_HD double dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-XA_HD double dot(Q a, Q b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
-XA_HD double len(V a) { return sqrt(dot(a, a)); }
-XA_HD V cross(V a, V b) { return mkv(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+template <class T> XA_HD VT<T> vzero() { return VT<T>{T(0.0), T(0.0), T(0.0)}; }
+// a constant vector (plane geometry, inertia) in the scalar type T
+template <class T> XA_HD VT<T> vc(V a) { return VT<T>{T(a.x), T(a.y), T(a.z)}; }
+template <class T> XA_HD VT<T> operator+(VT<T> a, VT<T> b) { return VT<T>{a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class T> XA_HD VT<T> operator-(VT<T> a, VT<T> b) { return VT<T>{a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class T> XA_HD VT<T> operator-(VT<T> a) { return VT<T>{-a.x, -a.y, -a.z}; }
+template <class S, class T> XA_HD VT<T> operator*(S s, VT<T> a) { return VT<T>{s * a.x, s * a.y, s * a.z}; }
+template <class T, class S> XA_HD VT<T> operator/(VT<T> a, S s) { return VT<T>{a.x / s, a.y / s, a.z / s}; }
+template <class T> XA_HD QT<T> operator+(QT<T> a, QT<T> b) { return QT<T>{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+template <class T> XA_HD QT<T> operator-(QT<T> a, QT<T> b) { return QT<T>{a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+template <class S, class T> XA_HD QT<T> operator*(S s, QT<T> a) { return QT<T>{s * a.x, s * a.y, s * a.z, s * a.w}; }
+template <class T> XA_HD T dot(VT<T> a, VT<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> XA_HD T dot(QT<T> a, QT<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+template <class T> XA_HD T len(VT<T> a) { return sqrt(dot(a, a)); }
+template <class T> XA_HD VT<T> cross(VT<T> a, VT<T> b)
+{
+    return VT<T>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
 XA_HD void addv(V& a, V b) { a = a + b; }
 XA_HD void addq(Q& a, Q b) { a = a + b; }
 
 // ---------------------------------------------------------------- Euler parameters
 // L(e) (3x4): rows (-e1, e0, e3, -e2), (-e2, -e3, e0, e1), (-e3, e2, -e1, e0)
 // with e = (e0, e1, e2, e3) held as (x, y, z, w).  L(e) x = -L(x) e.
-XA_HD V Lmul(Q e, Q x)
+template <class T>
+XA_HD VT<T> Lmul(QT<T> e, QT<T> x)
 {
-    return mkv(-e.y * x.x + e.x * x.y + e.w * x.z - e.z * x.w, -e.z * x.x - e.w * x.y + e.x * x.z + e.y * x.w,
-               -e.w * x.x + e.z * x.y - e.y * x.z + e.x * x.w);
+    return VT<T>{-e.y * x.x + e.x * x.y + e.w * x.z - e.z * x.w, -e.z * x.x - e.w * x.y + e.x * x.z + e.y * x.w,
+               -e.w * x.x + e.z * x.y - e.y * x.z + e.x * x.w};
 }
 // L(e)^T r (4-vector).  L(e)^T r = M(r) e with M(r) skew:
 // rows (0,-r0,-r1,-r2), (r0,0,r2,-r1), (r1,-r2,0,r0), (r2,r1,-r0,0).
-XA_HD Q LTmul(Q e, V r)
+template <class T>
+XA_HD QT<T> LTmul(QT<T> e, VT<T> r)
 {
-    return mkq(-e.y * r.x - e.z * r.y - e.w * r.z, e.x * r.x - e.w * r.y + e.z * r.z,
-               e.w * r.x + e.x * r.y - e.y * r.z, -e.z * r.x + e.y * r.y + e.x * r.z);
+    return QT<T>{-e.y * r.x - e.z * r.y - e.w * r.z, e.x * r.x - e.w * r.y + e.z * r.z,
+               e.w * r.x + e.x * r.y - e.y * r.z, -e.z * r.x + e.y * r.y + e.x * r.z};
 }
 XA_HD Q MTmul(V r, Q l)  // M(r)^T l = -M(r) l
 {
@@ -77,10 +154,11 @@ XA_HD Q MTmul(V r, Q l)  // M(r)^T l = -M(r) l
 }
 // G(e) (3x4) of the angular velocity: rows (-e1, e0, -e3, e2),
 // (-e2, e3, e0, -e1), (-e3, -e2, e1, e0).  G(e) d = -G(d) e.
-XA_HD V Gmul(Q e, Q d)
+template <class T>
+XA_HD VT<T> Gmul(QT<T> e, QT<T> d)
 {
-    return mkv(-e.y * d.x + e.x * d.y - e.w * d.z + e.z * d.w, -e.z * d.x + e.w * d.y + e.x * d.z - e.y * d.w,
-               -e.w * d.x - e.z * d.y + e.y * d.z + e.x * d.w);
+    return VT<T>{-e.y * d.x + e.x * d.y - e.w * d.z + e.z * d.w, -e.z * d.x + e.w * d.y + e.x * d.z - e.y * d.w,
+               -e.w * d.x - e.z * d.y + e.y * d.z + e.x * d.w};
 }
 XA_HD Q GTmul(Q e, V w)
 {
@@ -89,7 +167,7 @@ XA_HD Q GTmul(Q e, V w)
 }
 
 // omega = 2 G(e) d (impl:32-41)
-XA_HD V ang_vel(Q e, Q d) { return 2.0 * Gmul(e, d); }
+template <class T> XA_HD VT<T> ang_vel(QT<T> e, QT<T> d) { return 2.0 * Gmul(e, d); }
 XA_HD void ang_vel_vjp(Q e, Q d, V lw, Q& le, Q& ld)
 {
     addq(ld, 2.0 * GTmul(e, lw));
@@ -97,24 +175,27 @@ XA_HD void ang_vel_vjp(Q e, Q d, V lw, Q& le, Q& ld)
 }
 
 // Rotation A(e) (impl:8-30): A v (to_global) and A^T v (to_local).
-XA_HD void rot_rows(Q e, V& r0, V& r1, V& r2)
+template <class T>
+XA_HD void rot_rows(QT<T> e, VT<T>& r0, VT<T>& r1, VT<T>& r2)
 {
-    r0 = mkv(2.0 * (e.x * e.x + e.y * e.y - 0.5), 2.0 * (e.y * e.z - e.x * e.w), 2.0 * (e.y * e.w + e.x * e.z));
-    r1 = mkv(2.0 * (e.y * e.z + e.x * e.w), 2.0 * (e.x * e.x + e.z * e.z - 0.5), 2.0 * (e.z * e.w - e.x * e.y));
-    r2 = mkv(2.0 * (e.y * e.w - e.x * e.z), 2.0 * (e.z * e.w + e.x * e.y), 2.0 * (e.x * e.x + e.w * e.w - 0.5));
+    r0 = VT<T>{2.0 * (e.x * e.x + e.y * e.y - 0.5), 2.0 * (e.y * e.z - e.x * e.w), 2.0 * (e.y * e.w + e.x * e.z)};
+    r1 = VT<T>{2.0 * (e.y * e.z + e.x * e.w), 2.0 * (e.x * e.x + e.z * e.z - 0.5), 2.0 * (e.z * e.w - e.x * e.y)};
+    r2 = VT<T>{2.0 * (e.y * e.w - e.x * e.z), 2.0 * (e.z * e.w + e.x * e.y), 2.0 * (e.x * e.x + e.w * e.w - 0.5)};
 }
-XA_HD V to_global(V v, Q e)
+template <class T>
+XA_HD VT<T> to_global(VT<T> v, QT<T> e)
 {
-    V r0, r1, r2;
+    VT<T> r0, r1, r2;
     rot_rows(e, r0, r1, r2);
-    return mkv(dot(r0, v), dot(r1, v), dot(r2, v));
+    return VT<T>{dot(r0, v), dot(r1, v), dot(r2, v)};
 }
-XA_HD V to_local(V v, Q e)
+template <class T>
+XA_HD VT<T> to_local(VT<T> v, QT<T> e)
 {
-    V r0, r1, r2;
+    VT<T> r0, r1, r2;
     rot_rows(e, r0, r1, r2);
-    return mkv(r0.x * v.x + r1.x * v.y + r2.x * v.z, r0.y * v.x + r1.y * v.y + r2.y * v.z,
-               r0.z * v.x + r1.z * v.y + r2.z * v.z);
+    return VT<T>{r0.x * v.x + r1.x * v.y + r2.x * v.z, r0.y * v.x + r1.y * v.y + r2.y * v.z,
+                 r0.z * v.x + r1.z * v.y + r2.z * v.z};
 }
 // n = A(e)^T m: lm += A(e) ln, le += grad_e (m^T A(e) ln).
 XA_HD void to_local_vjp(V m, Q e, V ln, V& lm, Q& le)
@@ -134,15 +215,16 @@ XA_HD void to_local_vjp(V m, Q e, V ln, V& lm, Q& le)
 }
 
 // Euler-parameter acceleration (impl:74-133), closed form.
-XA_HD Q uceom(V J, Q e, Q d, V n)
+template <class T>
+XA_HD QT<T> uceom(V J, QT<T> e, QT<T> d, VT<T> n)
 {
-    const V w = Lmul(e, d);
-    const V T = mkv(J.x * w.x, J.y * w.y, J.z * w.z);
-    const Q h = 4.0 * LTmul(d, T);
-    const V lh = Lmul(e, h);
-    const V r = mkv((n.x - lh.x) / (2.0 * J.x), (n.y - lh.y) / (2.0 * J.y), (n.z - lh.z) / (2.0 * J.z));
-    const double s2 = dot(e, e), c = dot(d, d);
-    return (1.0 / s2) * (LTmul(e, r) - c * e);
+    const VT<T> w = Lmul(e, d);
+    const VT<T> Tj = VT<T>{J.x * w.x, J.y * w.y, J.z * w.z};
+    const QT<T> h = 4.0 * LTmul(d, Tj);
+    const VT<T> lh = Lmul(e, h);
+    const VT<T> r = VT<T>{(n.x - lh.x) / (2.0 * J.x), (n.y - lh.y) / (2.0 * J.y), (n.z - lh.z) / (2.0 * J.z)};
+    const T s2 = dot(e, e), c = dot(d, d);
+    return (T(1.0) / s2) * (LTmul(e, r) - c * e);
 }
 // The moment in body axes that gave q (q = uceom(J, e, d, n)): L(e) q = r.
 XA_HD V uceom_torque(V J, Q e, Q d, Q q)
@@ -191,10 +273,11 @@ XA_HD void uceom_vjp(V J, Q e, Q d, V n, Q lq, Q& le, Q& ld, V& ln)
 }
 
 // e1 = e' / |e'|
-XA_HD Q normalize(Q e)
+template <class T>
+XA_HD QT<T> normalize(QT<T> e)
 {
-    const double l = sqrt(dot(e, e));
-    return mkq(e.x / l, e.y / l, e.z / l, e.w / l);
+    const T l = sqrt(dot(e, e));
+    return QT<T>{e.x / l, e.y / l, e.z / l, e.w / l};
 }
 XA_HD void normalize_vjp(Q e, Q l1, Q& le)
 {
@@ -206,9 +289,11 @@ XA_HD void normalize_vjp(Q e, Q l1, Q& le)
 // ---------------------------------------------------------------- contact model
 // Material terms of a contact pair (the precomputed fields of getConstant
 // that the model reads; impl:362-386).
-struct Mat {
-    double Eeq, Seq8, beta, vs1, sratio, fric;
+template <class T>
+struct MatT {
+    T Eeq, Seq8, beta, vs1, sratio, fric;
 };
+using Mat = MatT<double>;
 // Loss gradient with respect to those fields.
 struct MatGrad {
     double Eeq, Seq8, beta, vs1, fric;
@@ -224,23 +309,26 @@ XA_HD void add_grad(MatGrad& a, const MatGrad& b)
 // the partner's contact point, the history (ds0, dots0) carried from the last
 // step.  `tang` is false when the tangential velocity is exactly zero: the
 // model then leaves Ft and the history untouched.
-struct Core {
-    double kn, vn, ks, vs, mu, Req, Meq;
-    double delta, ds0, dots0;
-    V u, rv;
+template <class T>
+struct CoreT {
+    T kn, vn, ks, vs, mu, Req, Meq;
+    T delta, ds0, dots0;
+    VT<T> u, rv;
     // outputs
-    V Fn, Ft;
-    double ds1, dots1;
+    VT<T> Fn, Ft;
+    T ds1, dots1;
     bool tang;
     // intermediates
-    double fsn, cn, fn, me, sdot, St, a, b, nFn;
-    V s;
+    T fsn, cn, fn, me, sdot, St, a, b, nFn;
+    VT<T> s;
 };
+using Core = CoreT<double>;
 
-XA_HD void core_consts(const Mat& m, int model, double ri, double rj, double mi, double mj, Core& c)
+template <class T>
+XA_HD void core_consts(const MatT<T>& m, int model, double ri, double rj, double mi, double mj, CoreT<T>& c)
 {
-    c.Meq = mj != 0.0 ? (mi * mj) / (mi + mj) : mi;
-    c.Req = rj != 0.0 ? (ri * rj) / (ri + rj) : ri;
+    c.Meq = T(mj != 0.0 ? (mi * mj) / (mi + mj) : mi);
+    c.Req = T(rj != 0.0 ? (ri * rj) / (ri + rj) : ri);
     c.kn = (4.0 / 3.0) * m.Eeq * sqrt(c.Req);
     c.vn = m.beta;
     c.ks = model == 1 ? m.Seq8 : c.kn * m.sratio;
@@ -248,19 +336,20 @@ XA_HD void core_consts(const Mat& m, int model, double ri, double rj, double mi,
     c.mu = m.fric;
 }
 
-XA_HD void core_fwd(int model, double dt, Core& c)
+template <class T>
+XA_HD void core_fwd(int model, double dt, CoreT<T>& c)
 {
     c.fsn = -c.kn * (c.delta * sqrt(c.delta));
     c.cn = dot(c.rv, c.u);
-    const double fdn = c.vn * c.cn;
+    const T fdn = c.vn * c.cn;
     c.fn = c.fsn + fdn;
     c.Fn = c.fn * c.u;
-    const V et = c.rv - dot(c.rv, c.u) * c.u;
+    const VT<T> et = c.rv - dot(c.rv, c.u) * c.u;
     c.me = len(et);
-    c.tang = c.me != 0.0;
+    c.tang = c.me != T(0.0);
     c.ds1 = c.ds0;
     c.dots1 = c.dots0;
-    c.Ft = mkv(0, 0, 0);
+    c.Ft = vzero<T>();
     c.nFn = len(c.Fn);
     if (c.tang) {
         c.s = et / c.me;
@@ -271,7 +360,7 @@ XA_HD void core_fwd(int model, double dt, Core& c)
             c.St = c.ks * sqrt(c.Req * c.delta);
             c.a = c.St * c.ds1 + c.vs * sqrt(c.St * c.Meq);
         } else {
-            c.St = 0.0;
+            c.St = T(0.0);
             c.a = c.ks * c.ds1 + c.vs * dot(c.rv, c.s);
         }
         c.b = c.mu * c.nFn;
@@ -356,7 +445,11 @@ XA_HD void core_vjp(int model, double dt, const Core& c, const Mat& m, V lFn, V 
 // Relative velocity of the partner's contact point seen from sphere i:
 // rv = (vj + wj x dj) - (vi + wi x di) with di, dj the contact point relative
 // to the two centres (impl:684-688).
-XA_HD V rel_vel(V vi, V wi, V di, V vj, V wj, V dj) { return (vj + cross(wj, dj)) - (vi + cross(wi, di)); }
+template <class T>
+XA_HD VT<T> rel_vel(VT<T> vi, VT<T> wi, VT<T> di, VT<T> vj, VT<T> wj, VT<T> dj)
+{
+    return (vj + cross(wj, dj)) - (vi + cross(wi, di));
+}
 XA_HD void rel_vel_vjp(V wi, V di, V wj, V dj, V lrv, V& lvi, V& lwi, V& ldi, V& lvj, V& lwj, V& ldj)
 {
     lvj = lvj + lrv;
@@ -369,17 +462,20 @@ XA_HD void rel_vel_vjp(V wi, V di, V wj, V dj, V lrv, V& lvi, V& lwi, V& ldi, V&
 
 // Particle pair (impl:676-688): rp = xj - xi, delta = (ri + rj) - |rp|,
 // u = rp / |rp|, contact point c = xi + ri u, di = c - xi, dj = c - xj.
-struct PairGeom {
-    V rp, u, di, dj;
-    double dist, delta;
+template <class T>
+struct PairGeomT {
+    VT<T> rp, u, di, dj;
+    T dist, delta;
 };
-XA_HD void pair_geom(V xi, V xj, double ri, double rj, PairGeom& g)
+using PairGeom = PairGeomT<double>;
+template <class T>
+XA_HD void pair_geom(VT<T> xi, VT<T> xj, double ri, double rj, PairGeomT<T>& g)
 {
-    g.rp = mkv(xj.x - xi.x, xj.y - xi.y, xj.z - xi.z);
+    g.rp = VT<T>{xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
     g.dist = len(g.rp);
-    g.delta = (ri + rj) - g.dist;
+    g.delta = T(ri + rj) - g.dist;
     g.u = g.rp / g.dist;
-    const V cpt = xi + ri * g.u;
+    const VT<T> cpt = xi + ri * g.u;
     g.di = cpt - xi;
     g.dj = cpt - xj;
 }
@@ -401,24 +497,28 @@ XA_HD void pair_geom_vjp(const PairGeom& g, double ri, double ldelta, V lu, V ld
 // (u = (x - w) / |x - w|), 2 edge (u = -hs / |hs| with hs the part of x - w
 // normal to the edge direction es), 3 face (u = -uw / |uw|,
 // delta = r - |(x - xw) . u|).
-struct PlaneGeom {
+template <class T>
+struct PlaneGeomT {
     int region;
-    double delta, h, side;
-    V u, X, es, hs;
+    T delta, h, side;
+    VT<T> u, X, es, hs;
 };
+using PlaneGeom = PlaneGeomT<double>;
 struct PlaneRect {
     V xw, u1, u2, uw, w2, w3, w4;
     double l1, l2;
 };
-XA_HD double plane_geom(const PlaneRect& pe, V xp, double r, PlaneGeom& g)
+template <class T>
+XA_HD T plane_geom(const PlaneRect& pe, VT<T> xp, double r, PlaneGeomT<T>& g)
 {
     g.region = 0;
-    g.delta = 0.0;
-    const V dp = xp - pe.xw;
-    const V wp = mkv(dot(dp, pe.u1), dot(dp, pe.u2), dot(dp, pe.uw));
-    const double a_l1 = (wp.x - pe.l1) * (wp.x - pe.l1);
-    const double b_l2 = (wp.y - pe.l2) * (wp.y - pe.l2);
-    const double sqa = wp.x * wp.x, sqb = wp.y * wp.y, sqc = wp.z * wp.z, sqr = r * r;
+    g.delta = T(0.0);
+    const VT<T> dp = xp - vc<T>(pe.xw);
+    const VT<T> wp = VT<T>{dot(dp, vc<T>(pe.u1)), dot(dp, vc<T>(pe.u2)), dot(dp, vc<T>(pe.uw))};
+    const T a_l1 = (wp.x - pe.l1) * (wp.x - pe.l1);
+    const T b_l2 = (wp.y - pe.l2) * (wp.y - pe.l2);
+    const T sqa = wp.x * wp.x, sqb = wp.y * wp.y, sqc = wp.z * wp.z;
+    const double sqr = r * r;
     V w = pe.xw;
     bool corner = false;
     if (wp.x < 0 && wp.y < 0 && (sqa + sqb + sqc) < sqr) {
@@ -432,10 +532,10 @@ XA_HD double plane_geom(const PlaneRect& pe, V xp, double r, PlaneGeom& g)
     }
     if (corner) {
         g.region = 1;
-        g.X = xp - w;
+        g.X = xp - vc<T>(w);
         g.h = len(g.X);
         g.u = g.X / g.h;
-        g.delta = r - g.h;
+        g.delta = T(r) - g.h;
         return g.delta;
     }
     V e0 = pe.xw, e1 = pe.w2;
@@ -449,25 +549,25 @@ XA_HD double plane_geom(const PlaneRect& pe, V xp, double r, PlaneGeom& g)
     }
     if (edge) {
         g.region = 2;
-        g.X = xp - e0;
+        g.X = xp - vc<T>(e0);
         const V ev = e1 - e0;
-        g.es = ev / len(ev);
+        g.es = vc<T>(ev / len(ev));
         g.hs = g.X - dot(g.X, g.es) * g.es;
         g.h = len(g.hs);
         g.u = (-g.hs) / g.h;
-        g.delta = r - g.h;
+        g.delta = T(r) - g.h;
         return g.delta;
     }
     if ((wp.x > 0 && wp.x < pe.l1) && (wp.y > 0 && wp.y < pe.l2)) {
         g.region = 3;
         const V uu = pe.uw / len(pe.uw);
-        g.u = -uu;
-        const double sd = dot(dp, g.u);
-        g.side = sd < 0.0 ? -1.0 : 1.0;
-        g.delta = r - fabs(sd);
+        g.u = vc<T>(-uu);
+        const T sd = dot(dp, g.u);
+        g.side = T(sd < T(0.0) ? -1.0 : 1.0);
+        g.delta = T(r) - fabs(sd);
         return g.delta;
     }
-    return 0.0;
+    return T(0.0);
 }
 XA_HD void plane_geom_vjp(const PlaneGeom& g, double ldelta, V lu, V& lx)
 {
@@ -487,24 +587,27 @@ XA_HD void plane_geom_vjp(const PlaneGeom& g, double ldelta, V lu, V& lx)
 
 // ---------------------------------------------------------------- one sphere's contacts
 // Sphere i and the state of one contact partner.
-struct Body {
-    V x, v, w;
+template <class T>
+struct BodyT {
+    VT<T> x, v, w;
     double r, m;
 };
+using Body = BodyT<double>;
 
 // Particle-particle contacts of sphere i in the order the step visited them
 // (the order of its pair list), impl:613-733 as the FP64 fused kernel runs
 // it: each contact adds Fn + Ft to F and di x (Fn + Ft) to M.  A contact
 // whose tangential velocity is exactly zero keeps the Ft of the contact
 // before it (the model leaves Ft untouched; impl:441-452).
-XA_HD void pp_sphere_fwd(int model, double dt, const Mat& mat, const Body& bi, const Body* nb, const double* ds0,
-                         const double* dots0, int n, V& F, V& M, double* ds1, double* dots1)
+template <class T>
+XA_HD void pp_sphere_fwd(int model, double dt, const MatT<T>& mat, const BodyT<T>& bi, const BodyT<T>* nb,
+                         const T* ds0, const T* dots0, int n, VT<T>& F, VT<T>& M, T* ds1, T* dots1)
 {
-    V Ft = mkv(0, 0, 0);
+    VT<T> Ft = vzero<T>();
     for (int s = 0; s < n; ++s) {
-        PairGeom pg;
+        PairGeomT<T> pg;
         pair_geom(bi.x, nb[s].x, bi.r, nb[s].r, pg);
-        Core c;
+        CoreT<T> c;
         core_consts(mat, model, bi.r, nb[s].r, bi.m, nb[s].m, c);
         c.delta = pg.delta;
         c.u = pg.u;
@@ -513,7 +616,7 @@ XA_HD void pp_sphere_fwd(int model, double dt, const Mat& mat, const Body& bi, c
         c.dots0 = dots0[s];
         core_fwd(model, dt, c);
         if (c.tang) Ft = c.Ft;
-        const V G = c.Fn + Ft;
+        const VT<T> G = c.Fn + Ft;
         F = F + G;
         M = M + cross(pg.di, G);
         ds1[s] = c.ds1;
@@ -586,26 +689,33 @@ struct PlaneContact {
     V bp, bv, bw;
     Mat mat;
 };
-XA_HD void plane_contact_fwd(int model, double dt, const PlaneContact& pc, const Body& bi, double ds0, double dots0,
-                             V& F, V& M, double& ds1, double& dots1)
+// The plane's material terms come in `mat` (pc.mat, or its dual form).
+template <class T>
+XA_HD void plane_contact_fwd_t(int model, double dt, const PlaneContact& pc, const MatT<T>& mat, const BodyT<T>& bi,
+                               T ds0, T dots0, VT<T>& F, VT<T>& M, T& ds1, T& dots1)
 {
-    PlaneGeom pg;
+    PlaneGeomT<T> pg;
     plane_geom(pc.rect, bi.x, bi.r, pg);
-    const V cpt = bi.x + bi.r * pg.u;
-    const V di = cpt - bi.x, dj = cpt - pc.bp;
-    Core c;
-    core_consts(pc.mat, model, bi.r, 0.0, bi.m, 0.0, c);
+    const VT<T> cpt = bi.x + bi.r * pg.u;
+    const VT<T> di = cpt - bi.x, dj = cpt - vc<T>(pc.bp);
+    CoreT<T> c;
+    core_consts(mat, model, bi.r, 0.0, bi.m, 0.0, c);
     c.delta = pg.delta;
     c.u = pg.u;
-    c.rv = rel_vel(bi.v, bi.w, di, pc.bv, pc.bw, dj);
+    c.rv = rel_vel(bi.v, bi.w, di, vc<T>(pc.bv), vc<T>(pc.bw), dj);
     c.ds0 = ds0;
     c.dots0 = dots0;
     core_fwd(model, dt, c);
-    const V G = c.Fn + c.Ft;
+    const VT<T> G = c.Fn + c.Ft;
     F = F + G;
     M = M + cross(di, G);
     ds1 = c.ds1;
     dots1 = c.dots1;
+}
+XA_HD void plane_contact_fwd(int model, double dt, const PlaneContact& pc, const Body& bi, double ds0, double dots0,
+                             V& F, V& M, double& ds1, double& dots1)
+{
+    plane_contact_fwd_t<double>(model, dt, pc, pc.mat, bi, ds0, dots0, F, M, ds1, dots1);
 }
 XA_HD void plane_contact_vjp(int model, double dt, const PlaneContact& pc, const Body& bi, double ds0, double dots0,
                              V lF, V lM, double lds1, double ldots1, V& lx, V& lv, V& lw, double& lds0,
