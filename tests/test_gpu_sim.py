@@ -243,11 +243,83 @@ def test_handle_with_cylinder_matches_oracle(simmod, oracle, cluster):
     assert np.abs(w).max() > 0
 
 
-def test_mixed_handle_with_cylinder_is_refused(simmod):
-    sm = simmod.Sim(drum(n=300), precision=T.XDEM_MIXED)
+def test_mixed_handle_with_cylinder_matches_fp64(simmod):
+    """The mixed step's cylinder contact (the FP64 regions of the launcher
+    kernel, FP32 forces) against the FP64 handle on the spinning, drifting
+    drum: after one step the particle-pair and cylinder pair lists are
+    identical and the contact accelerations (force / mass) and Euler-parameter
+    accelerations agree to 1e-4 of the largest, the cylinder's wrench to 1e-4;
+    over 200 steps the kinetic energy to 1e-3 and the cylinder contacts stay
+    equal."""
+    sc = drum(n=1500)
+    a = simmod.Sim(sc, precision=T.XDEM_FP64)
+    b = simmod.Sim(sc, precision=T.XDEM_MIXED)
+    a.step(1)
+    b.step(1)
+    sa, sb = a.state(), b.state()
+    g = np.tile(np.array(sc.gravity), sc.np_)
+    fa, fb = sa["acc"] - g, sb["acc"] - g
+    assert np.abs(fa - fb).max() <= 1e-4 * np.abs(fa).max()
+    assert np.abs(sa["ea"] - sb["ea"]).max() <= 1e-4 * np.abs(sa["ea"]).max()
+    touched = 0
+    for kind, cap in ((0, 12), (3, 3)):
+        ca, ia, _ = a.pairs(kind)
+        cb, ib, _ = b.pairs(kind)
+        assert np.array_equal(ca, cb), kind
+        ia, ib = ia.reshape(-1, cap), ib.reshape(-1, cap)
+        for i in np.nonzero(ca)[0]:
+            assert np.array_equal(ia[i, :ca[i]], ib[i, :ca[i]]), (kind, i)
+        if kind == 3:
+            touched = int(ca.sum())
+    assert touched > 0
+    wa, wb = a.wrench(a.bodies[0]), b.wrench(b.bodies[0])
+    for part in (slice(0, 3), slice(3, 6)):
+        assert np.abs(wa[part] - wb[part]).max() <= 1e-4 * np.abs(wa[part]).max(), (wa, wb)
+    a.step(199)
+    b.step(199)
+    ka, _ = a.energy()
+    kb, _ = b.energy()
+    assert abs(ka - kb) <= 1e-3 * ka, (ka, kb)
+    assert a.status() == 0 and b.status() == 0
+    a.close()
+    b.close()
+
+
+def test_mixed_cluster_handle_with_cylinder_is_refused(simmod):
+    sm = simmod.Sim(drum(n=300, cluster=True), precision=T.XDEM_MIXED)
     with pytest.raises(Exception):
         sm.step(1)
     sm.close()
+
+
+@pytest.mark.parametrize("nt", [64, 128, 256])
+def test_mixed_plane_wrench_rows_with_padding_warps(simmod, nt):
+    """1,100 spheres in an open box, numbered so that the first 64 rest on
+    the wall x = x0 (plane 1): the body kernel's last block holds padding
+    warps past the last sphere, which must leave the per-warp wrench rows of
+    the next plane alone.  Every plane's wrench of the mixed step against the
+    FP64 step on the same state, to 1e-4 of its size."""
+    sc = scenes.random_packed(1100, 0.8e-3, 1.2e-3, None, seed=21)
+    order = np.argsort(sc.pos.reshape(-1, 4)[:, 0], kind="stable")  # spheres nearest the wall x = x0 first
+    for key, w in (("pos", 4), ("vel", 3), ("acc", 3), ("ep", 4), ("ev", 4), ("ea", 4), ("mass", 1),
+                   ("inertia", 3)):
+        setattr(sc, key, np.asarray(getattr(sc, key)).reshape(-1, w)[order].ravel())
+    a = simmod.Sim(sc, precision=T.XDEM_FP64)
+    b = simmod.Sim(sc, precision=T.XDEM_MIXED)
+    b.set_tune(nt_pairs=nt, stage=16, nt_bodies=nt, occ_pairs=768, occ_bodies=768, skin_div=0)
+    a.step(1)
+    b.step(1)
+    touched = 0
+    for body in a.bodies:
+        wa, wb = a.wrench(body), b.wrench(body)
+        for part in (slice(0, 3), slice(3, 6)):
+            s_ = np.abs(wa[part]).max()
+            if s_ > 0:
+                touched += 1
+                assert np.abs(wa[part] - wb[part]).max() <= 1e-4 * s_, (body, wa, wb)
+    assert touched >= 4
+    a.close()
+    b.close()
 
 
 def test_cylinder_pairs_survive_a_part_file(simmod, tmp_path):

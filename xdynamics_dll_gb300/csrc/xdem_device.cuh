@@ -243,6 +243,104 @@ __device__ __forceinline__ void rolling_accumulate(double rf, double ir, double 
     Mr += Rij * rf * length(Fn);
 }
 
+// ---------------------------------------------------------------- cylinder regions (impl:1083-1322)
+// Shared by the launcher kernel (xdem_kernels.cu) and the mixed step's body
+// kernel, so both classify a sphere against a cylinder with the same FP64
+// arithmetic.
+// Base and top centres of a cylinder at its body pose.
+__device__ __forceinline__ void cylinder_ends(const device_cylinder_info& cy, const double* bi, d3& pos, d4& e,
+                                              d3& base, d3& top)
+{
+    pos = mk3(bi[XDEM_PX], bi[XDEM_PY], bi[XDEM_PZ]);
+    e = mk4(bi[XDEM_E0], bi[XDEM_E1], bi[XDEM_E2], bi[XDEM_E3]);
+    base = pos + to_global(dv3(cy.pbase), e);
+    top = pos + to_global(dv3(cy.ptop), e);
+}
+
+// impl:1189-1288: depth and unit vector of sphere (p, r) against the
+// cylinder -- side (axis parameter in [0, 1]; an inside contact flips the
+// normal and sets `inner`), the wall annulus beyond the ends, else the rim
+// point through the angle atan(x / z) of the local offset, as the reference
+// forms it.
+__device__ inline double cylinder_detection(const device_cylinder_info& cy, const double* bi, d3 p, d3& u, double r,
+                                     bool& inner)
+{
+    d3 cyl_pos, base, top;
+    d4 e;
+    cylinder_ends(cy, bi, cyl_pos, e, base, top);
+    const d3 ab = top - base;
+    const double t = dot(p - base, ab) / dot(ab, ab);
+    const d3 c = base + t * ab;
+    double dist = length(p - c);
+    if (t >= 0 && t <= 1) {
+        if (dist == 0) {
+            inner = true;
+            return 0;
+        }
+        u = (c - p) / dist;
+        if (dist < cy.len_rr.z) {
+            inner = true;
+            u = -u;
+            return dist + r - cy.len_rr.y;
+        }
+        return cy.len_rr.y + r - dist;
+    }
+    const double thick = cy.thickness;
+    const int one = thick != 0.0 ? 1 : 0;
+    if (dist < cy.len_rr.z + thick && dist > one * cy.len_rr.z) {
+        const d3 o2c = cyl_pos - c;
+        const double l = length(o2c);
+        u = o2c / l;
+        return cy.len_rr.x * 0.5 + r - l;
+    }
+    d3 at = to_local(p - top, e);
+    d3 cp = top;
+    if (fabs(at.y) > cy.len_rr.x) {
+        at = to_local(p - base, e);
+        cp = base;
+    }
+    const double pi = atan(at.x / at.z);
+    d3 q = mk3(0, 0, 0);
+    if (pi < 0 && at.z < 0) q.x = cy.len_rr.z * sin(-pi);
+    else if (pi > 0 && at.x < 0 && at.z < 0) q.x = cy.len_rr.z * sin(-pi);
+    else q.x = cy.len_rr.z * sin(pi);
+    q.z = cy.len_rr.z * cos(pi);
+    if (at.z < 0 && q.z > 0) q.z = -q.z;
+    else if (at.z > 0 && q.z < 0) q.z = -q.z;
+    q.y = 0.;
+    cp = cp + to_global(q, e);
+    const d3 dv = cp - p;
+    dist = length(dv);
+    u = dv / dist;
+    if (dist < r) return r - dist;
+    return -1.0;
+}
+
+// impl:1290-1322: the cap a sphere inside the cylinder faces (none near an
+// open end: empty 1 top for t > 0.6, empty 2 base for t < 0.4).
+__device__ inline double cylinder_inner_cap(const device_cylinder_info& cy, const double* bi, d3 p, d3& u, d3& cpt,
+                                     unsigned int empty, double r)
+{
+    d3 cyl_pos, base, top;
+    d4 e;
+    cylinder_ends(cy, bi, cyl_pos, e, base, top);
+    const d3 ab = top - base;
+    const double t = dot(p - base, ab) / dot(ab, ab);
+    const d3 c = base + t * ab;
+    const double dist = length(p - c);
+    if (empty == 1 && t > 0.6) return 0.0;
+    if (empty == 2 && t < 0.4) return 0.0;
+    double gab = -1.0;
+    if (dist < cy.len_rr.z) {
+        const d3 o2c = cyl_pos - c;
+        const double l = length(o2c);
+        u = -(o2c / l);
+        cpt = p + r * u;
+        gab = r + l - cy.len_rr.x * 0.5;
+    }
+    return gab;
+}
+
 // ---------------------------------------------------------------- plane (impl:735-815)
 __device__ __forceinline__ double plane_detection(const device_plane_info& pe, d3 xp, d3 wp, d3& u, double r)
 {

@@ -204,6 +204,11 @@ struct FusedArgs {
     const double* tri_sphere;
     unsigned int *ms_count, *ms_id;
     double* ms_tsd;
+    // cylinders (mixed sphere scenes): bodies nplane .. nplane + ncyl - 1
+    unsigned int ncyl = 0;
+    const device_cylinder_info* cyl = nullptr;
+    unsigned int *cy_count = nullptr, *cy_id = nullptr;
+    double* cy_tsd = nullptr;
     const double* body;
     const mat_pair* mp;
     double *bsums, *wrench;
@@ -325,6 +330,12 @@ struct ContactLaunch {
     double* ms_tsd;
     const float4* mesh_bs;  // [nmesh] bounding spheres (see FusedState)
     const double* tri_sphere;  // [ntri*4] fitted sphere of every triangle (x, y, z, r)
+    // cylinders (sphere scenes): cylinder k is body nplane + k; its pair
+    // list (MAX_P2CY_COUNT slots) is updated in place like the plane list
+    unsigned int ncyl;
+    const device_cylinder_info* cyl;
+    unsigned int *cy_count, *cy_id;
+    double* cy_tsd;
     const double* body;
     const mat_pair* mp;
     const MatF* mpf;

@@ -244,16 +244,17 @@ __global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk
 // memory), the last block of a body to finish adds the chunk sums in chunk
 // order.  The order of every addition is fixed: the result does not depend
 // on which block finishes last.
-__global__ void k_body_sums(const double* bsums, unsigned int nblocks, unsigned int nplane, unsigned int rows_plane,
-                            unsigned int rows_mesh, double* wrench, double* chunk, unsigned int* done)
+__global__ void k_body_sums(const double* bsums, unsigned int nblocks, unsigned int nrow_plane_bodies,
+                            unsigned int rows_plane, unsigned int rows_mesh, double* wrench, double* chunk,
+                            unsigned int* done)
 {
     __shared__ double sm[8 * 6];
     __shared__ bool last;
     const unsigned int b = blockIdx.x / kWrenchChunks, q = blockIdx.x % kWrenchChunks;
-    // rows of body b: one per block of the kernel that does its contacts
-    // (planes: the body kernel, meshes: the pair kernel); nblocks is the
-    // row stride
-    const unsigned int rows = b < nplane ? rows_plane : rows_mesh;
+    // rows of body b, written by the kernel that does its contacts: the
+    // body kernel for planes and cylinders (the first nrow_plane_bodies
+    // bodies), the pair kernel for meshes; nblocks is the row stride
+    const unsigned int rows = b < nrow_plane_bodies ? rows_plane : rows_mesh;
     const unsigned int per = (rows + kWrenchChunks - 1) / kWrenchChunks;
     const unsigned int i0 = q * per, i1 = min(rows, i0 + per);
     double s[6] = {0, 0, 0, 0, 0, 0};
@@ -774,6 +775,9 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.tri = a.tri; c.ms_count = a.ms_count; c.ms_id = a.ms_id; c.ms_tsd = a.ms_tsd;
     c.mesh_bs = fs.d_mesh_bs;
     c.tri_sphere = a.tri_sphere;
+    c.ncyl = fs.mixed ? a.ncyl : 0u;
+    c.cyl = a.cyl;
+    c.cy_count = a.cy_count; c.cy_id = a.cy_id; c.cy_tsd = a.cy_tsd;
     c.body = a.body; c.mp = a.mp;
     // body wrench partials: one row entry per block of the emitting kernel
     // (the mixed pair and body kernels share their block size whenever the
@@ -811,7 +815,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody && c.nscene == 1) {  // batched handles keep no body wrenches
         if (a.nbody > fs.wsum_cap) return XDEM_ERR_ARG;  // fused_set_bodies sizes the chunk sums
-        k_body_sums<<<a.nbody * kWrenchChunks, 256, 0, st>>>(a.bsums, c.nblocks, a.nplane, rows_plane, rows_mesh,
+        k_body_sums<<<a.nbody * kWrenchChunks, 256, 0, st>>>(a.bsums, c.nblocks, a.nplane + c.ncyl, rows_plane, rows_mesh,
                                                              a.wrench, fs.wsum, fs.wcnt);
         ok(cudaGetLastError());
     }

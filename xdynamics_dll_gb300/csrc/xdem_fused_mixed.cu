@@ -142,6 +142,16 @@ __device__ __forceinline__ float3 to_local_f(float3 v, float4 e)
     return make_float3(r0.x * v.x + r1.x * v.y + r2.x * v.z, r0.y * v.x + r1.y * v.y + r2.y * v.z,
                        r0.z * v.x + r1.z * v.y + r2.z * v.z);
 }
+// A(e) v: body frame to global frame.
+__device__ __forceinline__ float3 to_global_f(float3 v, float4 e)
+{
+    return make_float3(2.f * ((e.x * e.x + e.y * e.y - 0.5f) * v.x + (e.y * e.z - e.x * e.w) * v.y +
+                              (e.y * e.w + e.x * e.z) * v.z),
+                       2.f * ((e.y * e.z + e.x * e.w) * v.x + (e.x * e.x + e.z * e.z - 0.5f) * v.y +
+                              (e.z * e.w - e.x * e.y) * v.z),
+                       2.f * ((e.y * e.w - e.x * e.z) * v.x + (e.z * e.w + e.x * e.y) * v.y +
+                              (e.x * e.x + e.w * e.w - 0.5f) * v.z));
+}
 __device__ __forceinline__ float3 ang_vel_f(float4 e, float4 d)
 {
     return make_float3(2.f * (-e.y * d.x + e.x * d.y - e.w * d.z + e.z * d.w),
@@ -1127,6 +1137,114 @@ __device__ __noinline__ PlaneOut plane_call(const ContactLaunch* cp, unsigned in
     return o;
 }
 
+// One sphere against cylinder k (impl:1083-1601, as the launcher kernel
+// k_cylinder runs it): the FP64 regions of cylinder_detection (side, wall
+// annulus, rim) and, for a sphere inside, the cap it faces (pair id + 1000);
+// FP32 forces with the body's mass left out of the effective mass.  Both
+// passes look their history up in the slots as they were before this
+// cylinder wrote (the launcher kernel's per-launch copy); cylinder 0
+// restarts the list, later ones append (impl:1172-1174), bounded by
+// MAX_P2CY_COUNT.  Returns true when the sphere touched the cylinder.
+__device__ __forceinline__ bool cylinder_mixed(const ContactLaunch& c, unsigned int k, unsigned int oid, d4 ip,
+                                               V3<float> ivel, V3<float> iom, float im, unsigned int& cy_cnt,
+                                               Acc& acc, float f6[6], unsigned int& bits)
+{
+    const device_dem_parameters& p = c.prm;
+    const device_cylinder_info& cy = c.cyl[k];
+    const unsigned int bidx = c.nplane + k;
+    const double* bi = c.body + 15 * bidx;
+    const MatR<float> mr = matr(c.mpf[c.nscene + bidx]);
+    const unsigned int sid = oid * MAX_P2CY_COUNT;
+    unsigned int old_id[MAX_P2CY_COUNT];
+    double2 old_t[MAX_P2CY_COUNT];
+    for (unsigned int q = 0; q < MAX_P2CY_COUNT; ++q) {
+        old_id[q] = c.cy_id[sid + q];
+        old_t[q] = reinterpret_cast<const double2*>(c.cy_tsd)[sid + q];
+    }
+    const unsigned int old_cnt = cy_cnt;
+    if (cy.id == 0) cy_cnt = 0;
+    const d3 ipos = mk3(ip.x, ip.y, ip.z);
+    const double r = ip.w;
+    bool inner = false;
+    d3 unit = mk3(0, 0, 0);
+    double cdist = cylinder_detection(cy, bi, ipos, unit, r, inner);
+    d3 cpt = ipos + r * unit;
+    const BodyF b = load_body_f(bi);
+    const float rf = d2f_rn(r);
+    bool touched = false;
+    for (int pass = 0; pass < 2; ++pass) {
+        const unsigned int pid = pass ? cy.id + 1000u : cy.id;
+        if (pass) {
+            if (!inner) break;
+            cdist = cylinder_inner_cap(cy, bi, ipos, unit, cpt, cy.empty_part, r);
+        }
+        if (!(cdist > 0)) continue;
+        float sd0 = 0.f, sd1 = 0.f;
+        for (unsigned int q = 0; q < old_cnt && q < MAX_P2CY_COUNT; ++q)
+            if (old_id[q] == pid) {
+                sd0 = d2f_rn(old_t[q].x);
+                sd1 = d2f_rn(old_t[q].y);
+                break;
+            }
+        const V3<float> un = v3<float>(d2f_rn(unit.x), d2f_rn(unit.y), d2f_rn(unit.z));
+        // lever arms: contact point from the body's reference point and from
+        // the sphere's centre (r un for the side and for the inner cap)
+        const V3<float> po2cp = v3<float>(d2f_rn(cpt.x - bi[XDEM_PX]), d2f_rn(cpt.y - bi[XDEM_PY]),
+                                          d2f_rn(cpt.z - bi[XDEM_PZ]));
+        const V3<float> rc = rf * un;
+        const V3<float> dv = (b.v + tcross(b.om, po2cp)) - (ivel + tcross(iom, rc));
+        const FC<float> fc = fconst_f(mr, p.contact_model, rf, 0.f, im, 0.f);
+        V3<float> Ft = v3<float>(0, 0, 0), Fn = v3<float>(0, 0, 0);
+        model_f(p.contact_model, fc, c.dt_f, d2f_rn(cdist), sd0, sd1, dv, un, Ft, Fn, 0.f);
+        const V3<float> mf = Fn + Ft;
+        const V3<float> mm = rf * tcross(un, Ft);  // rc parallel to Fn: only Ft turns the sphere
+        acc.f[0].add(mf.x); acc.f[1].add(mf.y); acc.f[2].add(mf.z);
+        acc.m[0].add(mm.x); acc.m[1].add(mm.y); acc.m[2].add(mm.z);
+        if (c.rolling) {
+            acc.tm = acc.tm + mm;
+            acc.rs += rf * mr.rfric * tlen(Fn);
+        }
+        const V3<float> bm = tcross(po2cp, mf);
+        f6[0] -= mf.x; f6[1] -= mf.y; f6[2] -= mf.z;
+        f6[3] -= bm.x; f6[4] -= bm.y; f6[5] -= bm.z;
+        if (cy_cnt < MAX_P2CY_COUNT) {
+            c.cy_id[sid + cy_cnt] = pid;
+            reinterpret_cast<double2*>(c.cy_tsd)[sid + cy_cnt] = make_double2(f2d(sd0), f2d(sd1));
+            cy_cnt++;
+        } else {
+            bits |= XDEM_ERR_P2CY_OVERFLOW;
+        }
+        touched = true;
+    }
+    return touched;
+}
+// ... behind a call boundary, by value in and out like plane_call (the FP64
+// region geometry and its transcendentals run for the few spheres near a
+// cylinder).
+__device__ __noinline__ PlaneOut cyl_call(const ContactLaunch* cp, unsigned int k, unsigned int oid, d4 ip, float4 Bi,
+                                          float4 Ci, unsigned int cnt)
+{
+    Acc a;
+    a.tm = v3<float>(0.f, 0.f, 0.f);
+    a.rs = 0.f;
+    float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    PlaneOut o;
+    o.bits = 0;
+    o.cnt = cnt;
+    o.touched = cylinder_mixed(*cp, k, oid, ip, v3<float>(Bi.x, Bi.y, Bi.z), v3<float>(Ci.x, Ci.y, Ci.z), Bi.w, o.cnt,
+                               a, f6, o.bits);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        o.f[i] = a.f[i].value();
+        o.m[i] = a.m[i].value();
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.w[i] = f6[i];
+    o.tm[0] = a.tm.x; o.tm[1] = a.tm.y; o.tm[2] = a.tm.z;
+    o.rs = a.rs;
+    return o;
+}
+
 // One sphere against mesh m behind a call boundary (few spheres are near a
 // mesh, and the triangle search holds three candidate arrays): the same
 // value-in, value-out form as plane_call.  Both pair kernels go through it,
@@ -1420,8 +1538,11 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
             const float lim = ipf.w + c.margin;
             return fabsf(wz) <= lim && wx >= -lim && wx <= pf.v[12] + lim && wy >= -lim && wy <= pf.v[13] + lim;
         };
-        // wrench partials: one row per warp (no block barrier in the loop)
+        // wrench partials: one row per warp (no block barrier in the loop);
+        // the rows cover ceil(nentry / 32) warps, so a warp made only of the
+        // last block's padding threads has no row and writes none
         const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
+        const bool has_row = wrow < (c.nentry + 31u) / 32u;
         for (unsigned int k = kbeg; k < kend; ++k) {
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             bool touched = false;
@@ -1444,9 +1565,65 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
                     acc.rs += o.rs;
                 }
             }
-            if (!batched) emit_warp_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + wrow) * 6);
+            if (!batched && has_row) emit_warp_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + wrow) * 6);
         }
         if (live) c.pl_count[oid] = pl_cnt;
+    }
+
+    // ------------------------------------------------ cylinders in id order (impl:1083-1601)
+    if (c.ncyl) {
+        unsigned int cy_cnt = live ? c.cy_count[oid] : 0u;
+        const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
+        const bool has_row = wrow < (c.nentry + 31u) / 32u;
+        float3 xf = make_float3(0.f, 0.f, 0.f);
+        if (live) xf = make_float3(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2]);
+        for (unsigned int k = 0; k < c.ncyl; ++k) {
+            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            bool touched = false;
+            bool near = false;
+            if (live) {
+                // conservative FP32 test: every region lies within the sphere
+                // around the middle of the axis through the rims and the wall
+                const device_cylinder_info& cy = c.cyl[k];
+                const double* bi = c.body + 15 * (c.nplane + k);
+                const float4 e = make_float4(d2f_rn(bi[XDEM_E0]), d2f_rn(bi[XDEM_E1]), d2f_rn(bi[XDEM_E2]),
+                                             d2f_rn(bi[XDEM_E3]));
+                const float hx = 0.5f * (float)(cy.pbase.x + cy.ptop.x), hy = 0.5f * (float)(cy.pbase.y + cy.ptop.y),
+                            hz = 0.5f * (float)(cy.pbase.z + cy.ptop.z);
+                const float ax = (float)(cy.ptop.x - cy.pbase.x), ay = (float)(cy.ptop.y - cy.pbase.y),
+                            az = (float)(cy.ptop.z - cy.pbase.z);
+                const float half = 0.5f * sqrtf(ax * ax + ay * ay + az * az) + (float)cy.thickness;
+                const float rad = fmaxf((float)cy.len_rr.y, (float)cy.len_rr.z) + (float)cy.thickness;
+                const float3 m = to_global_f(make_float3(hx, hy, hz), e);
+                const float dx = xf.x - (d2f_rn(bi[XDEM_PX]) - c.o_hi[0] + m.x);
+                const float dy = xf.y - (d2f_rn(bi[XDEM_PY]) - c.o_hi[1] + m.y);
+                const float dz = xf.z - (d2f_rn(bi[XDEM_PZ]) - c.o_hi[2] + m.z);
+                const float lim = sqrtf(half * half + rad * rad) * (1.f + 1e-5f) + rh + c.margin;
+                near = dx * dx + dy * dy + dz * dz <= lim * lim;
+            }
+            if (near) {
+                need_bc();
+                const PlaneOut o = cyl_call(&c, k, oid, ip, Bi, Ci, cy_cnt);
+                touched = o.touched != 0;
+                cy_cnt = o.cnt;
+                bits |= o.bits;
+                if (touched) {
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        acc.f[i].add(o.f[i]);
+                        acc.m[i].add(o.m[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 6; ++i) f6[i] = o.w[i];
+                    acc.tm = acc.tm + v3<float>(o.tm[0], o.tm[1], o.tm[2]);
+                    acc.rs += o.rs;
+                }
+            } else if (live && c.cyl[k].id == 0) {
+                cy_cnt = 0;  // cylinder 0 restarts the list whether or not it is touched
+            }
+            if (has_row) emit_warp_f(f6, touched, c.bsums + ((size_t)(c.nplane + k) * c.nblocks + wrow) * 6);
+        }
+        if (live) c.cy_count[oid] = cy_cnt;
     }
 
     if (!live) return;

@@ -349,12 +349,13 @@ PairTables pair_tables(xdem_sim* s, int kind)
 }
 
 // Steps run on the fused step (sphere scenes of either precision, and
-// mixed cluster scenes) unless the launcher path was asked for or the scene
-// has cylinders.
+// mixed cluster scenes) unless the launcher path was asked for; an FP64
+// scene with cylinders runs the launcher kernels, a mixed sphere scene with
+// cylinders the fused step's cylinder loop.
 bool fused_path(const xdem_sim* s)
 {
-    // cylinders run on the launcher kernels (FP64)
-    return !s->cfg.launcher_path && s->cylinders.empty() && (!s->clusters || s->precision_mixed());
+    if (s->cfg.launcher_path || (s->clusters && !s->precision_mixed())) return false;
+    return s->cylinders.empty() || (s->precision_mixed() && !s->clusters);
 }
 
 // The particle-pair tangential history of a mixed handle on the fused step
@@ -390,6 +391,9 @@ FusedArgs fused_args(xdem_sim* s)
     }
     a.tri = s->d_tri; a.tri_sphere = s->d_sphere;
     a.ms_count = s->ms_count; a.ms_id = s->ms_id; a.ms_tsd = s->ms_tsd;
+    a.ncyl = (unsigned int)s->cylinders.size();
+    a.cyl = s->d_cyl;
+    a.cy_count = s->cy_count; a.cy_id = s->cy_id; a.cy_tsd = s->cy_tsd;
     a.body = s->d_body; a.mp = s->d_mp;
     a.bsums = s->bsums; a.wrench = s->wrench;
     a.status = s->d_status;
@@ -994,8 +998,13 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->clusters && !s->xci) return XDEM_ERR_ARG;
-    // cylinders run on the FP64 launcher kernels only
-    if (!s->cylinders.empty() && s->precision_mixed()) return XDEM_ERR_ARG;
+    // cylinders in the mixed form: sphere scenes, one scene, no cohesion in
+    // a cylinder's material (FP64 handles run them on the launcher kernels)
+    if (!s->cylinders.empty() && s->precision_mixed()) {
+        if (s->clusters || s->nscene > 1) return XDEM_ERR_ARG;
+        for (size_t k = 0; k < s->cylinders.size(); ++k)
+            if (s->body_cp[s->planes.size() + k].coh != 0.0) return XDEM_ERR_ARG;
+    }
     // mixed clusters: the fused step's cluster form (one member count, no
     // rolling resistance or cohesion)
     if (s->clusters && s->precision_mixed()) {
