@@ -67,17 +67,21 @@ TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_dambreak_1M.json")
 
 
 def profile_traffic():
-    """DRAM bytes (read + write) per sphere of the mixed contact stage on a
-    list step, from the machine-readable summary of ncu captures
-    (profiles/traffic_dambreak_1M.json: per kernel dram__bytes_read.sum +
-    dram__bytes_write.sum of one launch, the sphere count captured, and the
-    command).  Returns (bytes per sphere, source description) or
-    (None, None) when no capture summary is present."""
+    """DRAM bytes (read + write) and warp instructions per sphere of the
+    mixed contact stage on a list step, from the machine-readable summary of
+    ncu captures (profiles/traffic_dambreak_1M.json: per kernel
+    dram__bytes_read.sum + dram__bytes_write.sum and smsp__inst_executed.sum
+    of one launch, the sphere count captured, and the command).  Returns
+    (bytes per sphere, instructions per sphere or None, source description),
+    or (None, None, None) when no capture summary is present."""
     if not os.path.exists(TRAFFIC_FILE):
-        return None, None
+        return None, None, None
     d = json.load(open(TRAFFIC_FILE))
     per = sum(k["dram_bytes"] for k in d["kernels"]) / float(d["spheres"])
-    return per, f"{os.path.basename(TRAFFIC_FILE)} ({d.get('capture', '')})"
+    inst = None
+    if all("warp_instructions" in k for k in d["kernels"]):
+        inst = sum(k["warp_instructions"] for k in d["kernels"]) / float(d["spheres"])
+    return per, inst, f"{os.path.basename(TRAFFIC_FILE)} ({d.get('capture', '')})"
 
 
 class ClockSampler:
@@ -823,7 +827,7 @@ def main():
     peak, peak_kind = load_peaks()
     b_contact = (B_CONTACT_FIXED + B_PER_CONTACT * cbar) * n
     achieved = b_contact / (rmx["contact_ms"] * 1e-3) / 1e9
-    traffic_per_sphere, tfile = profile_traffic()
+    traffic_per_sphere, inst_per_sphere, tfile = profile_traffic()
     roof = {"bound": "hbm", "kernel": "k_mixed_pairs_list + k_mixed_bodies (mixed contact stage; the list kernel "
                                       "walks the stencil on rebuild steps)", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -831,6 +835,19 @@ def main():
             "algorithmic_bytes_per_launch": b_contact,
             "bytes_model": "400 + 24 c per sphere (mixed form: 8-byte FP32 tangential history per contact)",
             "contact_kernel_ms": rmx["contact_ms"], "traffic_source": tfile}
+    # the stage is bound by instruction issue, not by HBM: its warp
+    # instructions (ncu, per sphere, times n) over the event-timed stage,
+    # against 4 issue slots a cycle on every SM at the sampled SM clock
+    issue = None
+    if inst_per_sphere:
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+        if mhz:
+            got = inst_per_sphere * n / (rmx["contact_ms"] * 1e-3)
+            pk = 4.0 * nsm * mhz * 1e6
+            issue = {"achieved": got, "peak": pk, "unit": "warp instructions/s", "frac": got / pk,
+                     "warp_instructions_per_launch": inst_per_sphere * n, "sm_count": nsm, "sm_mhz": mhz,
+                     "source": tfile}
     step_bw = (B_STEP_FIXED + B_PER_CONTACT * cbar) * n / (secsx / args.steps) / 1e9
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": warmup,
@@ -847,6 +864,7 @@ def main():
         "step_hbm": {"achieved": step_bw, "peak": peak, "frac": step_bw / peak, "unit": "GB/s",
                      "bytes_per_sphere": B_STEP_FIXED + B_PER_CONTACT * cbar},
         "roofline": roof,
+        "issue_roofline": issue,
         "e2e": e2e,
         "clocks": clocks,
         "gpu_launches": rmx["launches"],
