@@ -2,10 +2,12 @@
 
 Each .cu unit compiles in parallel with nvcc; the FP64 units use -fmad=false
 so their arithmetic rounds operation by operation like the CPU oracle.  The
-mixed-precision unit uses -fmad=false too: its FMAs are the explicit fmaf of
-the float-pair helpers, so a contact computes the same bits whether the walk,
-the candidate list or a separately compiled call evaluates it (implicit
-contraction depends on the inlining context).  Host code is compiled without
+mixed form's sphere unit uses -fmad=false too: its FMAs are the explicit fmaf
+of the float-pair helpers, so a contact computes the same bits whether the
+walk, the candidate list or a separately compiled call evaluates it
+(implicit contraction depends on the inlining context).  Its mesh and
+cluster-body unit contracts: FP64 geometry there runs on the slow FP64 pipe.
+Host code is compiled without
 contraction too (-ffp-contract=off), so host-side setup math is identical on
 x86 and Arm.
 """
@@ -32,6 +34,7 @@ UNITS = {
     "xdem_fused_host.cu": ["-fmad=false"],
     "xdem_fused_fp64.cu": ["-fmad=false"],
     "xdem_fused_mixed.cu": ["-fmad=false"],
+    "xdem_fused_mixed_mesh.cu": ["-fmad=true"],
     "xdem_noalloc.cu": [],
     "xdem_adjoint.cu": ["-fmad=false"],
     "xdem_tune.cu": [],

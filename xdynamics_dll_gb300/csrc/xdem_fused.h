@@ -365,6 +365,10 @@ __host__ __device__ inline unsigned int scene_index(const ContactLaunch& c, unsi
 
 cudaError_t launch_fused_contact_fp64(const ContactLaunch& c, cudaStream_t st);
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st);
+// The mixed pair kernels' mesh forms and the cluster body kernel
+// (xdem_fused_mixed_mesh.cu, compiled with FMA contraction).
+cudaError_t launch_mixed_mesh_pairs(const ContactLaunch& c, cudaStream_t st);
+cudaError_t launch_mixed_cluster_bodies(const ContactLaunch& c, cudaStream_t st);
 constexpr int kFusedThreads = 128;
 
 // Packed unwrapped cell coordinates: 11 bits x, 11 bits y, 10 bits z, each
