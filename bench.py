@@ -243,7 +243,10 @@ def bench_precision(scene, precision, steps, warmup, torch, dev, sampler=None, s
         sm.set_tune(**shapes)
         tune = sm.get_tune()
     else:
-        tune, _ = sm.autotune(trial_steps=10)
+        # 40 trial steps a candidate: every candidate replays the same steps
+        # from the same state, and 10 steps left shapes 3 % apart to timing
+        # noise
+        tune, _ = sm.autotune(trial_steps=40)
     sm.set_graph(True)
     if advance:
         sm.step(advance)  # untimed: the timed steps start from a developed flow
@@ -436,7 +439,7 @@ def bench_sweep(args, torch, local):
     b = batch.Batch(members, precision=T.XDEM_MIXED)
     setup_s = time.perf_counter() - t0
     stage(f"batch of {nsc} scenes, {b.combined.np_} spheres, grid {b.combined.grid}: {setup_s:.1f} s")
-    tune, _ = b.autotune(trial_steps=10)
+    tune, _ = b.autotune(trial_steps=40)
     stage("autotune: " + "/".join(str(tune[k]) for k in ("nt_pairs", "stage", "occ_pairs", "nt_bodies", "occ_bodies",
                                                          "skin_div")))
     stream = torch.cuda.Stream(device=local)
