@@ -342,15 +342,26 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
         return;
     }
     // history (impl:683-690): partner ids from the shared-memory copy of the
-    // old list, the matching history from global memory
+    // old list, the matching history from global memory.  A partner id occurs
+    // once in a list, so the slot found does not depend on where the search
+    // starts; it starts at this contact's new slot, where the partner sits
+    // whenever the contacts before it are those of the last step
     float sd0 = 0.f, sd1 = 0.f;
-    for (unsigned int q = 0; q < old_count; ++q)
-        if (old_id[q * NT] == k) {
-            // FP32 history (float2 slots in the double2 buffer)
-            const float2 t = reinterpret_cast<const float2*>(c.pp_tsd_old)[sid + q];
-            sd0 = t.x; sd1 = t.y;
-            break;
-        }
+    unsigned int hit = old_count;
+    if (cnt < old_count && old_id[cnt * NT] == k) {
+        hit = cnt;
+    } else {
+        for (unsigned int q = 0; q < old_count; ++q)
+            if (old_id[q * NT] == k) {
+                hit = q;
+                break;
+            }
+    }
+    if (hit < old_count) {
+        // FP32 history (float2 slots in the double2 buffer)
+        const float2 t = reinterpret_cast<const float2*>(c.pp_tsd_old)[sid + hit];
+        sd0 = t.x; sd1 = t.y;
+    }
     const MatR<float> mr = matr(c.mpf[scene]);
     const V3<float> unit = qdiv(rp, dist);
     const V3<float> dcpr = ir * unit;
