@@ -302,8 +302,8 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
                                              float4 Lj, float4 Bj, float4 Cj, unsigned int ux, unsigned int uy,
                                              unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
                                              unsigned int sid, unsigned int old_count, const unsigned int* old_id,
-                                             unsigned int scene, bool coh, V3<float>& Ft, V3<float>& Fn,
-                                             unsigned int& cnt, Acc& acc, unsigned int& bits)
+                                             unsigned int scene, const MatR<float>& mr, bool coh, V3<float>& Ft,
+                                             V3<float>& Fn, unsigned int& cnt, Acc& acc, unsigned int& bits)
 {
     const float cs = c.cs_f, cs_lo = c.cs_lo;
     const uint2 it = make_uint2(k, Tk);
@@ -362,7 +362,6 @@ __device__ __forceinline__ void p2p_pair_rec(const ContactLaunch& c, unsigned in
         const float2 t = reinterpret_cast<const float2*>(c.pp_tsd_old)[sid + hit];
         sd0 = t.x; sd1 = t.y;
     }
-    const MatR<float> mr = matr(c.mpf[scene]);
     const V3<float> unit = qdiv(rp, dist);
     const V3<float> dcpr = ir * unit;
     const V3<float> dcpr_j = dcpr - rp;
@@ -405,8 +404,8 @@ template <unsigned int NT>
 __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oid, unsigned int j, unsigned int ux,
                                          unsigned int uy, unsigned int uz, float4 Ai, float4 Li, float4 Bi, float4 Ci,
                                          unsigned int sid, unsigned int old_count, const unsigned int* old_id,
-                                         unsigned int scene, bool coh, V3<float>& Ft, V3<float>& Fn,
-                                         unsigned int& cnt, Acc& acc, unsigned int& bits)
+                                         unsigned int scene, const MatR<float>& mr, bool coh, V3<float>& Ft,
+                                         V3<float>& Fn, unsigned int& cnt, Acc& acc, unsigned int& bits)
 {
     const uint2 it = reinterpret_cast<const uint2*>(c.mIT)[j];
     if (c.scene_of && c.scene_of[it.x] != scene) return;  // another scene of the batch
@@ -414,8 +413,8 @@ __device__ __forceinline__ void p2p_pair(const ContactLaunch& c, unsigned int oi
     const float4 Lj = reinterpret_cast<const float4*>(c.mL)[j];
     const float4 Bj = reinterpret_cast<const float4*>(c.mB)[j];
     const float4 Cj = reinterpret_cast<const float4*>(c.mC)[j];
-    p2p_pair_rec<NT>(c, it.x, it.y, Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene, coh, Ft,
-                     Fn, cnt, acc, bits);
+    p2p_pair_rec<NT>(c, it.x, it.y, Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene, mr, coh,
+                     Ft, Fn, cnt, acc, bits);
 }
 
 // Pass 1 + 2 over the 27-cell stencil.  With `build` the screen widens by
@@ -431,6 +430,7 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
     unsigned int nlist = 0;
     unsigned int* vl = build ? c.vl_ids + (size_t)oid * kListCap : nullptr;
     const unsigned int scene = scene_index(c, oid);
+    const MatR<float> mr = matr(c.mpf[scene]);  // the pair material, once per sphere
     const bool coh = c.mpf[scene].coh != 0;
     const float cs = c.cs_f;
     const float screen = 1.0f + 0x1p-11f;
@@ -529,7 +529,7 @@ __device__ __forceinline__ void p2p_mixed(const ContactLaunch& c, unsigned int o
         cp_async_wait_all();
         // ---- pass 2: float-pair overlap and contact force, in walk order
         for (unsigned int q = 0; q < nc; ++q)
-            p2p_pair<NT>(c, oid, stage[q * NT], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
+            p2p_pair<NT>(c, oid, stage[q * NT], ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene, mr,
                      coh, Ft, Fn, cnt, acc, bits);
     }
     c.pp_count_new[oid] = cnt;
@@ -569,6 +569,7 @@ __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oi
                                          unsigned int* keys, Acc& acc, unsigned int& bits)
 {
     const unsigned int scene = scene_index(c, oid);
+    const MatR<float> mr = matr(c.mpf[scene]);  // the pair material, once per sphere
     const bool coh = false;  // lists are only kept without cohesion
     const float cs = c.cs_f;
     const float screen = 1.0f + 0x1p-11f;
@@ -624,7 +625,7 @@ __device__ __forceinline__ void p2p_list(const ContactLaunch& c, unsigned int oi
         const float4* r = c.rec + 4 * (size_t)k;
         const float4 Aj = r[kRecA], Lj = r[kRecL], Bj = r[kRecB], Cj = r[kRecC];
         p2p_pair_rec<NT>(c, k, rec_cell(Cj), Aj, Lj, Bj, Cj, ux, uy, uz, Ai, Li, Bi, Ci, sid, old_count, old_id, scene,
-                         coh, Ft, Fn, cnt, acc, bits);
+                         mr, coh, Ft, Fn, cnt, acc, bits);
     }
     c.pp_count_new[oid] = cnt;
 }
