@@ -8,6 +8,61 @@
 
 using namespace xdem;
 
+// The field-by-field form of d2f_rn that the mixed kernels used first: the
+// reference the rebias-and-round form is checked against, bit for bit.
+__device__ __forceinline__ float d2f_rn_fields(double x)
+{
+    const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
+    const unsigned int sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned int rest = lo & 0x1fffffffu;
+    const int fe = e - 896;
+    unsigned int r = ((unsigned int)fe << 23) + m;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    r = fe <= 0 ? 0u : r;
+    r = (fe >= 255 || r >= 0x7f800000u) ? 0x7f800000u : r;
+    r = e == 0x7ff ? (0x7f800000u | ((m | rest) ? 0x400000u : 0u)) : r;
+    return __uint_as_float(sign | r);
+}
+
+// Bit patterns where d2f_rn and d2f_rn_fields differ, over n doubles made on
+// the device from a counter-based hash of (seed, i): every exponent, random
+// mantissas, and the rounding boundaries (dropped bits 0x0fffffff,
+// 0x10000000, 0x10000001 with either lowest kept bit).
+__global__ void k_d2f_sweep(unsigned long long seed, unsigned long long n, unsigned long long* mismatches)
+{
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long z = (i + 1) * 0x9E3779B97F4A7C15ull ^ seed;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    unsigned long long b = z;
+    const unsigned int kind = (unsigned int)(i & 7u);
+    if (kind >= 4) {
+        const unsigned long long drop[4] = {0x0fffffffull, 0x10000000ull, 0x10000001ull, 0x1fffffffull};
+        b = (b & ~0x1fffffffull) | drop[kind - 4];
+    }
+    const double x = __longlong_as_double((long long)b);
+    if (__float_as_uint(d2f_rn(x)) != __float_as_uint(d2f_rn_fields(x))) atomicAdd(mismatches, 1ull);
+}
+
+extern "C" int d2f_sweep(unsigned long long seed, unsigned long long n, unsigned long long* mismatches)
+{
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        k_d2f_sweep<<<(unsigned int)((n + 255) / 256), 256>>>(seed, n, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? 0 : 1;
+}
+
 __global__ void k_probe(const double* x, const float* f, const float* a, const float* b, int n, float* d2f,
                         double* f2d_out, float* shi, float* slo, float* sum_hi, float* sum_lo, float* prod_hi,
                         float* prod_lo)

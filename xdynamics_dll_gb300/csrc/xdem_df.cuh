@@ -19,20 +19,23 @@
 namespace xdem {
 
 // ---------------------------------------------------------------- conversions
-// double -> float, round to nearest even, on the integer pipes.
+// double -> float, round to nearest even, on the integer pipes.  In the
+// FP32 normal range the exponent is rebiased on the high word (the bias has
+// no low-word bits) and the 29 dropped mantissa bits are rounded by adding
+// 0x0fffffff plus the lowest kept bit, so that a halfway case rounds to
+// even; a carry runs on into the exponent, reaching 0x7f800000 (infinity)
+// past FLT_MAX.  Two compares of the high word pick the flushed zero, the
+// overflow infinity and NaN.
 __device__ __forceinline__ float d2f_rn(double x)
 {
     const unsigned int hi = (unsigned int)__double2hiint(x), lo = (unsigned int)__double2loint(x);
     const unsigned int sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu);
-    const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 mantissa bits
-    const unsigned int rest = lo & 0x1fffffffu;                   // 29 dropped bits
-    const int fe = e - 896;                                       // FP32 biased exponent
-    unsigned int r = ((unsigned int)fe << 23) + m;
-    r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
-    r = fe <= 0 ? 0u : r;
-    r = (fe >= 255 || r >= 0x7f800000u) ? 0x7f800000u : r;
-    r = e == 0x7ff ? (0x7f800000u | ((m | rest) ? 0x400000u : 0u)) : r;
+    const unsigned int ah = hi & 0x7fffffffu;  // high word of |x|
+    const unsigned long long t = ((unsigned long long)(ah - (896u << 20)) << 32) | lo;
+    unsigned int r = (unsigned int)((t + 0x0fffffffull + ((lo >> 29) & 1u)) >> 29);
+    r = ah < (897u << 20) ? 0u : r;           // below FLT_MIN: a signed zero
+    r = ah >= (1151u << 20) ? 0x7f800000u : r;  // beyond FLT_MAX, infinity
+    r = (ah > 0x7ff00000u || (ah == 0x7ff00000u && lo != 0u)) ? 0x7fc00000u : r;  // NaN
     return __uint_as_float(sign | r);
 }
 
