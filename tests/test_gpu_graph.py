@@ -49,3 +49,28 @@ def test_graph_replay_matches_eager(simmod, precision):
     assert a.status() == 0 and b.status() == 0
     a.close()
     b.close()
+
+
+def test_mixed_fp32_copies_are_written_back_before_a_restart(simmod):
+    """A mixed sphere handle keeps its accelerations in FP32 copies between
+    steps and writes them back to the FP64 arrays before anything reads
+    those.  Re-setting the pair lists makes the next step start over from the
+    FP64 arrays (the first position update reads them): with a state read
+    before it (write-back on the read) and without one (write-back inside the
+    step) the runs stay bit-identical, graphs or not."""
+    sc = scenes.dam_break(n_target=3000)
+    hs = [simmod.Sim(sc, precision=T.XDEM_MIXED) for _ in range(3)]
+    hs[2].set_graph(True)
+    for h in hs:
+        h.step(7)
+    hs[0].state()
+    for h in hs:
+        for kind in range(2):
+            cnt, ids, tsd = h.pairs(kind)
+            h.set_pairs(kind, cnt, ids, tsd)
+        h.step(9)
+    _same(hs[0], hs[1])
+    _same(hs[0], hs[2])
+    for h in hs:
+        assert h.status() == 0
+        h.close()

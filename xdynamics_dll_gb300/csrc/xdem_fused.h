@@ -138,6 +138,15 @@ struct FusedState {
     // parts), B (velocity, mass), C (spin, packed cell bits in w) -- a
     // neighbour's record is two sectors
     float4* rec = nullptr;      // [np*4]
+    // FP32 copies of a mixed sphere handle's acceleration, Euler-parameter
+    // acceleration, and principal inertia + mass (np entries each): the body
+    // kernel reads and writes these instead of the FP64 arrays, which are
+    // brought up to date only when something reads them.  f32_ready: the
+    // copies hold the state; f64_stale: the FP64 acc and ea arrays lag them.
+    float4* accf = nullptr;
+    float4* eaf = nullptr;
+    float4* jm = nullptr;
+    bool f32_ready = false, f64_stale = false;
     float* fA = nullptr;        // [np*4] particle-particle force, rolling resistance (original order)
     float* fB = nullptr;        // [np*4] particle-particle moment
     float* fC = nullptr;        // [np*4] rolling: sum of contact moments
@@ -230,6 +239,12 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
                 unsigned int ns = 0);
 void fused_free(FusedState& fs);
 void fused_invalidate(FusedState& fs);
+// The handle's state arrays were written from outside the step (state
+// upload, restore): the next step starts over and refreshes the FP32 copies.
+void fused_state_written(FusedState& fs);
+// Brings the FP64 acc and ea arrays up to date from the FP32 copies before
+// something reads them (np sphere entries).
+int fused_sync_fp64(FusedState& fs, double* acc, double* ea, cudaStream_t st);
 // host_mp holds nscene particle-pair entries followed by one per body.
 int fused_set_bodies(FusedState& fs, const device_plane_info* planes, unsigned int nplane, const double* body,
                      const mat_pair* mp, const device_plane_info* host_planes, const mat_pair* host_mp,
@@ -310,6 +325,8 @@ struct ContactLaunch {
     double* ep_next;
     double *vel, *acc, *ev, *ea;
     const double *mass, *inertia;
+    float4 *accf, *eaf;         // FP32 copies (see FusedState), sphere handles
+    const float4* jm;
     unsigned int *k_out, *v_out;
     // contacts
     bool has_pp;

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "xdem_device.cuh"
+#include "xdem_df.cuh"
 #include "xdem_fused.h"
 #include "xdem_kernels.h"
 
@@ -394,6 +395,10 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.mC, (size_t)nentry * 4);
         if (e == cudaSuccess) e = dalloc(fs.mIT, (size_t)nentry * 2);
         if (e == cudaSuccess) e = dalloc(fs.rec, (size_t)np * 4);
+        if (e == cudaSuccess) e = dalloc(fs.accf, np);
+        if (e == cudaSuccess) e = dalloc(fs.eaf, np);
+        if (e == cudaSuccess) e = dalloc(fs.jm, np);
+        fs.f32_ready = fs.f64_stale = false;
         if (e == cudaSuccess) e = dalloc(fs.fA, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.fB, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.fC, (size_t)np * 4);
@@ -431,7 +436,7 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
 void fused_free(FusedState& fs)
 {
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.cpos_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
-                  fs.mC, fs.mIT, fs.rec, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
+                  fs.mC, fs.mIT, fs.rec, fs.accf, fs.eaf, fs.jm, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
                   fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag,
                   fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf, fs.wsum, fs.wcnt,
                   fs.d_mesh_bs};
@@ -442,6 +447,61 @@ void fused_free(FusedState& fs)
 }
 
 void fused_invalidate(FusedState& fs) { fs.primed = false; }
+
+void fused_state_written(FusedState& fs)
+{
+    fs.primed = false;
+    fs.f32_ready = false;
+    fs.f64_stale = false;
+}
+
+namespace {
+
+// FP64 state -> FP32 copies of a mixed sphere handle (d2f_rn, as the body
+// kernel rounds them when it reads the FP64 arrays).
+__global__ void k_state_to_f32(const double* acc, const double* ea, const double* inertia, const double* mass,
+                               float4* accf, float4* eaf, float4* jm, unsigned int n)
+{
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    accf[i] = make_float4(d2f_rn(acc[3 * (size_t)i]), d2f_rn(acc[3 * (size_t)i + 1]), d2f_rn(acc[3 * (size_t)i + 2]),
+                          0.f);
+    eaf[i] = make_float4(d2f_rn(ea[4 * (size_t)i]), d2f_rn(ea[4 * (size_t)i + 1]), d2f_rn(ea[4 * (size_t)i + 2]),
+                         d2f_rn(ea[4 * (size_t)i + 3]));
+    jm[i] = make_float4(d2f_rn(inertia[3 * (size_t)i]), d2f_rn(inertia[3 * (size_t)i + 1]),
+                        d2f_rn(inertia[3 * (size_t)i + 2]), d2f_rn(mass[i]));
+}
+
+// FP32 copies -> FP64 acc and ea (exact).
+__global__ void k_state_to_f64(const float4* accf, const float4* eaf, double* acc, double* ea, unsigned int n)
+{
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = accf[i], q = eaf[i];
+    acc[3 * (size_t)i] = f2d(a.x); acc[3 * (size_t)i + 1] = f2d(a.y); acc[3 * (size_t)i + 2] = f2d(a.z);
+    ea[4 * (size_t)i] = f2d(q.x); ea[4 * (size_t)i + 1] = f2d(q.y); ea[4 * (size_t)i + 2] = f2d(q.z);
+    ea[4 * (size_t)i + 3] = f2d(q.w);
+}
+
+// A conversion must not land in a step graph: it is a host decision of one
+// step, not part of every replay.
+bool capturing(cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+
+}  // namespace
+
+int fused_sync_fp64(FusedState& fs, double* acc, double* ea, cudaStream_t st)
+{
+    if (!fs.f64_stale) return XDEM_OK;
+    if (capturing(st)) return XDEM_ERR_ARG;
+    k_state_to_f64<<<blocks_for(fs.np), kThreads, 0, st>>>(fs.accf, fs.eaf, acc, ea, fs.np);
+    if (cudaGetLastError() != cudaSuccess) return XDEM_ERR_CUDA;
+    fs.f64_stale = false;
+    return XDEM_OK;
+}
 
 namespace {
 
@@ -600,6 +660,19 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     if (clusters && (!fs.mixed || !fs.cpos_alt || !a.cpos || !a.rloc || !a.cl.neach ||
                      (unsigned long long)a.cl.ns * a.cl.neach != np))
         return XDEM_ERR_ARG;
+    // a mixed sphere handle keeps acc and ea in FP32 copies: the first
+    // position update reads the FP64 arrays, the body kernel the copies
+    const bool f32_state = fs.mixed && !clusters;
+    if (f32_state && !fs.primed && fs.f64_stale) {
+        if (int r = fused_sync_fp64(fs, a.acc, a.ea, st)) return r;
+    }
+    if (f32_state && !fs.f32_ready) {
+        if (capturing(st)) return XDEM_ERR_ARG;
+        k_state_to_f32<<<blocks_for(np), kThreads, 0, st>>>(a.acc, a.ea, a.inertia, a.mass, fs.accf, fs.eaf, fs.jm,
+                                                             np);
+        ok(cudaGetLastError());
+        fs.f32_ready = true;
+    }
     if (!fs.primed) {
         // empty cell table, first position update + hash, and the extent of
         // the FP32 frame (grid origin to the far side of the particle cloud)
@@ -761,6 +834,9 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.sorted_index = a.sorted_index; c.cstart = a.cstart; c.cend = a.cend; c.skey = fs.skey_prev;
     c.pos_cur = *a.pos; c.pos_next = fs.pos_alt; c.ep_cur = *a.ep; c.ep_next = fs.ep_alt;
     c.vel = a.vel; c.acc = a.acc; c.ev = a.ev; c.ea = a.ea; c.mass = a.mass; c.inertia = a.inertia;
+    c.accf = f32_state ? fs.accf : nullptr;
+    c.eaf = f32_state ? fs.eaf : nullptr;
+    c.jm = f32_state ? fs.jm : nullptr;
     c.k_out = a.k0; c.v_out = a.v0;
     c.has_pp = a.has_pp;
     c.pp_count_old = *a.pp_count; c.pp_id_old = *a.pp_id; c.pp_tsd_old = *a.pp_tsd;
@@ -809,6 +885,7 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.scene_plane_first = c.nscene > 1 ? a.scene_plane_first : nullptr;
     if (e0) cudaEventRecord(e0, st);
     ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
+    if (f32_state) fs.f64_stale = true;
     // the mixed contact stage is two kernels (pairs, bodies), with candidate
     // lists three (list pairs, bodies, flag roll)
     if (fs.mixed) nl += c.use_list ? 2 : 1;

@@ -976,27 +976,49 @@ __device__ __forceinline__ bool mesh_mixed(const ContactLaunch& c, unsigned int 
 // additions of FP32 increments to the FP64 state.  The Euler parameters are
 // renormalised to second order, 1/sqrt(1 + eps) ~ 1 - eps/2 + 3/8 eps^2,
 // with eps = |e + de|^2 - 1 formed in float pairs from the FP64 e.
-// Writes vel, acc, ev, ea and ep_next of body i; returns the next centre,
-// the next Euler parameters (FP64, as stored, and FP32), their new rates and
-// the new velocity in FP32.
+// Writes vel, ev and ep_next of body i, and its new acceleration and Euler-
+// parameter acceleration: to the FP32 copies (F32: spheres) or to the FP64
+// arrays (clusters); returns the next centre, the next Euler parameters
+// (FP64, as stored, and FP32), their new rates and the new velocity in FP32.
 struct NextBody {
     d3 x;
     d4 e;
     float4 ef, ev;
     V3<float> v;
 };
-// The state integrate_f reads for body i (FP64, reference layout).
+// The state integrate_f reads for body i: velocity, Euler parameters and
+// their rates in FP64; acceleration, Euler-parameter acceleration and
+// principal inertia in FP32 (the step computes the accelerations in FP32, so
+// they are exact in either storage).
 struct BodyIn {
-    d3 v, a, J;
-    d4 e, ev, ea;
+    d3 v;
+    d4 e, ev;
+    float3 a, J;
+    float4 ea;
 };
+// From the FP64 arrays of the reference layout (clusters).
 __device__ __forceinline__ BodyIn body_in(const ContactLaunch& c, unsigned int i)
 {
     BodyIn b;
-    b.v = ld3(c.vel, i); b.a = ld3(c.acc, i); b.J = ld3(c.inertia, i);
-    b.e = ld4(c.ep_cur, i); b.ev = ld4(c.ev, i); b.ea = ld4(c.ea, i);
+    b.v = ld3(c.vel, i); b.a = d2f3(ld3(c.acc, i)); b.J = d2f3(ld3(c.inertia, i));
+    b.e = ld4(c.ep_cur, i); b.ev = ld4(c.ev, i); b.ea = d2f4(ld4(c.ea, i));
     return b;
 }
+// From the FP32 copies of a sphere handle (acc, ea, and inertia + mass);
+// m receives the mass.
+__device__ __forceinline__ BodyIn body_in_f32(const ContactLaunch& c, unsigned int i, float& m)
+{
+    BodyIn b;
+    b.v = ld3(c.vel, i);
+    b.e = ld4(c.ep_cur, i); b.ev = ld4(c.ev, i);
+    const float4 a = c.accf[i], jm = c.jm[i];
+    b.a = make_float3(a.x, a.y, a.z);
+    b.J = make_float3(jm.x, jm.y, jm.z);
+    b.ea = c.eaf[i];
+    m = jm.w;
+    return b;
+}
+template <bool F32>
 __device__ __forceinline__ NextBody integrate_f(const ContactLaunch& c, unsigned int i, d3 xi, float m,
                                                 V3<float> Ff, V3<float> Mf, bool apply_vel, const BodyIn& in)
 {
@@ -1008,23 +1030,29 @@ __device__ __forceinline__ NextBody integrate_f(const ContactLaunch& c, unsigned
     const d3 v = in.v;
     V3<float> vn = vf(d2f3(v));
     if (apply_vel) {
-        const V3<float> dv = hdt * (vf(d2f3(in.a)) + a_new);
+        const V3<float> dv = hdt * (vf(in.a) + a_new);
         st3(c.vel, i, mk3(v.x + f2d(dv.x), v.y + f2d(dv.y), v.z + f2d(dv.z)));
         vn = vn + dv;
     }
-    st3(c.acc, i, mk3(f2d(a_new.x), f2d(a_new.y), f2d(a_new.z)));
+    if (F32)
+        c.accf[i] = make_float4(a_new.x, a_new.y, a_new.z, 0.f);
+    else
+        st3(c.acc, i, mk3(f2d(a_new.x), f2d(a_new.y), f2d(a_new.z)));
     // rotation
     const d4 e = in.e;
     const df e0 = split_d(e.x), e1 = split_d(e.y), e2 = split_d(e.z), e3 = split_d(e.w);
     const float4 ef = make_float4(df_f(e0), df_f(e1), df_f(e2), df_f(e3));
     const d4 ev = in.ev;
     const float4 evf = d2f4(ev);
-    const float4 eaf = d2f4(in.ea);
-    const float3 J = d2f3(in.J);
+    const float4 eaf = in.ea;
+    const float3 J = in.J;
     const float4 q = uceom_f(J, ef, evf, to_local_f(make_float3(Mf.x, Mf.y, Mf.z), ef));
     const float4 dev = make_float4(hdt * (eaf.x + q.x), hdt * (eaf.y + q.y), hdt * (eaf.z + q.z), hdt * (eaf.w + q.w));
     st4(c.ev, i, mk4(ev.x + f2d(dev.x), ev.y + f2d(dev.y), ev.z + f2d(dev.z), ev.w + f2d(dev.w)));
-    st4(c.ea, i, mk4(f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w)));
+    if (F32)
+        c.eaf[i] = q;
+    else
+        st4(c.ea, i, mk4(f2d(q.x), f2d(q.y), f2d(q.z), f2d(q.w)));
     const float4 evn = make_float4(evf.x + dev.x, evf.y + dev.y, evf.z + dev.z, evf.w + dev.w);
     const float4 de = make_float4(dt * evn.x + h2 * q.x, dt * evn.y + h2 * q.y, dt * evn.z + h2 * q.z,
                                   dt * evn.w + h2 * q.w);
@@ -1117,7 +1145,7 @@ __device__ __forceinline__ void mixed_tail(const ContactLaunch& c, unsigned int 
                                            float m, V3<float> Ff, V3<float> Mf, unsigned int& bits,
                                            const BodyIn& in)
 {
-    const NextBody nx = integrate_f(c, oid, mk3(ip.x, ip.y, ip.z), m, Ff, Mf, !c.vel_compat, in);
+    const NextBody nx = integrate_f<true>(c, oid, mk3(ip.x, ip.y, ip.z), m, Ff, Mf, !c.vel_compat, in);
     st4(c.pos_next, oid, mk4(nx.x.x, nx.x.y, nx.x.z, ip.w));
     const df X[3] = {df_sub(split_d(nx.x.x), df{c.o_hi[0], c.o_lo[0]}),
                      df_sub(split_d(nx.x.y), df{c.o_hi[1], c.o_lo[1]}),
@@ -1505,6 +1533,90 @@ __global__ void k_vl_roll(unsigned int* flag)
 // id order), rolling resistance, the velocity and position update and the
 // next step's records, on top of kernel 1's particle-particle sums.
 // OCC / NT blocks per SM (OCC 512: 128 registers a thread, 768: 80, 1024: 64).
+// The sphere body kernel's cylinder loop behind a call boundary: its vote,
+// FP64 region calls and wrench rows would otherwise raise the register
+// allocation of the whole kernel, also for scenes without cylinders.  The
+// caller's running sums come in and go out by value, so every addition
+// happens in the same order as inline.  Every lane of the warp calls it.
+struct CylsOut {
+    Acc acc;
+    unsigned int bits;
+    float4 Bi, Ci;
+    int have_bc;
+};
+template <unsigned int NT>
+__device__ __noinline__ CylsOut cylinders_call(const ContactLaunch* cp, unsigned int oid, bool live, d4 ip, float rh,
+                                               float4 Bi, float4 Ci, bool have_bc, Acc acc, unsigned int bits)
+{
+    const ContactLaunch& c = *cp;
+    auto need_bc = [&]() {
+        if (have_bc) return;
+        const float4* r = c.rec + 4 * (size_t)oid;
+        Bi = r[kRecB];
+        Ci = r[kRecC];
+        have_bc = true;
+    };
+    unsigned int cy_cnt = live ? c.cy_count[oid] : 0u;
+    const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
+    const bool has_row = wrow < (c.nentry + 31u) / 32u;
+    float3 xf = make_float3(0.f, 0.f, 0.f);
+    if (live) xf = make_float3(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2]);
+    for (unsigned int k = 0; k < c.ncyl; ++k) {
+        float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        bool touched = false;
+        bool near = false;
+        if (live) {
+            // conservative FP32 test: every region lies within the sphere
+            // around the middle of the axis through the rims and the wall
+            const device_cylinder_info& cy = c.cyl[k];
+            const double* bi = c.body + 15 * (c.nplane + k);
+            const float4 e = make_float4(d2f_rn(bi[XDEM_E0]), d2f_rn(bi[XDEM_E1]), d2f_rn(bi[XDEM_E2]),
+                                         d2f_rn(bi[XDEM_E3]));
+            const float hx = 0.5f * (float)(cy.pbase.x + cy.ptop.x), hy = 0.5f * (float)(cy.pbase.y + cy.ptop.y),
+                        hz = 0.5f * (float)(cy.pbase.z + cy.ptop.z);
+            const float ax = (float)(cy.ptop.x - cy.pbase.x), ay = (float)(cy.ptop.y - cy.pbase.y),
+                        az = (float)(cy.ptop.z - cy.pbase.z);
+            const float half = 0.5f * sqrtf(ax * ax + ay * ay + az * az) + (float)cy.thickness;
+            const float rad = fmaxf((float)cy.len_rr.y, (float)cy.len_rr.z) + (float)cy.thickness;
+            const float3 m = to_global_f(make_float3(hx, hy, hz), e);
+            const float dx = xf.x - (d2f_rn(bi[XDEM_PX]) - c.o_hi[0] + m.x);
+            const float dy = xf.y - (d2f_rn(bi[XDEM_PY]) - c.o_hi[1] + m.y);
+            const float dz = xf.z - (d2f_rn(bi[XDEM_PZ]) - c.o_hi[2] + m.z);
+            const float lim = sqrtf(half * half + rad * rad) * (1.f + 1e-5f) + rh + c.margin;
+            near = dx * dx + dy * dy + dz * dz <= lim * lim;
+        }
+        if (near) {
+            need_bc();
+            const PlaneOut o = cyl_call(&c, k, oid, ip, Bi, Ci, cy_cnt);
+            touched = o.touched != 0;
+            cy_cnt = o.cnt;
+            bits |= o.bits;
+            if (touched) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    acc.f[i].add(o.f[i]);
+                    acc.m[i].add(o.m[i]);
+                }
+#pragma unroll
+                for (int i = 0; i < 6; ++i) f6[i] = o.w[i];
+                acc.tm = acc.tm + v3<float>(o.tm[0], o.tm[1], o.tm[2]);
+                acc.rs += o.rs;
+            }
+        } else if (live && c.cyl[k].id == 0) {
+            cy_cnt = 0;  // cylinder 0 restarts the list whether or not it is touched
+        }
+        if (has_row) emit_warp_f(f6, touched, c.bsums + ((size_t)(c.nplane + k) * c.nblocks + wrow) * 6);
+    }
+    if (live) c.cy_count[oid] = cy_cnt;
+    CylsOut o;
+    o.acc = acc;
+    o.bits = bits;
+    o.Bi = Bi;
+    o.Ci = Ci;
+    o.have_bc = have_bc ? 1 : 0;
+    return o;
+}
+
 template <unsigned int NT, unsigned int OCC>
 __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
 {
@@ -1600,58 +1712,12 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
 
     // ------------------------------------------------ cylinders in id order (impl:1083-1601)
     if (c.ncyl) {
-        unsigned int cy_cnt = live ? c.cy_count[oid] : 0u;
-        const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
-        const bool has_row = wrow < (c.nentry + 31u) / 32u;
-        float3 xf = make_float3(0.f, 0.f, 0.f);
-        if (live) xf = make_float3(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2]);
-        for (unsigned int k = 0; k < c.ncyl; ++k) {
-            float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            bool touched = false;
-            bool near = false;
-            if (live) {
-                // conservative FP32 test: every region lies within the sphere
-                // around the middle of the axis through the rims and the wall
-                const device_cylinder_info& cy = c.cyl[k];
-                const double* bi = c.body + 15 * (c.nplane + k);
-                const float4 e = make_float4(d2f_rn(bi[XDEM_E0]), d2f_rn(bi[XDEM_E1]), d2f_rn(bi[XDEM_E2]),
-                                             d2f_rn(bi[XDEM_E3]));
-                const float hx = 0.5f * (float)(cy.pbase.x + cy.ptop.x), hy = 0.5f * (float)(cy.pbase.y + cy.ptop.y),
-                            hz = 0.5f * (float)(cy.pbase.z + cy.ptop.z);
-                const float ax = (float)(cy.ptop.x - cy.pbase.x), ay = (float)(cy.ptop.y - cy.pbase.y),
-                            az = (float)(cy.ptop.z - cy.pbase.z);
-                const float half = 0.5f * sqrtf(ax * ax + ay * ay + az * az) + (float)cy.thickness;
-                const float rad = fmaxf((float)cy.len_rr.y, (float)cy.len_rr.z) + (float)cy.thickness;
-                const float3 m = to_global_f(make_float3(hx, hy, hz), e);
-                const float dx = xf.x - (d2f_rn(bi[XDEM_PX]) - c.o_hi[0] + m.x);
-                const float dy = xf.y - (d2f_rn(bi[XDEM_PY]) - c.o_hi[1] + m.y);
-                const float dz = xf.z - (d2f_rn(bi[XDEM_PZ]) - c.o_hi[2] + m.z);
-                const float lim = sqrtf(half * half + rad * rad) * (1.f + 1e-5f) + rh + c.margin;
-                near = dx * dx + dy * dy + dz * dz <= lim * lim;
-            }
-            if (near) {
-                need_bc();
-                const PlaneOut o = cyl_call(&c, k, oid, ip, Bi, Ci, cy_cnt);
-                touched = o.touched != 0;
-                cy_cnt = o.cnt;
-                bits |= o.bits;
-                if (touched) {
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) {
-                        acc.f[i].add(o.f[i]);
-                        acc.m[i].add(o.m[i]);
-                    }
-#pragma unroll
-                    for (int i = 0; i < 6; ++i) f6[i] = o.w[i];
-                    acc.tm = acc.tm + v3<float>(o.tm[0], o.tm[1], o.tm[2]);
-                    acc.rs += o.rs;
-                }
-            } else if (live && c.cyl[k].id == 0) {
-                cy_cnt = 0;  // cylinder 0 restarts the list whether or not it is touched
-            }
-            if (has_row) emit_warp_f(f6, touched, c.bsums + ((size_t)(c.nplane + k) * c.nblocks + wrow) * 6);
-        }
-        if (live) c.cy_count[oid] = cy_cnt;
+        const CylsOut co = cylinders_call<NT>(&c, oid, live, ip, rh, Bi, Ci, have_bc, acc, bits);
+        acc = co.acc;
+        bits = co.bits;
+        Bi = co.Bi;
+        Ci = co.Ci;
+        have_bc = co.have_bc != 0;
     }
 
     if (!live) return;
@@ -1673,7 +1739,9 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
         }
     }
     const V3<float> Ff = v3<float>(acc.f[0].value(), acc.f[1].value(), acc.f[2].value());
-    mixed_tail(c, oid, ip, rh, d2f_rn(ip.w - f2d(rh)), d2f_rn(c.mass[oid]), Ff, Mf, bits, body_in(c, oid));
+    float m;
+    const BodyIn in = body_in_f32(c, oid, m);
+    mixed_tail(c, oid, ip, rh, d2f_rn(ip.w - f2d(rh)), m, Ff, Mf, bits, in);
 }
 
 // Kernel 2 for clusters (impl:817-948, 224-287, 149-190): one thread per
@@ -1768,7 +1836,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_cluster_bodies(const __g
     // ------------------------------------------------ integration (impl:224-287, 149-190)
     const V3<float> Ff = v3<float>(F[0].value(), F[1].value(), F[2].value());
     const V3<float> Mf = v3<float>(M[0].value(), M[1].value(), M[2].value());
-    const NextBody nx = integrate_f(c, cid, mk3(xc.x, xc.y, xc.z), m, Ff, Mf, true, body_in(c, cid));
+    const NextBody nx = integrate_f<false>(c, cid, mk3(xc.x, xc.y, xc.z), m, Ff, Mf, true, body_in(c, cid));
     st4(c.cpos_next, cid, mk4(nx.x.x, nx.x.y, nx.x.z, xc.w));
     // A(e) of the next Euler parameters in float pairs (rows as rot_rows)
     const df e0 = split_d(nx.e.x), e1 = split_d(nx.e.y), e2 = split_d(nx.e.z), e3 = split_d(nx.e.w);

@@ -662,7 +662,7 @@ XDEM_API int xdem_sim_set_state(xdem_sim* s, const double* pos, const double* ve
     H(s->mass, mass, ns, 0, 0, 0);
     H(s->inertia, inertia, ns * 3, 0, 0, 0);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-    fused_invalidate(s->fs);
+    fused_state_written(s->fs);
     return cerr(e);
 }
 
@@ -1054,6 +1054,9 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
                 if (g >= 0) {
                     const cudaError_t e = cudaGraphLaunch(s->graphs[g].exec, s->st);
                     if (e != cudaSuccess) return cerr(e);
+                    // a replay runs no host code: a mixed sphere step wrote
+                    // its accelerations to the FP32 copies only
+                    if (s->fs.mixed && !s->clusters) s->fs.f64_stale = true;
                     if (!captured) step_swaps(s);
                     s->launches += s->graphs[g].launches;
                     s->cells_clean = true;
@@ -1119,6 +1122,8 @@ XDEM_API int xdem_sim_get_state(xdem_sim* s, double* pos, double* vel, double* a
 {
     if (!s) return XDEM_ERR_ARG;
     const size_t n = s->np, ns = s->ns;
+    // a mixed sphere handle's acc and ea live in FP32 copies between steps
+    if (int r = fused_sync_fp64(s->fs, s->acc, s->ea, s->st)) return r;
     cudaError_t e = cudaStreamSynchronize(s->st);
     auto D = [&](double* h, const double* d, size_t cnt) {
         if (e == cudaSuccess && h && d) e = cudaMemcpy(h, d, cnt * sizeof(double), cudaMemcpyDeviceToHost);

@@ -22,6 +22,9 @@ struct Snapshot {
     std::vector<void**> live;                     // the handle fields copied, in order
     cudaError_t take(xdem_sim* s)
     {
+        // the FP64 acc and ea arrays are what is copied: bring them up to
+        // date from a mixed sphere handle's FP32 copies first
+        if (fused_sync_fp64(s->fs, s->acc, s->ea, s->st) != XDEM_OK) return cudaErrorInvalidValue;
         const size_t n = s->np, ns = s->ns;
         const size_t bytes[] = {n * 32, ns * 24, ns * 24, ns * 32, ns * 32, ns * 32,
                                 n * 4, n * MAX_P2P_COUNT * 4, n * MAX_P2P_COUNT * 16,
@@ -56,7 +59,7 @@ struct Snapshot {
         for (size_t i = 0; i < bufs.size() && e == cudaSuccess; ++i)
             e = cudaMemcpyAsync(*live[i], bufs[i].first, bufs[i].second, cudaMemcpyDeviceToDevice, s->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-        fused_invalidate(s->fs);
+        fused_state_written(s->fs);
         return e;
     }
     ~Snapshot()
