@@ -67,6 +67,9 @@ enum {
                                          (the reference writes on past the
                                          particle's slots; here they are
                                          dropped and this bit is raised)     */
+    XDEM_ERR_BARRIER       = 1 << 6,  /* a grid barrier of the persistent
+                                         batched step waited past its time
+                                         limit; the step is incomplete       */
     XDEM_ERR_CUDA          = 1 << 8,  /* a CUDA runtime call failed          */
     XDEM_ERR_ARG           = 1 << 9,  /* invalid argument (null, size, mode) */
     XDEM_ERR_NOT_SET       = 1 << 10, /* setDEMSymbolicParameter not called  */
@@ -513,6 +516,19 @@ XDEM_API int xdem_sim_set_profiling(xdem_sim* sim, int on);
  * instead of about 14 kernel launches.  Profiling (xdem_sim_set_profiling)
  * runs the steps eagerly.  Results are identical either way. */
 XDEM_API int xdem_sim_set_graph(xdem_sim* sim, int on);
+/* Persistent batched step: with on != 0, each list step of a batched mixed
+ * handle (xdem_sim_set_scenes, candidate lists) is one cooperative kernel
+ * launch -- the gated cell sort, the particle-pair phase, the body phase and
+ * the list-flag roll separated by grid barriers -- instead of four to
+ * sixteen kernels; with xdem_sim_set_graph the step graph holds that one
+ * kernel (after a memset of the barrier's two words).  Results are identical
+ * either way.  Each barrier waits at most barrier_limit_ns (0: one second)
+ * on the GPU's global timer; a block that waits longer raises
+ * XDEM_ERR_BARRIER in the status and the kernel returns, leaving the step
+ * incomplete (restore a state, e.g. with xdem_sim_set_state, to go on).
+ * Other handles and the first step after a new state run the usual
+ * kernels.  Returns XDEM_OK or XDEM_ERR_ARG. */
+XDEM_API int xdem_sim_set_persistent(xdem_sim* sim, int on, unsigned long long barrier_limit_ns);
 XDEM_API int xdem_sim_profile(xdem_sim* sim, unsigned int* launches,
                               double* contact_ms, unsigned int* contact_launches);
 

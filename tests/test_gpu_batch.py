@@ -96,3 +96,89 @@ def test_batch_graph_replay_is_identical(mods):
         assert np.array_equal(sa[k], sg[k]), k
     a.close()
     g.close()
+
+
+def _list_batch(batch, members, persist=False, graph=False):
+    b = batch.Batch(members, precision=T.XDEM_MIXED)
+    b.sim.set_tune(nt_pairs=64, stage=16, nt_bodies=64, occ_pairs=768, occ_bodies=1024, skin_div=32)
+    if persist:
+        b.set_persistent(True)
+    if graph:
+        b.set_graph(True)
+    return b
+
+
+def _same(a, b):
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+    for kind in range(2):
+        for x, y in zip(a.pairs(kind), b.pairs(kind)):
+            assert np.array_equal(x, y), kind
+
+
+def test_persistent_step_matches_kernels(mods):
+    """A batched list step as one cooperative launch (xdem_sim_set_persistent:
+    gated sort, pair phase, body phase and flag roll behind grid barriers)
+    against the same steps as separate kernels: states and pair lists bit for
+    bit, eager and replayed from a graph, over steps that rebuild the
+    candidate lists; one kernel per step."""
+    batch, _ = mods
+    members = _members()
+    ref = _list_batch(batch, members)
+    per = _list_batch(batch, members, persist=True)
+    pg = _list_batch(batch, members, persist=True, graph=True)
+    # the columns start at rest: a seeded random velocity (the same in all
+    # three) makes spheres cross half the skin within tens of steps, so the
+    # lists are rebuilt on motion (those steps clear the last sort's cells,
+    # sort and reorder inside the kernel)
+    st = ref.sim.state()
+    vel = st["vel"] + np.random.default_rng(7).uniform(-0.2, 0.2, st["vel"].shape)
+    for b in (ref, per, pg):
+        b.sim.set_state(st["pos"], vel, st["acc"], st["ep"], st["ev"], st["ea"], b.combined.mass,
+                        b.combined.inertia)
+    for n in (1, 5, 20, 54, 120):
+        for b in (ref, per, pg):
+            b.step(n)
+        _same(ref.sim, per.sim)
+        _same(ref.sim, pg.sim)
+    assert per.sim.list_rebuilds() == ref.sim.list_rebuilds() >= 1
+    for b in (ref, per, pg):
+        b.step(1)
+    launches, _, _ = per.sim.profile()
+    assert launches == 1
+    launches_ref, _, _ = ref.sim.profile()
+    assert launches_ref >= 3
+    _same(ref.sim, per.sim)
+    for b in (ref, per, pg):
+        assert b.status() == 0
+        b.close()
+
+
+def test_persistent_barrier_limit_stops_the_step(mods):
+    """The grid barriers wait at most the host-set limit: at 1 ns a block that
+    has to wait gives up at once, the step stops with XDEM_ERR_BARRIER and the
+    kernel returns (no hang).  Restored to a saved state with the default
+    limit, the handle steps as one that never stopped."""
+    batch, _ = mods
+    members = _members()
+    ref = _list_batch(batch, members, persist=True)
+    b = _list_batch(batch, members, persist=True)
+    ref.step(4)
+    b.step(4)
+    st = b.sim.state()
+    prs = [b.sim.pairs(k) for k in range(2)]
+    b.set_persistent(True, 1)
+    b.step(1)
+    assert b.status() & T.XDEM_ERR_BARRIER
+    b.set_persistent(True, 0)
+    mass, inertia = b.combined.mass, b.combined.inertia
+    for h in (ref, b):
+        h.sim.set_state(st["pos"], st["vel"], st["acc"], st["ep"], st["ev"], st["ea"], mass, inertia)
+        for k, pr in enumerate(prs):
+            h.sim.set_pairs(k, *pr)
+        h.step(12)
+    _same(ref.sim, b.sim)
+    assert ref.status() == 0 and b.status() == 0
+    ref.close()
+    b.close()

@@ -76,6 +76,7 @@ _SIGS = {
     "xdem_sim_set_stream": ([vp, vp], i32),
     "xdem_sim_set_profiling": ([vp, i32], i32),
     "xdem_sim_set_graph": ([vp, i32], i32),
+    "xdem_sim_set_persistent": ([vp, i32, C.c_ulonglong], i32),
     "xdem_sim_profile": ([vp, vp, vp, vp], i32),
     "xdem_sim_set_tune": ([vp, vp], i32),
     "xdem_sim_get_tune": ([vp, vp], i32),

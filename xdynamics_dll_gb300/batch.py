@@ -7,7 +7,8 @@ handle over a grid that covers the tiling and declares the scenes with
 xdem_sim_set_scenes: each keeps its own particle-particle material and its
 own planes, and no contact is formed between scenes.  All scenes share the
 time step, gravity and contact model.  A step advances every scene; with
-set_graph(True) the step is replayed from a CUDA graph.
+set_graph(True) the step is replayed from a CUDA graph, and with
+set_persistent(True) a list step is one cooperative kernel launch.
 
 This is the parameter-sweep form: a sweep over friction and restitution is
 one batch whose scenes differ in their contact properties.
@@ -132,6 +133,10 @@ class Batch:
 
     def set_graph(self, on):
         self.sim.set_graph(on)
+
+    def set_persistent(self, on, barrier_limit_ns=0):
+        """One cooperative kernel launch per list step (see Sim.set_persistent)."""
+        self.sim.set_persistent(on, barrier_limit_ns)
 
     def autotune(self, trial_steps=10, cache=None):
         """Block shapes for this batch from the autotuner (or from `cache`,

@@ -104,6 +104,46 @@ struct MixedTune {
 enum { kRecA = 0, kRecL = 1, kRecB = 2, kRecC = 3 };
 __device__ __forceinline__ unsigned int rec_cell(float4 C) { return __float_as_uint(C.w); }
 
+// Cell ranges of the sorted keys (impl:317-360) for sorted entry s with key k.
+__device__ __forceinline__ void cell_bounds(const unsigned int* sk, unsigned int s, unsigned int n,
+                                            unsigned int* cstart, unsigned int* cend, unsigned int k)
+{
+    const unsigned int prev = s ? sk[s - 1] : 0u;
+    if (s == 0 || k != prev) {
+        cstart[k] = s;
+        if (s > 0) cend[prev] = s;
+    }
+    if (s == n - 1) cend[k] = s + 1;
+}
+
+// Mixed form, sorted entry s < n: its cell range bounds, and its FP32
+// records permuted into sorted order (entries >= np, mesh spheres, get an
+// empty record).
+__device__ __forceinline__ void reorder_mixed_entry(unsigned int s, const unsigned int* sk, const unsigned int* sv,
+                                                    unsigned int n, unsigned int np, unsigned int* cstart,
+                                                    unsigned int* cend, unsigned int* sorted_index,
+                                                    unsigned int* skey, const float4* rec, float4* mA, float4* mL,
+                                                    float4* mB, float4* mC, uint2* mIT)
+{
+    const unsigned int k = sk[s];
+    cell_bounds(sk, s, n, cstart, cend, k);
+    const unsigned int oid = sv[s];
+    sorted_index[s] = oid;
+    skey[s] = k;
+    if (oid < np) {
+        const float4* r = rec + 4 * (size_t)oid;
+        mA[s] = r[kRecA];
+        mL[s] = r[kRecL];
+        mB[s] = r[kRecB];
+        const float4 C = r[kRecC];
+        mC[s] = C;
+        mIT[s] = make_uint2(oid, rec_cell(C));
+    } else {
+        mA[s] = make_float4(0.f, 0.f, 0.f, -1.f);
+        mIT[s] = make_uint2(oid, 0xffffffffu);
+    }
+}
+
 // Candidates a sphere's list holds; a sphere with more walks the stencil.
 constexpr unsigned int kListCap = 24;
 // Blocks per body of the wrench reduction.
@@ -157,6 +197,13 @@ struct FusedState {
     float* vl_xb = nullptr;          // [np*4]
     unsigned int* vl_flag = nullptr; // [kVlWords], indices kVl* below
     bool any_coh = false;            // cohesion in a particle-pair material (no lists)
+    // persistent batched step (xdem_sim_set_persistent): on, the grid
+    // barriers' time limit, their two words (arrivals, generation), and the
+    // co-resident grid of each register budget (768 / 1024 threads per SM)
+    bool persist = false;
+    unsigned long long persist_limit_ns = 1000000000ull;
+    unsigned int* d_bar = nullptr;   // [2]
+    unsigned int persist_grid[2] = {0u, 0u};
     // bounding sphere of each mesh (centre relative to the grid origin,
     // radius): a sphere that cannot reach it skips the triangle search
     cudaStream_t side_st = nullptr;  // captures the conditional sort section of a step graph
@@ -382,6 +429,32 @@ __host__ __device__ inline unsigned int scene_index(const ContactLaunch& c, unsi
 
 cudaError_t launch_fused_contact_fp64(const ContactLaunch& c, cudaStream_t st);
 cudaError_t launch_fused_contact_mixed(const ContactLaunch& c, cudaStream_t st);
+
+// The cell sort of a step as the persistent batched step runs it: gated by
+// *gate (rebuild or overflowed list), the clear of last step's cells (when
+// have_prev), the radix passes over (k0, v0) with (k1, v1) as the other
+// buffer, and the reorder into the mixed records; bar and limit_ns: the
+// grid barriers (FusedState::d_bar, persist_limit_ns).
+struct BatchSort {
+    const unsigned int* gate;
+    unsigned int *k0, *v0, *k1, *v1, *hist;
+    unsigned int n, np, bits, ntiles;
+    int have_prev;
+    unsigned int *skey_prev, *cstart, *cend, *sorted_index;
+    const float4* rec;
+    float4 *mA, *mL, *mB, *mC;
+    uint2* mIT;
+    unsigned int* bar;
+    unsigned long long limit_ns;
+};
+// One cooperative launch for a whole list step of a batched mixed handle
+// (sphere scenes, candidate lists): the gated sort, the list pair phase,
+// the body phase and the flag roll, with grid barriers between the phases.
+// occ: 768 or 1024 threads per SM (80 or 64 registers); *grid caches the
+// co-resident grid of that budget (0: not yet known).  Zeroes the barrier
+// words first.
+cudaError_t launch_batch_step(const ContactLaunch& c, const BatchSort& b, unsigned int occ, unsigned int* grid,
+                              cudaStream_t st);
 // The mixed pair kernels' mesh forms and the cluster body kernel
 // (xdem_fused_mixed_mesh.cu, compiled with FMA contraction).
 cudaError_t launch_mixed_mesh_pairs(const ContactLaunch& c, cudaStream_t st);

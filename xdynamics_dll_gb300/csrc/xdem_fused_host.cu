@@ -162,17 +162,6 @@ __global__ void k_bbox(const double* pos, unsigned int n, double* out)
     }
 }
 
-__device__ __forceinline__ void cell_bounds(const unsigned int* sk, unsigned int s, unsigned int n,
-                                            unsigned int* cstart, unsigned int* cend, unsigned int k)
-{
-    const unsigned int prev = s ? sk[s - 1] : 0u;
-    if (s == 0 || k != prev) {
-        cstart[k] = s;
-        if (s > 0) cend[prev] = s;
-    }
-    if (s == n - 1) cend[k] = s + 1;
-}
-
 // FP64 form: cell ranges of the sorted keys (impl:317-360) and the sorted
 // FP64 snapshot, plus an FP32 copy of the position relative to the grid
 // origin for the prefilter.
@@ -220,23 +209,7 @@ __global__ void k_reorder_mixed(const unsigned int* gate, const unsigned int* sk
     if (gate && !*gate) return;
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const unsigned int k = sk[s];
-    cell_bounds(sk, s, n, cstart, cend, k);
-    const unsigned int oid = sv[s];
-    sorted_index[s] = oid;
-    skey[s] = k;
-    if (oid < np) {
-        const float4* r = rec + 4 * (size_t)oid;
-        mA[s] = r[kRecA];
-        mL[s] = r[kRecL];
-        mB[s] = r[kRecB];
-        const float4 C = r[kRecC];
-        mC[s] = C;
-        mIT[s] = make_uint2(oid, rec_cell(C));
-    } else {
-        mA[s] = make_float4(0.f, 0.f, 0.f, -1.f);
-        mIT[s] = make_uint2(oid, 0xffffffffu);
-    }
+    reorder_mixed_entry(s, sk, sv, n, np, cstart, cend, sorted_index, skey, rec, mA, mL, mB, mC, mIT);
 }
 
 // Sum of the contact kernel's per-block wrench partials, kWrenchChunks
@@ -408,6 +381,7 @@ int fused_alloc(FusedState& fs, unsigned int np, unsigned int nentry, bool mixed
         if (e == cudaSuccess) e = dalloc(fs.vl_cnt, np);
         if (e == cudaSuccess) e = dalloc(fs.vl_xb, (size_t)np * 4);
         if (e == cudaSuccess) e = dalloc(fs.vl_flag, kVlWords);
+        if (e == cudaSuccess) e = dalloc(fs.d_bar, 2);
         if (e == cudaSuccess) e = cudaMemsetAsync(fs.vl_flag, 0, kVlWords * sizeof(unsigned int), st);
         // until the handle sets them, every mesh is searched by every sphere
         for (unsigned int m = 0; m < kMaxFusedMeshes; ++m) fs.h_mesh_bs[m] = make_float4(0.f, 0.f, 0.f, 1e18f);
@@ -437,7 +411,7 @@ void fused_free(FusedState& fs)
 {
     void* ps[] = {fs.pos_alt, fs.ep_alt, fs.cpos_alt, fs.snap_pos, fs.snap_vel, fs.snap_om, fs.snap_f, fs.mA, fs.mL, fs.mB,
                   fs.mC, fs.mIT, fs.rec, fs.accf, fs.eaf, fs.jm, fs.fA, fs.fB, fs.fC, fs.pp_count2, fs.pp_id2,
-                  fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag,
+                  fs.pp_tsd2, fs.vl_ids, fs.vl_cnt, fs.vl_xb, fs.vl_flag, fs.d_bar,
                   fs.skey_prev, fs.d_energy, fs.d_bbox, fs.d_planef, fs.d_planedf, fs.d_mpf, fs.wsum, fs.wcnt,
                   fs.d_mesh_bs};
     for (void* q : ps)
@@ -739,6 +713,10 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     // build): the device skips the clear, sort and reorder otherwise.
     const bool use_list = fs.mixed && fs.tune.skin_div != 0 && a.has_pp && !fs.any_coh && fs.vl_flag;
     const unsigned int* sort_gate = use_list ? fs.vl_flag + kVlSort : nullptr;
+    // a batched list step as one persistent launch: the gated sort runs
+    // inside it
+    const bool persist = fs.persist && use_list && a.nscene > 1 && a.nmesh == 0 && !clusters && fs.d_bar;
+    if (!persist) {
     // Captured into a graph, the gated section becomes the body of an IF
     // node whose condition a one-thread kernel sets from the gate, so that
     // between rebuilds the graph skips it instead of launching kernels that
@@ -801,6 +779,8 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
             e = cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies);
         if (e != cudaSuccess) return XDEM_ERR_CUDA;
     }
+    }  // !persist
+    const bool had_prev = fs.have_prev;
     fs.have_prev = true;
 
     ContactLaunch c{};
@@ -884,11 +864,28 @@ int fused_step(FusedState& fs, FusedArgs& a, cudaStream_t st, cudaEvent_t e0, cu
     c.scene_of = c.nscene > 1 ? a.scene_of : nullptr;
     c.scene_plane_first = c.nscene > 1 ? a.scene_plane_first : nullptr;
     if (e0) cudaEventRecord(e0, st);
-    ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
+    if (persist) {
+        BatchSort b{};
+        b.gate = sort_gate;
+        b.k0 = a.k0; b.v0 = a.v0; b.k1 = a.k1; b.v1 = a.v1; b.hist = a.hist;
+        b.n = n; b.np = np; b.bits = (unsigned int)std::max(a.sort_bits, 0);
+        b.ntiles = (n + 2047u) / 2048u;  // the sort's tile: 256 threads x 8 keys
+        b.have_prev = had_prev ? 1 : 0;
+        b.skey_prev = fs.skey_prev; b.cstart = a.cstart; b.cend = a.cend; b.sorted_index = a.sorted_index;
+        b.rec = fs.rec;
+        b.mA = reinterpret_cast<float4*>(fs.mA); b.mL = reinterpret_cast<float4*>(fs.mL);
+        b.mB = reinterpret_cast<float4*>(fs.mB); b.mC = reinterpret_cast<float4*>(fs.mC);
+        b.mIT = reinterpret_cast<uint2*>(fs.mIT);
+        b.bar = fs.d_bar;
+        b.limit_ns = fs.persist_limit_ns;
+        ok(launch_batch_step(c, b, fs.tune.occ_pairs, fs.persist_grid, st));
+    } else {
+        ok(fs.mixed ? launch_fused_contact_mixed(c, st) : launch_fused_contact_fp64(c, st));
+    }
     if (f32_state) fs.f64_stale = true;
     // the mixed contact stage is two kernels (pairs, bodies), with candidate
-    // lists three (list pairs, bodies, flag roll)
-    if (fs.mixed) nl += c.use_list ? 2 : 1;
+    // lists three (list pairs, bodies, flag roll); the persistent step one
+    if (fs.mixed && !persist) nl += c.use_list ? 2 : 1;
     if (e1) cudaEventRecord(e1, st);
     if (a.nbody && c.nscene == 1) {  // batched handles keep no body wrenches
         if (a.nbody > fs.wsum_cap) return XDEM_ERR_ARG;  // fused_set_bodies sizes the chunk sums

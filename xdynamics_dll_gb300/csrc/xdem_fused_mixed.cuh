@@ -1458,15 +1458,17 @@ __device__ __noinline__ WalkOut walk_call(const ContactLaunch* cp, unsigned int 
     return o;
 }
 
-template <bool MESH, unsigned int NT, unsigned int OCC>
-__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
+// Block bx of the list pair kernel (spheres bx * NT ...).  stage: walk
+// fallback candidates or the list's sort keys, old_id: the old pair list,
+// both [slot][thread] with stride NT (kListCap and MAX_P2P_COUNT slots);
+// smf: the mesh wrench partials.  Meshes write their rows at blockIdx.x, so
+// with meshes bx must be blockIdx.x.
+template <bool MESH, unsigned int NT>
+__device__ __forceinline__ void pairs_list_block(const ContactLaunch& c, unsigned int bx, unsigned int* stage,
+                                                 unsigned int* old_id, float* smf)
 {
-    __shared__ float smf[MESH ? (NT / 32) * 6 * 2 : 1];
-    // walk fallback candidates or the list's sort keys, [slot][thread]
-    __shared__ unsigned int stage[kListCap * NT];
-    __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];       // old pair list, [slot][thread]
     const bool rebuild = c.vl_flag[kVlRebuild] != 0u;
-    const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned int oid = bx * NT + threadIdx.x;
     const bool live = oid < c.np;
     if (!MESH && !live) return;
     float4 Ai = make_float4(0.f, 0.f, 0.f, 0.f), Li = Ai, Bi = Ai, Ci = Ai;
@@ -1512,11 +1514,20 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_
     if (bits) atomicOr(c.status, bits);
 }
 
+template <bool MESH, unsigned int NT, unsigned int OCC>
+__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_pairs_list(const __grid_constant__ ContactLaunch c)
+{
+    __shared__ float smf[MESH ? (NT / 32) * 6 * 2 : 1];
+    __shared__ unsigned int stage[kListCap * NT];
+    __shared__ unsigned int old_id[MAX_P2P_COUNT * NT];
+    pairs_list_block<MESH, NT>(c, blockIdx.x, stage, old_id, smf);
+}
+
 // After kernel 2: this step's "moved too far" flag becomes the next step's
 // rebuild flag (a rebuild also clears the overflow mark its build will
 // set again if needed), and the next step's sort is needed on a rebuild or
 // while a list overflowed.
-__global__ void k_vl_roll(unsigned int* flag)
+__device__ __forceinline__ void vl_roll(unsigned int* flag)
 {
     const unsigned int moved = flag[kVlMoved];
     flag[kVlRebuild] = moved;
@@ -1527,6 +1538,7 @@ __global__ void k_vl_roll(unsigned int* flag)
     flag[kVlSort] = moved | flag[kVlOverflow];
     flag[kVlMoved] = 0u;
 }
+__global__ void k_vl_roll(unsigned int* flag) { vl_roll(flag); }
 
 // Kernel 2 of the mixed step: one thread per sphere in original order, so
 // every state array is read and written coalesced.  Plane contact (planes in
@@ -1557,7 +1569,7 @@ __device__ __noinline__ CylsOut cylinders_call(const ContactLaunch* cp, unsigned
         have_bc = true;
     };
     unsigned int cy_cnt = live ? c.cy_count[oid] : 0u;
-    const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
+    const unsigned int wrow = oid >> 5;  // oid = block * NT + thread
     const bool has_row = wrow < (c.nentry + 31u) / 32u;
     float3 xf = make_float3(0.f, 0.f, 0.f);
     if (live) xf = make_float3(d2f_rn(ip.x) - c.o_hi[0], d2f_rn(ip.y) - c.o_hi[1], d2f_rn(ip.z) - c.o_hi[2]);
@@ -1617,10 +1629,11 @@ __device__ __noinline__ CylsOut cylinders_call(const ContactLaunch* cp, unsigned
     return o;
 }
 
-template <unsigned int NT, unsigned int OCC>
-__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
+// Block bx of the sphere body kernel (spheres bx * NT ...).
+template <unsigned int NT>
+__device__ __forceinline__ void bodies_block(const ContactLaunch& c, unsigned int bx)
 {
-    const unsigned int oid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned int oid = bx * NT + threadIdx.x;
     const bool live = oid < c.np;
     // the record's velocity + mass (B) and spin (C) are read only by a sphere
     // that meets a plane or has rolling resistance (one 32-byte sector); the
@@ -1681,7 +1694,7 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
         // wrench partials: one row per warp (no block barrier in the loop);
         // the rows cover ceil(nentry / 32) warps, so a warp made only of the
         // last block's padding threads has no row and writes none
-        const unsigned int wrow = (blockIdx.x * NT + threadIdx.x) >> 5;
+        const unsigned int wrow = oid >> 5;
         const bool has_row = wrow < (c.nentry + 31u) / 32u;
         for (unsigned int k = kbeg; k < kend; ++k) {
             float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1742,6 +1755,12 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     float m;
     const BodyIn in = body_in_f32(c, oid, m);
     mixed_tail(c, oid, ip, rh, d2f_rn(ip.w - f2d(rh)), m, Ff, Mf, bits, in);
+}
+
+template <unsigned int NT, unsigned int OCC>
+__global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_constant__ ContactLaunch c)
+{
+    bodies_block<NT>(c, blockIdx.x);
 }
 
 // Kernel 2 for clusters (impl:817-948, 224-287, 149-190): one thread per

@@ -1049,7 +1049,13 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
                         g = 0;
                     }
                     captured = capture_step_graph(s, g) == XDEM_OK;
-                    if (!captured) g = -1;
+                    if (!captured) {
+                        if (!s->capture_failed_noted)
+                            fprintf(stderr, "xdem_sim_step: the step graph could not be captured; stepping "
+                                            "without it\n");
+                        s->capture_failed_noted = true;
+                        g = -1;
+                    }
                 }
                 if (g >= 0) {
                     const cudaError_t e = cudaGraphLaunch(s->graphs[g].exec, s->st);
@@ -1250,6 +1256,15 @@ XDEM_API int xdem_sim_set_graph(xdem_sim* s, int on)
     if (!s) return XDEM_ERR_ARG;
     s->use_graph = on != 0;
     if (!s->use_graph) drop_graph(s);
+    return XDEM_OK;
+}
+
+XDEM_API int xdem_sim_set_persistent(xdem_sim* s, int on, unsigned long long barrier_limit_ns)
+{
+    if (!s) return XDEM_ERR_ARG;
+    s->fs.persist = on != 0;
+    s->fs.persist_limit_ns = barrier_limit_ns ? barrier_limit_ns : 1000000000ull;
+    drop_graph(s);  // the captured steps bake in the launches and the limit
     return XDEM_OK;
 }
 

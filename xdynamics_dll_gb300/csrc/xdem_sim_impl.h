@@ -107,6 +107,7 @@ struct xdem_sim {
         unsigned int launches = 0;
     };
     bool use_graph = false;
+    bool capture_failed_noted = false;  // a failed step-graph capture is reported once
     StepGraph graphs[2];
     // batched scenes (nscene == 1: one scene)
     unsigned int nscene = 1;

@@ -185,6 +185,14 @@ class Sim:
         """Replay the step from a captured CUDA graph (identical results)."""
         _lib.check(self.L.xdem_sim_set_graph(self.h, int(on)), "xdem_sim_set_graph")
 
+    def set_persistent(self, on, barrier_limit_ns=0):
+        """Batched list steps as one cooperative kernel launch (identical
+        results); each grid barrier waits at most barrier_limit_ns on the
+        GPU's timer (0: one second), past which the step stops with
+        XDEM_ERR_BARRIER in the status."""
+        _lib.check(self.L.xdem_sim_set_persistent(self.h, int(on), int(barrier_limit_ns)),
+                   "xdem_sim_set_persistent")
+
     def set_tune(self, nt_pairs=128, stage=16, nt_bodies=128, occ_pairs=768, occ_bodies=512, skin_div=0):
         """Block shapes and pair search of the mixed contact stage (results do
         not depend on them)."""

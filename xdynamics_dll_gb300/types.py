@@ -25,6 +25,7 @@ XDEM_ERR_P2MS_OVERFLOW = 1 << 2
 XDEM_ERR_TRI_CANDIDATES = 1 << 3
 XDEM_ERR_NONFINITE = 1 << 4
 XDEM_ERR_P2CY_OVERFLOW = 1 << 5
+XDEM_ERR_BARRIER = 1 << 6
 XDEM_ERR_CUDA = 1 << 8
 XDEM_ERR_ARG = 1 << 9
 XDEM_ERR_NOT_SET = 1 << 10
