@@ -423,9 +423,9 @@ XDEM_API int xdem_sim_add_plane(xdem_sim* sim, const device_plane_info* plane,
 /* Adds a cylinder (xParticleCylinderContact): its id is its rank among the
  * handle's cylinders.  Planes come first, then cylinders, then meshes.  An
  * XDEM_FP64 handle with cylinders steps on the FP64 launcher kernels; an
- * XDEM_MIXED sphere handle runs them in its fused step (FP64 region
- * geometry, FP32 forces).  xdem_sim_step returns XDEM_ERR_ARG for a mixed
- * handle with cylinders and clusters, batched scenes, or cohesion in a
+ * XDEM_MIXED handle (spheres or clusters) runs them in its fused step (FP64
+ * region geometry, FP32 forces).  xdem_sim_step returns XDEM_ERR_ARG for a
+ * mixed handle with cylinders and batched scenes, or with cohesion in a
  * cylinder's contact property. */
 XDEM_API int xdem_sim_add_cylinder(xdem_sim* sim, const device_cylinder_info* cyl,
                                    const double body[15],

@@ -285,11 +285,44 @@ def test_mixed_handle_with_cylinder_matches_fp64(simmod):
     b.close()
 
 
-def test_mixed_cluster_handle_with_cylinder_is_refused(simmod):
-    sm = simmod.Sim(drum(n=300, cluster=True), precision=T.XDEM_MIXED)
-    with pytest.raises(Exception):
-        sm.step(1)
-    sm.close()
+def test_mixed_cluster_handle_with_cylinder_matches_fp64(simmod):
+    """The mixed cluster step's cylinder contact (members with their
+    cluster's mass, velocity and spin, moments about the cluster centre)
+    against the FP64 cluster handle on the launcher kernels, on the spinning,
+    drifting drum of three-sphere clusters: after one step the particle-pair
+    and cylinder pair lists are identical, the contact accelerations and
+    Euler-parameter accelerations agree to 1e-4 of the largest and the
+    cylinder's wrench to 1e-4; over 100 steps the kinetic energy to 1e-3."""
+    sc = drum(cluster=True)
+    a = simmod.Sim(sc, precision=T.XDEM_FP64)
+    b = simmod.Sim(sc, precision=T.XDEM_MIXED)
+    a.step(1)
+    b.step(1)
+    assert a.status() == 0 and b.status() == 0
+    sa, sb = a.state(), b.state()
+    g = np.asarray(sc.gravity, dtype=np.float64)
+    fa, fb = sa["acc"].reshape(-1, 3) - g, sb["acc"].reshape(-1, 3) - g
+    assert np.abs(fa - fb).max() <= 1e-4 * np.abs(fa).max()
+    assert np.abs(sa["ea"] - sb["ea"]).max() <= 1e-4 * np.abs(sa["ea"]).max()
+    touched = 0
+    for kind, cap in ((0, 12), (3, 3)):
+        ca, ia, _ = a.pairs(kind)
+        cb, ib, _ = b.pairs(kind)
+        assert kseq.pairs_equal(cb, ib, ca, ia, cap) == sc.np_, kind
+        if kind == 3:
+            touched = int(ca.sum())
+    assert touched > 0
+    wa, wb = a.wrench(a.bodies[0]), b.wrench(b.bodies[0])
+    for part in (slice(0, 3), slice(3, 6)):
+        assert np.abs(wa[part] - wb[part]).max() <= 1e-4 * np.abs(wa[part]).max(), (wa, wb)
+    a.step(99)
+    b.step(99)
+    ka, _ = a.energy()
+    kb, _ = b.energy()
+    assert abs(ka - kb) <= 1e-3 * ka, (ka, kb)
+    assert a.status() == 0 and b.status() == 0
+    a.close()
+    b.close()
 
 
 @pytest.mark.parametrize("nt", [64, 128, 256])

@@ -1763,6 +1763,78 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_bodies(const __grid_cons
     bodies_block<NT>(c, blockIdx.x);
 }
 
+// The cluster body kernel's cylinder loop behind a call boundary (its
+// geometry would otherwise raise the allocation of the whole kernel, also
+// for scenes without cylinders).  Each member against each cylinder with its
+// cluster's mass, velocity and spin, as k_cylinder<true> (xdem_kernels.cu):
+// the member's rigid velocity vc + om x d makes the contact-point velocity
+// vc + om x (cpt - x_c), and m + d x f is the moment about the cluster
+// centre.  A member's count carries over from cylinder to cylinder;
+// cylinder 0 restarts it.  The cluster's running sums come in and go out by
+// value, so every addition happens in the same order as inline.  Every
+// thread of the block calls it (block wrench rows).
+struct ClusterSums {
+    CSum F[3], M[3];
+    unsigned int bits;
+};
+__device__ __noinline__ ClusterSums cluster_cylinders_call(const ContactLaunch* cp, unsigned int cid, bool live, d4 xc,
+                                                           V3<float> vc, V3<float> om, float m, ClusterSums acc,
+                                                           float* smf)
+{
+    const ContactLaunch& c = *cp;
+    const unsigned int ne = c.cl.neach;
+    const df xcd[3] = {split_d(xc.x), split_d(xc.y), split_d(xc.z)};
+    for (unsigned int k = 0; k < c.ncyl; ++k) {
+        float f6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        bool touched = false;
+        const device_cylinder_info& cy = c.cyl[k];
+        const double* bi = c.body + 15 * (c.nplane + k);
+        for (unsigned int j = 0; live && j < ne; ++j) {
+            const unsigned int id = cid * ne + j;
+            const d4 ip = ld4(c.pos_cur, id);
+            unsigned int cnt = c.cy_count[id];
+            // conservative FP32 test: every region lies within the sphere
+            // around the middle of the axis through the rims and the wall
+            const float4 e = make_float4(d2f_rn(bi[XDEM_E0]), d2f_rn(bi[XDEM_E1]), d2f_rn(bi[XDEM_E2]),
+                                         d2f_rn(bi[XDEM_E3]));
+            const float hx = 0.5f * (float)(cy.pbase.x + cy.ptop.x), hy = 0.5f * (float)(cy.pbase.y + cy.ptop.y),
+                        hz = 0.5f * (float)(cy.pbase.z + cy.ptop.z);
+            const float ax = (float)(cy.ptop.x - cy.pbase.x), ay = (float)(cy.ptop.y - cy.pbase.y),
+                        az = (float)(cy.ptop.z - cy.pbase.z);
+            const float half = 0.5f * sqrtf(ax * ax + ay * ay + az * az) + (float)cy.thickness;
+            const float rad = fmaxf((float)cy.len_rr.y, (float)cy.len_rr.z) + (float)cy.thickness;
+            const float3 mid = to_global_f(make_float3(hx, hy, hz), e);
+            const float dx = (d2f_rn(ip.x) - c.o_hi[0]) - (d2f_rn(bi[XDEM_PX]) - c.o_hi[0] + mid.x);
+            const float dy = (d2f_rn(ip.y) - c.o_hi[1]) - (d2f_rn(bi[XDEM_PY]) - c.o_hi[1] + mid.y);
+            const float dz = (d2f_rn(ip.z) - c.o_hi[2]) - (d2f_rn(bi[XDEM_PZ]) - c.o_hi[2] + mid.z);
+            const float lim = sqrtf(half * half + rad * rad) * (1.f + 1e-5f) + d2f_rn(ip.w) + c.margin;
+            if (dx * dx + dy * dy + dz * dz <= lim * lim) {
+                const V3<float> d = v3<float>(df_f(df_sub(split_d(ip.x), xcd[0])), df_f(df_sub(split_d(ip.y), xcd[1])),
+                                              df_f(df_sub(split_d(ip.z), xcd[2])));
+                const V3<float> vm = vc + tcross(om, d);
+                const PlaneOut o = cyl_call(&c, k, id, ip, make_float4(vm.x, vm.y, vm.z, m),
+                                            make_float4(om.x, om.y, om.z, 0.f), cnt);
+                acc.bits |= o.bits;
+                cnt = o.cnt;
+                if (o.touched) {
+                    const V3<float> f = v3<float>(o.f[0], o.f[1], o.f[2]);
+                    const V3<float> t = v3<float>(o.m[0], o.m[1], o.m[2]) + tcross(d, f);
+                    acc.F[0].add(f.x); acc.F[1].add(f.y); acc.F[2].add(f.z);
+                    acc.M[0].add(t.x); acc.M[1].add(t.y); acc.M[2].add(t.z);
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) f6[q] += o.w[q];
+                    touched = true;
+                }
+            } else if (cy.id == 0) {
+                cnt = 0;  // cylinder 0 restarts the list whether or not it is touched
+            }
+            c.cy_count[id] = cnt;
+        }
+        emit_body_f(f6, touched, c.bsums + ((size_t)(c.nplane + k) * c.nblocks + blockIdx.x) * 6, smf);
+    }
+    return acc;
+}
+
 // Kernel 2 for clusters (impl:817-948, 224-287, 149-190): one thread per
 // cluster.  The cluster's force is the sum of its members' particle-pair and
 // plane forces, its moment the sum of the members' moments about their
@@ -1841,6 +1913,22 @@ __global__ void __launch_bounds__(NT, OCC / NT) k_mixed_cluster_bodies(const __g
             }
             emit_body_f(f6, touched, c.bsums + ((size_t)k * c.nblocks + blockIdx.x) * 6, smf);
         }
+    }
+
+    // ------------------------------------------------ cylinders in id order (impl:1324-1601)
+    if (c.ncyl) {
+        ClusterSums cs;
+        for (int i = 0; i < 3; ++i) {
+            cs.F[i] = F[i];
+            cs.M[i] = M[i];
+        }
+        cs.bits = bits;
+        cs = cluster_cylinders_call(&c, cid, live, xc, vc, om, m, cs, smf);
+        for (int i = 0; i < 3; ++i) {
+            F[i] = cs.F[i];
+            M[i] = cs.M[i];
+        }
+        bits = cs.bits;
     }
     if (!live) return;
 

@@ -350,12 +350,12 @@ PairTables pair_tables(xdem_sim* s, int kind)
 
 // Steps run on the fused step (sphere scenes of either precision, and
 // mixed cluster scenes) unless the launcher path was asked for; an FP64
-// scene with cylinders runs the launcher kernels, a mixed sphere scene with
-// cylinders the fused step's cylinder loop.
+// scene with cylinders runs the launcher kernels, a mixed scene with
+// cylinders (spheres or clusters) the fused step's cylinder loops.
 bool fused_path(const xdem_sim* s)
 {
     if (s->cfg.launcher_path || (s->clusters && !s->precision_mixed())) return false;
-    return s->cylinders.empty() || (s->precision_mixed() && !s->clusters);
+    return s->cylinders.empty() || s->precision_mixed();
 }
 
 // The particle-pair tangential history of a mixed handle on the fused step
@@ -998,10 +998,10 @@ XDEM_API int xdem_sim_step(xdem_sim* s, unsigned int nsteps)
 {
     if (!s) return XDEM_ERR_ARG;
     if (s->clusters && !s->xci) return XDEM_ERR_ARG;
-    // cylinders in the mixed form: sphere scenes, one scene, no cohesion in
-    // a cylinder's material (FP64 handles run them on the launcher kernels)
+    // cylinders in the mixed form: one scene, no cohesion in a cylinder's
+    // material (FP64 handles run them on the launcher kernels)
     if (!s->cylinders.empty() && s->precision_mixed()) {
-        if (s->clusters || s->nscene > 1) return XDEM_ERR_ARG;
+        if (s->nscene > 1) return XDEM_ERR_ARG;
         for (size_t k = 0; k < s->cylinders.size(); ++k)
             if (s->body_cp[s->planes.size() + k].coh != 0.0) return XDEM_ERR_ARG;
     }
