@@ -11,7 +11,6 @@ scene's energy from xdem_sim_scene_energy must match the scene run alone.
 import numpy as np
 import pytest
 
-import kseq
 from xdynamics_dll_gb300 import scenes, types as T
 
 pytestmark = pytest.mark.gpu
